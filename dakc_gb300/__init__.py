@@ -1,0 +1,242 @@
+"""dakc_gb300 -- GB300-native k-mer counting, a drop-in for DAKC's counting path.
+
+The engine is native code (``_build/libdakc_gb300.so``: sm_103a CUDA kernels
+and a C++ host pipeline behind the C ABI of ``include/dakc_gb300.h``).  This
+module is a thin ctypes mirror of that ABI for Python callers, tests and the
+benchmark.  There is no CPU fallback: loading fails loudly when the library
+is missing, and counting fails with ``DkError`` when no GPU is usable.
+
+DAKC's counter is ``kmercounter(read_chunk, vectordbg)``
+(dakc/src/kcounter/kcounter.hpp:84-99): k and the line width are compile-time
+there (KMERLEN, READLEN) and the table is left in the member ``lightdbg``.
+``Engine.count(text, line_width, k)`` takes the same read buffer and returns
+the same table, globally sorted: ``(kmers uint64[n], counts uint32[n],
+n_kmers)``.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libdakc_gb300.so")
+
+DK_OK = 0
+DK_ERR_INVALID_ARG = -1
+DK_ERR_OOM = -2
+DK_ERR_COUNT_OVERFLOW = -3
+DK_ERR_CUDA = -4
+DK_ERR_TIMEOUT = -5
+DK_ERR_ADMISSION = -6
+DK_ERR_PENDING = -7
+DK_ERR_NOT_FOUND = -8
+DK_ERR_CANCELLED = -9
+DK_ERR_NO_DEVICE = -10
+
+VARIANT_AUTO, VARIANT_SORT, VARIANT_HASH = 0, 1, 2
+RESIDENT_HOST, RESIDENT_DEVICE = 0, 1
+CONV_DAKC = 0
+
+# exported symbols, in the order include/dakc_gb300.h declares them
+ABI_SYMBOLS = [
+    "dk_create", "dk_destroy", "dk_strerror", "dk_last_error_string", "dk_abi_version",
+    "dk_count", "dk_count_device", "dk_table_free", "dk_last_stats", "dk_num_lines",
+    "dk_host_alloc", "dk_host_free",
+]
+
+
+class DkError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"{msg} (status {status})")
+        self.status = status
+
+
+class Config(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_int), ("reserved0", ctypes.c_int),
+                ("mem_budget", ctypes.c_uint64), ("flags", ctypes.c_uint64)]
+
+
+class InputDesc(ctypes.Structure):
+    _fields_ = [("line_width", ctypes.c_int), ("k", ctypes.c_int), ("convention", ctypes.c_int),
+                ("variant", ctypes.c_int), ("residency", ctypes.c_int),
+                ("reserved", ctypes.c_int * 3)]
+
+
+class Table(ctypes.Structure):
+    _fields_ = [("kmers", ctypes.POINTER(ctypes.c_uint64)),
+                ("counts", ctypes.POINTER(ctypes.c_uint32)),
+                ("n", ctypes.c_uint64), ("n_kmers", ctypes.c_uint64),
+                ("on_device", ctypes.c_int), ("variant_used", ctypes.c_int),
+                ("handle", ctypes.c_uint64)]
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [("ms_device", ctypes.c_double), ("ms_h2d", ctypes.c_double),
+                ("ms_d2h", ctypes.c_double), ("ms_wall", ctypes.c_double),
+                ("ms_stage", ctypes.c_double * 8),
+                ("n_kmers", ctypes.c_uint64), ("n_distinct", ctypes.c_uint64),
+                ("n_lines", ctypes.c_uint64), ("kernel_launches", ctypes.c_uint64),
+                ("dev_bytes_peak", ctypes.c_uint64), ("variant_used", ctypes.c_int),
+                ("partition_levels", ctypes.c_int), ("n_bins", ctypes.c_uint64)]
+
+    def as_dict(self) -> dict:
+        d = {f: getattr(self, f) for f, _ in self._fields_ if f != "ms_stage"}
+        d["ms_stage"] = list(self.ms_stage)
+        return d
+
+
+_lib = None
+
+
+def load_library(path: str = LIB_PATH):
+    """Load the engine library (build it first if it is absent and nvcc exists)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        from . import build as _b
+        _b.build_engine()
+    lib = ctypes.CDLL(path)
+    vp, u64, i32 = ctypes.c_void_p, ctypes.c_uint64, ctypes.c_int
+    lib.dk_create.argtypes = [ctypes.POINTER(Config), ctypes.POINTER(vp)]
+    lib.dk_destroy.argtypes = [vp]
+    lib.dk_strerror.argtypes = [i32]
+    lib.dk_strerror.restype = ctypes.c_char_p
+    lib.dk_last_error_string.argtypes = [vp]
+    lib.dk_last_error_string.restype = ctypes.c_char_p
+    lib.dk_count.argtypes = [vp, vp, u64, ctypes.POINTER(InputDesc), ctypes.POINTER(Table)]
+    lib.dk_count_device.argtypes = [vp, vp, u64, ctypes.POINTER(InputDesc), ctypes.POINTER(Table)]
+    lib.dk_table_free.argtypes = [vp, ctypes.POINTER(Table)]
+    lib.dk_last_stats.argtypes = [vp, ctypes.POINTER(Stats)]
+    lib.dk_num_lines.argtypes = [vp, u64, i32]
+    lib.dk_num_lines.restype = ctypes.c_int64
+    lib.dk_host_alloc.argtypes = [u64, ctypes.POINTER(vp)]
+    lib.dk_host_free.argtypes = [vp]
+    _lib = lib
+    return lib
+
+
+def _buf_ptr(text) -> tuple[int, int, object]:
+    if isinstance(text, (bytes, bytearray)):
+        arr = np.frombuffer(bytes(text), dtype=np.uint8)
+    else:
+        arr = np.ascontiguousarray(text, dtype=np.uint8)
+    return arr.ctypes.data, arr.size, arr
+
+
+@dataclass
+class CountResult:
+    kmers: np.ndarray   # uint64, ascending
+    counts: np.ndarray  # uint32
+    n_kmers: int
+    variant: int
+
+
+class PinnedBuffer:
+    """Page-locked host bytes from the engine (cudaMallocHost); numpy view in .array."""
+
+    def __init__(self, nbytes: int):
+        lib = load_library()
+        p = ctypes.c_void_p()
+        rc = lib.dk_host_alloc(max(1, nbytes), ctypes.byref(p))
+        if rc != DK_OK:
+            raise DkError(rc, "dk_host_alloc failed")
+        self._p = p
+        self.nbytes = nbytes
+        buf = (ctypes.c_uint8 * max(1, nbytes)).from_address(p.value)
+        self.array = np.frombuffer(buf, dtype=np.uint8, count=nbytes)
+
+    @property
+    def ptr(self) -> int:
+        return self._p.value
+
+    def free(self):
+        if self._p:
+            load_library().dk_host_free(self._p)
+            self._p = None
+            self.array = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+class Engine:
+    """One engine context: a CUDA stream, its device arenas and table pool."""
+
+    def __init__(self, device: int = 0, mem_budget: int = 0):
+        self.lib = load_library()
+        cfg = Config(device, 0, mem_budget, 0)
+        h = ctypes.c_void_p()
+        rc = self.lib.dk_create(ctypes.byref(cfg), ctypes.byref(h))
+        if rc != DK_OK:
+            raise DkError(rc, "dk_create: " + self.lib.dk_strerror(rc).decode())
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.dk_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc: int, what: str):
+        if rc != DK_OK:
+            msg = self.lib.dk_last_error_string(self.h).decode()
+            raise DkError(rc, f"{what}: {self.lib.dk_strerror(rc).decode()}: {msg}")
+
+    @staticmethod
+    def desc(line_width: int, k: int, variant: int = VARIANT_AUTO,
+             residency: int = RESIDENT_HOST) -> InputDesc:
+        return InputDesc(line_width, k, CONV_DAKC, variant, residency)
+
+    def count_raw(self, ptr: int, nbytes: int, d: InputDesc, on_device: bool = False) -> Table:
+        t = Table()
+        fn = self.lib.dk_count_device if on_device else self.lib.dk_count
+        self._check(fn(self.h, ctypes.c_void_p(ptr), nbytes, ctypes.byref(d), ctypes.byref(t)),
+                    "dk_count")
+        return t
+
+    def free_table(self, t: Table):
+        self._check(self.lib.dk_table_free(self.h, ctypes.byref(t)), "dk_table_free")
+
+    def count(self, text, line_width: int, k: int, variant: int = VARIANT_AUTO) -> CountResult:
+        """Count the k-mers of `text` (bytes or uint8 array of DAKC lines)."""
+        ptr, n, keep = _buf_ptr(text)
+        t = self.count_raw(ptr, n, self.desc(line_width, k, variant))
+        try:
+            nd = int(t.n)
+            if nd:
+                kmers = np.ctypeslib.as_array(t.kmers, shape=(nd,)).copy()
+                counts = np.ctypeslib.as_array(t.counts, shape=(nd,)).copy()
+            else:
+                kmers, counts = np.zeros(0, np.uint64), np.zeros(0, np.uint32)
+            return CountResult(kmers, counts, int(t.n_kmers), int(t.variant_used))
+        finally:
+            self.free_table(t)
+            del keep
+
+    def stats(self) -> dict:
+        s = Stats()
+        self._check(self.lib.dk_last_stats(self.h, ctypes.byref(s)), "dk_last_stats")
+        return s.as_dict()
+
+
+def num_lines(text, line_width: int) -> int:
+    ptr, n, keep = _buf_ptr(text)
+    return int(load_library().dk_num_lines(ctypes.c_void_p(ptr), n, line_width))

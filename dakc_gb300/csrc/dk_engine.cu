@@ -1,0 +1,632 @@
+// Host side of the k-mer counting engine: context, device arenas, the
+// stream-ordered pipeline and the C ABI declared in include/dakc_gb300.h.
+//
+// The reference's entry point is the kmercounter constructor
+// (dakc/src/kcounter/kcounter.hpp:84-99 -> perform_kcount, kcounter.cpp:247-507);
+// dk_count is its one-GPU replacement.  Every stage of the reference maps to
+// kernels launched here on the context's stream:
+//   read_till_buf_max + get_kmers + owner_pe + send   -> l1_count, l1_scatter
+//   (kcounter_funcs.cpp:25-111, kcounter.cpp:29-54,146-300)
+//   ska_sort + run-length reduce (kcounter.cpp:385-414) -> partition levels +
+//                                                         bin_count + compact
+#include "dk_internal.cuh"
+#include "dk_engine.hpp"
+#include "../../include/dakc_gb300.h"
+
+#include <cuda_runtime.h>
+#include <algorithm>
+#include <chrono>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+namespace dk {
+
+// --------------------------------------------------------------- helpers
+static int ceil_log2(uint64_t x) {
+  int b = 0;
+  while ((1ull << b) < x && b < 63) ++b;
+  return b;
+}
+
+int Arena::ensure(Engine* e, DevBuf& b, size_t bytes) {
+  if (b.cap >= bytes) return DK_OK;
+  const size_t want = std::max(bytes, b.cap + b.cap / 4);  // grow geometrically
+  if (b.p) {
+    cudaFree(b.p);
+    e->dev_bytes -= b.cap;
+    b.p = nullptr;
+    b.cap = 0;
+  }
+  if (e->budget && e->dev_bytes + want > e->budget) {
+    if (e->dev_bytes + bytes > e->budget) return DK_ERR_ADMISSION;
+  }
+  size_t got = want;
+  if (e->budget && e->dev_bytes + got > e->budget) got = bytes;
+  cudaError_t st = cudaMalloc(&b.p, got);
+  if (st != cudaSuccess && got != bytes) {
+    cudaGetLastError();
+    got = bytes;
+    st = cudaMalloc(&b.p, got);
+  }
+  if (st != cudaSuccess) {
+    cudaGetLastError();
+    b.p = nullptr;
+    return DK_ERR_OOM;
+  }
+  b.cap = got;
+  e->dev_bytes += got;
+  e->dev_peak = std::max(e->dev_peak, e->dev_bytes);
+  return DK_OK;
+}
+
+void Arena::release(Engine* e, DevBuf& b) {
+  if (b.p) {
+    cudaFree(b.p);
+    e->dev_bytes -= b.cap;
+  }
+  b.p = nullptr;
+  b.cap = 0;
+}
+
+#define DK_CUDA(call)                                                        \
+  do {                                                                       \
+    cudaError_t _e = (call);                                                 \
+    if (_e != cudaSuccess) {                                                 \
+      e->set_error(std::string(#call) + ": " + cudaGetErrorString(_e));     \
+      return DK_ERR_CUDA;                                                    \
+    }                                                                        \
+  } while (0)
+
+#define DK_TRY(expr)            \
+  do {                          \
+    int _rc = (expr);           \
+    if (_rc != DK_OK) return _rc; \
+  } while (0)
+
+void Engine::set_error(const std::string& m) { last_error = m; }
+
+int Engine::init(const dk_config* cfg) {
+  Engine* e = this;
+  device = cfg ? cfg->device : 0;
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n <= device) {
+    cudaGetLastError();
+    set_error("no CUDA device");
+    return DK_ERR_NO_DEVICE;
+  }
+  DK_CUDA(cudaSetDevice(device));
+  cudaDeviceProp p;
+  DK_CUDA(cudaGetDeviceProperties(&p, device));
+  sm_count = p.multiProcessorCount;
+  if (p.major * 10 + p.minor < 100) {
+    set_error("engine is built for sm_103a; device is older");
+    return DK_ERR_NO_DEVICE;
+  }
+  size_t fr = 0, tot = 0;
+  DK_CUDA(cudaMemGetInfo(&fr, &tot));
+  budget = (cfg && cfg->mem_budget) ? cfg->mem_budget : (uint64_t)(0.8 * (double)fr);
+  DK_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+  for (auto& ev : ev_stage) DK_CUDA(cudaEventCreate(&ev));
+  DK_CUDA(cudaEventCreate(&ev_h2d0));
+  DK_CUDA(cudaEventCreate(&ev_d2h1));
+  DK_CUDA(cudaMallocHost(&h_scratch, 256));
+  return DK_OK;
+}
+
+Engine::~Engine() {
+  if (stream) cudaStreamSynchronize(stream);
+  for (DevBuf* b : {&text, &keysA, &keysB, &cnt, &H, &O, &nodes, &tiles, &TH, &finals, &ctrs})
+    Arena::release(this, *b);
+  for (auto& t : tables) {
+    if (t.on_device) {
+      cudaFree(t.k);
+      cudaFree(t.c);
+    } else {
+      cudaFreeHost(t.k);
+      cudaFreeHost(t.c);
+    }
+  }
+  for (auto& ev : ev_stage)
+    if (ev) cudaEventDestroy(ev);
+  if (ev_h2d0) cudaEventDestroy(ev_h2d0);
+  if (ev_d2h1) cudaEventDestroy(ev_d2h1);
+  if (h_scratch) cudaFreeHost(h_scratch);
+  for (auto& s : stage_pinned)
+    if (s) cudaFreeHost(s);
+  if (stream) cudaStreamDestroy(stream);
+}
+
+int Engine::sync_read(const void* dsrc, size_t bytes, void* hdst) {
+  Engine* e = this;
+  DK_CUDA(cudaMemcpyAsync(h_scratch, dsrc, bytes, cudaMemcpyDeviceToHost, stream));
+  DK_CUDA(cudaStreamSynchronize(stream));
+  std::memcpy(hdst, h_scratch, bytes);
+  return DK_OK;
+}
+
+// framing: lines in a buffer of nbytes (host-side part; NUL lines are found on device)
+int64_t frame_lines(uint64_t nbytes, int W) {
+  if (W < 1) return DK_ERR_INVALID_ARG;
+  if (nbytes == 0) return 0;
+  const uint64_t stride = (uint64_t)W + 1;
+  const uint64_t rem = nbytes % stride;
+  if (rem != 0 && rem != (uint64_t)W) return DK_ERR_INVALID_ARG;
+  return (int64_t)((nbytes + 1) / stride);
+}
+
+// Table storage: a pool of allocations reused across calls (pinned host or device).
+int Engine::acquire_table(uint64_t n, bool on_device, TableBuf** out) {
+  Engine* e = this;
+  TableBuf* best = nullptr;
+  for (auto& t : tables)
+    if (!t.in_use && t.on_device == on_device && t.cap >= n && (!best || t.cap < best->cap)) best = &t;
+  if (!best) {
+    TableBuf t;
+    t.on_device = on_device;
+    t.cap = std::max<uint64_t>(n, 1);
+    if (on_device) {
+      if (budget && dev_bytes + t.cap * 12 > budget) return DK_ERR_ADMISSION;
+      if (cudaMalloc(&t.k, t.cap * 8) != cudaSuccess || cudaMalloc(&t.c, t.cap * 4) != cudaSuccess) {
+        cudaGetLastError();
+        if (t.k) cudaFree(t.k);
+        return DK_ERR_OOM;
+      }
+      dev_bytes += t.cap * 12;
+      dev_peak = std::max(dev_peak, dev_bytes);
+    } else {
+      if (cudaMallocHost(&t.k, t.cap * 8) != cudaSuccess ||
+          cudaMallocHost(&t.c, t.cap * 4) != cudaSuccess) {
+        cudaGetLastError();
+        if (t.k) cudaFreeHost(t.k);
+        return DK_ERR_OOM;
+      }
+    }
+    t.id = ++table_ids;
+    tables.push_back(t);
+    best = &tables.back();
+  }
+  best->in_use = true;
+  *out = best;
+  (void)e;
+  return DK_OK;
+}
+
+int Engine::release_table(uint64_t id) {
+  for (auto& t : tables)
+    if (t.id == id && t.in_use) {
+      t.in_use = false;
+      return DK_OK;
+    }
+  return DK_ERR_NOT_FOUND;
+}
+
+// Copy host reads into device memory: one async copy when the buffer is
+// pinned, else through two pinned staging slots so host memcpy overlaps the
+// previous slot's DMA.
+int Engine::upload(const char* h, uint64_t nbytes, uint8_t* d) {
+  Engine* e = this;
+  cudaPointerAttributes at;
+  bool pinned = false;
+  if (cudaPointerGetAttributes(&at, h) == cudaSuccess)
+    pinned = (at.type == cudaMemoryTypeHost);
+  cudaGetLastError();
+  if (pinned) {
+    DK_CUDA(cudaMemcpyAsync(d, h, nbytes, cudaMemcpyHostToDevice, stream));
+    return DK_OK;
+  }
+  const size_t slot = 64ull << 20;
+  for (int i = 0; i < 2; ++i) {
+    if (!stage_pinned[i]) DK_CUDA(cudaMallocHost(&stage_pinned[i], slot));
+    if (!stage_ev[i]) DK_CUDA(cudaEventCreateWithFlags(&stage_ev[i], cudaEventDisableTiming));
+  }
+  uint64_t off = 0;
+  int i = 0;
+  bool used[2] = {false, false};
+  while (off < nbytes) {
+    const size_t len = (size_t)std::min<uint64_t>(slot, nbytes - off);
+    if (used[i]) DK_CUDA(cudaEventSynchronize(stage_ev[i]));
+    std::memcpy(stage_pinned[i], h + off, len);
+    DK_CUDA(cudaMemcpyAsync(d + off, stage_pinned[i], len, cudaMemcpyHostToDevice, stream));
+    DK_CUDA(cudaEventRecord(stage_ev[i], stream));
+    used[i] = true;
+    off += len;
+    i ^= 1;
+  }
+  return DK_OK;
+}
+
+// The device pipeline: reads at d_text (nbytes, padded by >= 64 bytes of
+// readable memory) -> sorted table in out (device).  Fills stats.
+int Engine::count_device(const uint8_t* d_text, uint64_t nbytes, const dk_input_desc& desc,
+                         DeviceTable* out) {
+  Engine* e = this;
+  const int W = desc.line_width, k = desc.k;
+  out->n = 0;
+  out->n_kmers = 0;
+  out->k = nullptr;
+  out->c = nullptr;
+  stats = dk_stats();
+  stats.variant_used = DK_VARIANT_SORT;
+  int64_t L0 = frame_lines(nbytes, W);
+  if (L0 < 0) {
+    set_error("buffer size is not a whole number of lines");
+    return DK_ERR_INVALID_ARG;
+  }
+  uint64_t L = (uint64_t)L0;
+  launches = 0;
+  DK_CUDA(cudaEventRecord(ev_stage[0], stream));
+  const uint64_t per_line = (W >= k) ? (uint64_t)(W - k + 1) : 0;
+  if (L == 0 || per_line == 0) {
+    DK_CUDA(cudaEventRecord(ev_stage[6], stream));
+    DK_CUDA(cudaEventSynchronize(ev_stage[6]));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, ev_stage[0], ev_stage[6]);
+    stats.ms_device = ms;
+    stats.n_lines = L;
+    return DK_OK;
+  }
+  // level-1 fan-out: aim at ~kBinCap/2 keys per final bin after at most one
+  // 8-bit partition level
+  const uint64_t n_upper = L * per_line;
+  const double target = 0.5 * kBinCap;
+  int B1;
+  if ((double)n_upper / 4096.0 <= target)
+    B1 = ceil_log2((uint64_t)((double)n_upper / target) + 1);
+  else
+    B1 = ceil_log2((uint64_t)((double)n_upper / (target * kFanout)) + 1);
+  B1 = std::max(1, std::min(B1, kMaxL1Bits));
+  B1 = std::min(B1, 2 * k);
+  const int F1 = 1 << B1;
+  const int shift1 = 2 * k - B1;
+  const int G = 2 * sm_count;
+
+  ExtractArgs a;
+  a.text = d_text;
+  a.W = W;
+  a.k = k;
+  a.kmask = (~0ull) >> (64 - 2 * k);
+  a.shift1 = shift1;
+  a.F1 = F1;
+
+  DK_TRY(Arena::ensure(this, H, (size_t)G * F1 * 4));
+  DK_TRY(Arena::ensure(this, O, (size_t)G * F1 * 8));
+  DK_TRY(Arena::ensure(this, ctrs, 256));
+  unsigned long long* c64 = (unsigned long long*)ctrs.p;        // [0]=n_kmers [1]=nul [2]=total_d
+  LevelCounters* lc = (LevelCounters*)((char*)ctrs.p + 64);
+  int* overflow = (int*)((char*)ctrs.p + 128);
+
+  uint64_t n_kmers = 0;
+  for (int attempt = 0; attempt < 2; ++attempt) {
+    a.n_lines = L;
+    DK_CUDA(cudaMemsetAsync(ctrs.p, 0, 256, stream));
+    launches += launch_l1_count(a, G, (uint32_t*)H.p, c64, stream);
+    uint64_t hc[2];
+    DK_TRY(sync_read(c64, 16, hc));
+    if (hc[1] == 0) {
+      n_kmers = hc[0];
+      break;
+    }
+    L = L - hc[1];  // first line whose first byte is NUL
+  }
+  stats.n_lines = L;
+  DK_CUDA(cudaEventRecord(ev_stage[1], stream));
+  if (n_kmers == 0) {
+    DK_CUDA(cudaEventRecord(ev_stage[6], stream));
+    DK_CUDA(cudaEventSynchronize(ev_stage[6]));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, ev_stage[0], ev_stage[6]);
+    stats.ms_device = ms;
+    return DK_OK;
+  }
+  // level-1 nodes and offsets
+  node_cap_needed = (size_t)F1;
+  DK_TRY(Arena::ensure(this, nodes, node_cap_needed * sizeof(Node)));
+  launches += launch_l1_scan((uint32_t*)H.p, G, F1, (uint64_t*)O.p, (Node*)nodes.p, shift1, stream);
+  DK_TRY(Arena::ensure(this, keysA, n_kmers * 8));
+  DK_TRY(Arena::ensure(this, keysB, n_kmers * 8));
+  DK_TRY(Arena::ensure(this, cnt, n_kmers * 4));
+  launches += launch_l1_scatter(a, G, (const uint64_t*)O.p, (uint64_t*)keysA.p, stream);
+  DK_CUDA(cudaEventRecord(ev_stage[2], stream));
+
+  // partition levels
+  std::vector<std::pair<uint32_t, uint32_t>> levels;  // node ranges per level
+  uint32_t lo = 0, hi = (uint32_t)F1;
+  DK_TRY(Arena::ensure(this, finals, (size_t)hi * 4));
+  for (int lvl = 0; lvl < 16; ++lvl) {
+    levels.emplace_back(lo, hi);
+    // the final list can grow by at most this level's node count
+    uint32_t hc[8];
+    DK_TRY(sync_read(lc, 32, hc));
+    const uint32_t n_final_so_far = hc[0];
+    {
+      // finals must hold n_final_so_far + (hi - lo)
+      DevBuf& f = finals;
+      const size_t need = ((size_t)n_final_so_far + (hi - lo)) * 4;
+      if (f.cap < need) {
+        DevBuf nb;
+        DK_TRY(Arena::ensure(this, nb, need));
+        if (n_final_so_far)
+          DK_CUDA(cudaMemcpyAsync(nb.p, f.p, (size_t)n_final_so_far * 4, cudaMemcpyDeviceToDevice, stream));
+        Arena::release(this, f);
+        f = nb;
+      }
+    }
+    DK_CUDA(cudaMemsetAsync((char*)lc + 4, 0, 28, stream));  // keep n_final
+    launches += launch_classify((Node*)nodes.p, lo, hi, (uint32_t*)finals.p, lc, kBinCap, stream);
+    DK_TRY(sync_read(lc, 32, hc));
+    const uint32_t n_split = hc[1], n_tiles = hc[2];
+    if (hc[3]) {
+      set_error("a partition node holds >= 2^32 keys");
+      return DK_ERR_INVALID_ARG;
+    }
+    if (n_split == 0) break;
+    // grow node storage for the children (copying existing nodes)
+    const size_t need_nodes = (size_t)hi + (size_t)n_split * kFanout;
+    if (nodes.cap < need_nodes * sizeof(Node)) {
+      DevBuf nb;
+      DK_TRY(Arena::ensure(this, nb, need_nodes * sizeof(Node)));
+      DK_CUDA(cudaMemcpyAsync(nb.p, nodes.p, (size_t)hi * sizeof(Node), cudaMemcpyDeviceToDevice, stream));
+      Arena::release(this, nodes);
+      nodes = nb;
+    }
+    DK_TRY(Arena::ensure(this, tiles, (size_t)n_tiles * sizeof(Tile)));
+    DK_TRY(Arena::ensure(this, TH, (size_t)n_tiles * kFanout * 4));
+    launches += launch_assign((Node*)nodes.p, lo, hi, hi, (Tile*)tiles.p, lc, stream);
+    launches += launch_tile_hist((Node*)nodes.p, (Tile*)tiles.p, n_tiles, (uint64_t*)keysA.p,
+                                 (uint64_t*)keysB.p, (uint32_t*)TH.p, stream);
+    launches += launch_node_scan((Node*)nodes.p, lo, hi, (Tile*)tiles.p, (uint32_t*)TH.p, stream);
+    launches += launch_tile_scatter((Node*)nodes.p, (Tile*)tiles.p, n_tiles, (uint64_t*)keysA.p,
+                                    (uint64_t*)keysB.p, (uint32_t*)TH.p, stream);
+    lo = hi;
+    hi = hi + n_split * kFanout;
+  }
+  stats.partition_levels = (int)levels.size();
+  DK_CUDA(cudaEventRecord(ev_stage[3], stream));
+  uint32_t hc[8];
+  DK_TRY(sync_read(lc, 32, hc));
+  const uint32_t n_final = hc[0];
+  stats.n_bins = n_final;
+  launches += launch_bin_count((Node*)nodes.p, (uint32_t*)finals.p, n_final, (uint64_t*)keysA.p,
+                               (uint64_t*)keysB.p, (uint32_t*)cnt.p, desc.variant, overflow, stream);
+  DK_CUDA(cudaEventRecord(ev_stage[4], stream));
+  // distinct counts up the tree, offsets down
+  for (int l = (int)levels.size() - 2; l >= 0; --l)
+    launches += launch_aggregate((Node*)nodes.p, levels[l].first, levels[l].second, stream);
+  launches += launch_l1_offsets((Node*)nodes.p, (uint32_t)F1, c64 + 2, stream);
+  for (size_t l = 0; l + 1 < levels.size(); ++l)
+    launches += launch_child_offsets((Node*)nodes.p, levels[l].first, levels[l].second, stream);
+  uint64_t tail[2];
+  DK_TRY(sync_read(c64 + 2, 16, tail));
+  const uint64_t n_distinct = tail[0];
+  int ovf = 0;
+  DK_TRY(sync_read(overflow, 4, &ovf));
+  if (ovf) {
+    set_error("a k-mer count does not fit 32 bits");
+    return DK_ERR_COUNT_OVERFLOW;
+  }
+  out->n = n_distinct;
+  out->n_kmers = n_kmers;
+  out->k = out_k;
+  out->c = out_c;
+  if (!out->k || !out->c) {
+    set_error("internal: no output buffers");
+    return DK_ERR_INVALID_ARG;
+  }
+  launches += launch_compact((Node*)nodes.p, (uint32_t*)finals.p, n_final, (uint64_t*)keysA.p,
+                             (uint64_t*)keysB.p, (uint32_t*)cnt.p, out_k, out_c, stream);
+  DK_CUDA(cudaGetLastError());
+  DK_CUDA(cudaEventRecord(ev_stage[5], stream));
+  DK_CUDA(cudaEventSynchronize(ev_stage[5]));
+  float ms = 0;
+  cudaEventElapsedTime(&ms, ev_stage[0], ev_stage[5]);
+  stats.ms_device = ms;
+  const int idx[6][2] = {{0, 1}, {1, 2}, {2, 3}, {3, 4}, {4, 5}, {0, 0}};
+  for (int s = 0; s < 5; ++s) {
+    float t = 0;
+    cudaEventElapsedTime(&t, ev_stage[idx[s][0]], ev_stage[idx[s][1]]);
+    stats.ms_stage[s] = t;
+  }
+  stats.n_kmers = n_kmers;
+  stats.n_distinct = n_distinct;
+  stats.kernel_launches = launches;
+  return DK_OK;
+}
+
+int Engine::count(const char* text, uint64_t nbytes, bool text_on_device, const dk_input_desc* desc,
+                  dk_table* out) {
+  Engine* e = this;
+  std::lock_guard<std::mutex> g(mu);
+  const auto w0 = std::chrono::steady_clock::now();
+  if (!desc || !out || (!text && nbytes)) {
+    set_error("null argument");
+    return DK_ERR_INVALID_ARG;
+  }
+  std::memset(out, 0, sizeof(*out));
+  if (desc->k < 1 || desc->k > 32 || desc->line_width < 1 || desc->convention != DK_CONV_DAKC ||
+      desc->variant < DK_VARIANT_AUTO || desc->variant > DK_VARIANT_HASH ||
+      (desc->residency != DK_RESIDENT_HOST && desc->residency != DK_RESIDENT_DEVICE)) {
+    set_error("invalid input descriptor");
+    return DK_ERR_INVALID_ARG;
+  }
+  if (desc->line_width > 1024) {
+    set_error("line_width > 1024 is not supported");
+    return DK_ERR_INVALID_ARG;
+  }
+  if (frame_lines(nbytes, desc->line_width) < 0) {
+    set_error("buffer size is not a whole number of lines");
+    return DK_ERR_INVALID_ARG;
+  }
+  DK_CUDA(cudaSetDevice(device));
+  const uint8_t* d_text = (const uint8_t*)text;
+  float ms_h2d = 0;
+  if (!text_on_device) {
+    DK_TRY(Arena::ensure(this, this->text, nbytes + 64));
+    DK_CUDA(cudaEventRecord(ev_h2d0, stream));
+    if (nbytes) DK_TRY(upload(text, nbytes, (uint8_t*)this->text.p));
+    d_text = (const uint8_t*)this->text.p;
+  }
+  // output buffers sized by an upper bound of distinct k-mers (<= occurrences)
+  const int64_t L = frame_lines(nbytes, desc->line_width);
+  const uint64_t per_line = desc->line_width >= desc->k ? (uint64_t)(desc->line_width - desc->k + 1) : 0;
+  uint64_t upper = (uint64_t)L * per_line;
+  if (desc->k <= 16) upper = std::min<uint64_t>(upper, 1ull << (2 * desc->k));
+  TableBuf* dev_tb = nullptr;
+  DK_TRY(acquire_table(upper, true, &dev_tb));
+  out_k = (uint64_t*)dev_tb->k;
+  out_c = (uint32_t*)dev_tb->c;
+  DeviceTable dt;
+  int rc = count_device(d_text, nbytes, *desc, &dt);
+  if (rc != DK_OK) {
+    release_table(dev_tb->id);
+    return rc;
+  }
+  if (!text_on_device) {
+    cudaEventElapsedTime(&ms_h2d, ev_h2d0, ev_stage[0]);
+    stats.ms_h2d = ms_h2d;
+  }
+  out->n = dt.n;
+  out->n_kmers = dt.n_kmers;
+  out->variant_used = stats.variant_used;
+  if (desc->residency == DK_RESIDENT_DEVICE) {
+    out->kmers = (uint64_t*)dev_tb->k;
+    out->counts = (uint32_t*)dev_tb->c;
+    out->on_device = 1;
+    out->handle = dev_tb->id;
+  } else {
+    TableBuf* h_tb = nullptr;
+    rc = acquire_table(dt.n, false, &h_tb);
+    if (rc != DK_OK) {
+      release_table(dev_tb->id);
+      return rc;
+    }
+    if (dt.n) {
+      DK_CUDA(cudaMemcpyAsync(h_tb->k, dev_tb->k, dt.n * 8, cudaMemcpyDeviceToHost, stream));
+      DK_CUDA(cudaMemcpyAsync(h_tb->c, dev_tb->c, dt.n * 4, cudaMemcpyDeviceToHost, stream));
+    }
+    DK_CUDA(cudaEventRecord(ev_d2h1, stream));
+    DK_CUDA(cudaEventSynchronize(ev_d2h1));
+    float ms_d2h = 0;
+    cudaEventElapsedTime(&ms_d2h, ev_stage[5], ev_d2h1);
+    stats.ms_d2h = dt.n ? ms_d2h : 0.0;
+    release_table(dev_tb->id);
+    out->kmers = (uint64_t*)h_tb->k;
+    out->counts = (uint32_t*)h_tb->c;
+    out->on_device = 0;
+    out->handle = h_tb->id;
+  }
+  stats.dev_bytes_peak = dev_peak;
+  stats.ms_wall =
+      std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - w0).count();
+  return DK_OK;
+}
+
+}  // namespace dk
+
+// =================================================================== C ABI
+using dk::Engine;
+
+extern "C" {
+
+struct dk_ctx {
+  Engine eng;
+};
+
+int dk_abi_version(void) { return DK_ABI_VERSION; }
+
+const char* dk_strerror(int s) {
+  switch (s) {
+    case DK_OK: return "ok";
+    case DK_ERR_INVALID_ARG: return "invalid argument";
+    case DK_ERR_OOM: return "out of memory";
+    case DK_ERR_COUNT_OVERFLOW: return "k-mer count overflows 32 bits";
+    case DK_ERR_CUDA: return "CUDA error";
+    case DK_ERR_TIMEOUT: return "timed out";
+    case DK_ERR_ADMISSION: return "job exceeds the memory budget";
+    case DK_ERR_PENDING: return "pending";
+    case DK_ERR_NOT_FOUND: return "not found";
+    case DK_ERR_CANCELLED: return "cancelled";
+    case DK_ERR_NO_DEVICE: return "no usable CUDA device";
+  }
+  return "unknown status";
+}
+
+int dk_create(const dk_config* cfg, dk_ctx** out) {
+  if (!out) return DK_ERR_INVALID_ARG;
+  *out = nullptr;
+  dk_ctx* c = new (std::nothrow) dk_ctx();
+  if (!c) return DK_ERR_OOM;
+  const int rc = c->eng.init(cfg);
+  if (rc != DK_OK) {
+    delete c;
+    return rc;
+  }
+  *out = c;
+  return DK_OK;
+}
+
+int dk_destroy(dk_ctx* ctx) {
+  if (!ctx) return DK_ERR_INVALID_ARG;
+  delete ctx;
+  return DK_OK;
+}
+
+const char* dk_last_error_string(dk_ctx* ctx) {
+  return ctx ? ctx->eng.last_error.c_str() : "null context";
+}
+
+int dk_count(dk_ctx* ctx, const char* text, uint64_t nbytes, const dk_input_desc* desc,
+             dk_table* out) {
+  if (!ctx) return DK_ERR_INVALID_ARG;
+  return ctx->eng.count(text, nbytes, false, desc, out);
+}
+
+int dk_count_device(dk_ctx* ctx, const char* d_text, uint64_t nbytes, const dk_input_desc* desc,
+                    dk_table* out) {
+  if (!ctx) return DK_ERR_INVALID_ARG;
+  return ctx->eng.count(d_text, nbytes, true, desc, out);
+}
+
+int dk_table_free(dk_ctx* ctx, dk_table* t) {
+  if (!ctx || !t) return DK_ERR_INVALID_ARG;
+  if (!t->handle) return DK_OK;  // empty table
+  std::lock_guard<std::mutex> g(ctx->eng.mu);
+  const int rc = ctx->eng.release_table(t->handle);
+  std::memset(t, 0, sizeof(*t));
+  return rc;
+}
+
+int dk_last_stats(dk_ctx* ctx, dk_stats* out) {
+  if (!ctx || !out) return DK_ERR_INVALID_ARG;
+  *out = ctx->eng.stats;
+  return DK_OK;
+}
+
+int dk_host_alloc(uint64_t nbytes, void** out) {
+  if (!out) return DK_ERR_INVALID_ARG;
+  *out = nullptr;
+  if (cudaMallocHost(out, nbytes ? nbytes : 1) != cudaSuccess) {
+    cudaGetLastError();
+    *out = nullptr;
+    return DK_ERR_OOM;
+  }
+  return DK_OK;
+}
+
+int dk_host_free(void* p) {
+  if (!p) return DK_OK;
+  return cudaFreeHost(p) == cudaSuccess ? DK_OK : DK_ERR_CUDA;
+}
+
+int64_t dk_num_lines(const char* text, uint64_t nbytes, int line_width) {
+  const int64_t L = dk::frame_lines(nbytes, line_width);
+  if (L <= 0 || !text) return L;
+  const uint64_t stride = (uint64_t)line_width + 1;
+  for (int64_t i = 1; i < L; ++i)
+    if (text[(uint64_t)i * stride] == '\0') return i;
+  return L;
+}
+
+}  // extern "C"

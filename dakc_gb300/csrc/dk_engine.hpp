@@ -1,0 +1,83 @@
+// Engine state behind the C ABI (host side).
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <mutex>
+#include <string>
+#include <deque>
+
+#include "../../include/dakc_gb300.h"
+
+namespace dk {
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t cap = 0;
+};
+
+struct Engine;
+struct Arena {
+  // make b hold >= bytes (contents are not preserved); respects the budget
+  static int ensure(Engine* e, DevBuf& b, size_t bytes);
+  static void release(Engine* e, DevBuf& b);
+};
+
+// A table allocation (pinned host or device) handed out by dk_count and
+// returned to the pool by dk_table_free.
+struct TableBuf {
+  void* k = nullptr;
+  void* c = nullptr;
+  uint64_t cap = 0;
+  uint64_t id = 0;
+  bool on_device = false;
+  bool in_use = false;
+};
+
+struct DeviceTable {
+  uint64_t* k;
+  uint32_t* c;
+  uint64_t n;
+  uint64_t n_kmers;
+};
+
+int64_t frame_lines(uint64_t nbytes, int W);
+
+struct Engine {
+  int device = 0;
+  int sm_count = 0;
+  uint64_t budget = 0;
+  uint64_t dev_bytes = 0, dev_peak = 0;
+  cudaStream_t stream = nullptr;
+  std::mutex mu;
+  std::string last_error;
+  dk_stats stats{};
+  uint64_t launches = 0;
+
+  // device arenas
+  DevBuf text, keysA, keysB, cnt, H, O, nodes, tiles, TH, finals, ctrs;
+  size_t node_cap_needed = 0;
+  uint64_t* out_k = nullptr;
+  uint32_t* out_c = nullptr;
+  std::deque<TableBuf> tables;  // deque: stable addresses
+  uint64_t table_ids = 0;
+
+  cudaEvent_t ev_stage[8] = {};
+  cudaEvent_t ev_h2d0 = nullptr, ev_d2h1 = nullptr;
+  void* h_scratch = nullptr;
+  void* stage_pinned[2] = {nullptr, nullptr};
+  cudaEvent_t stage_ev[2] = {nullptr, nullptr};
+
+  int init(const dk_config* cfg);
+  ~Engine();
+  void set_error(const std::string& m);
+  int sync_read(const void* dsrc, size_t bytes, void* hdst);
+  int upload(const char* h, uint64_t nbytes, uint8_t* d);
+  int acquire_table(uint64_t n, bool on_device, TableBuf** out);
+  int release_table(uint64_t id);
+  int count_device(const uint8_t* d_text, uint64_t nbytes, const dk_input_desc& desc,
+                   DeviceTable* out);
+  int count(const char* text, uint64_t nbytes, bool text_on_device, const dk_input_desc* desc,
+            dk_table* out);
+};
+
+}  // namespace dk

@@ -1,0 +1,93 @@
+// Internal declarations shared by the engine's host pipeline and its kernels.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace dk {
+
+// A node of the MSD partition tree.  All keys of a node share their bits
+// [shift, 2k); the node's keys occupy index range [start, start+n) of buffer
+// `buf` (0 = A, 1 = B).  Children of a split node are 2^width consecutive
+// nodes starting at `first_child`, in digit (= key) order, and occupy
+// consecutive sub-ranges of the parent's index range in the other buffer, so
+// index order is key order at every level.
+struct Node {
+  uint64_t start;
+  uint64_t n;
+  uint64_t d;        // distinct keys in the subtree (filled bottom-up)
+  uint64_t out_off;  // output offset of the subtree's first distinct key
+  uint32_t first_child;  // valid when split
+  int16_t shift;     // remaining low bits not fixed by the path to this node
+  uint8_t buf;
+  uint8_t state;     // NODE_FINAL or NODE_SPLIT
+  uint32_t tile_base;  // first partition tile (split nodes)
+  uint32_t ntiles;
+};
+enum : uint8_t { NODE_FINAL = 1, NODE_SPLIT = 2, NODE_EMPTY = 3 };
+
+struct Tile {  // a slice of a split node's keys, partitioned by one CTA
+  uint64_t start;
+  uint32_t n;
+  uint32_t node;  // global node index
+};
+
+// counters written by the classify / assign kernels.  n_final accumulates over
+// all levels; the others are per level.
+struct LevelCounters {
+  uint32_t n_final;
+  uint32_t n_split;
+  uint32_t n_tiles;
+  uint32_t too_big;  // a split node holds >= 2^32 keys
+  uint32_t n_children;
+  uint32_t n_tiles_assigned;
+  uint32_t pad[2];
+};
+
+constexpr int kDigitBits = 8;           // fan-out of partition levels 2+
+constexpr int kFanout = 1 << kDigitBits;
+constexpr int kTileKeys = 8192;         // keys per partition tile
+constexpr int kBinCap = 12288;          // keys a bin-count CTA sorts in shared memory
+constexpr int kDenseBits = 12;          // nodes with <= this many free bits are counted densely
+constexpr int kBinThreads = 512;
+constexpr int kMaxL1Bits = 12;          // level-1 fan-out <= 4096 buckets
+
+struct ExtractArgs {
+  const uint8_t* text;  // device text (padded)
+  uint64_t n_lines;
+  int W;
+  int k;
+  uint64_t kmask;
+  int shift1;  // level-1 bucket = key >> shift1
+  int F1;      // number of level-1 buckets
+};
+
+// ---- launchers (dk_kernels.cu); every launcher returns the number of kernel
+// launches it issued (for the launch count reported in stats)
+int launch_l1_count(const ExtractArgs& a, int grid, uint32_t* H, unsigned long long* n_kmers,
+                    cudaStream_t s);
+int launch_l1_scan(const uint32_t* H, int grid, int F1, uint64_t* O, Node* nodes, int shift1,
+                   cudaStream_t s);
+int launch_l1_scatter(const ExtractArgs& a, int grid, const uint64_t* O, uint64_t* keys,
+                      cudaStream_t s);
+int launch_classify(Node* nodes, uint32_t node_lo, uint32_t node_hi, uint32_t* final_list,
+                    LevelCounters* ctr, int bin_cap, cudaStream_t s);
+int launch_assign(Node* nodes, uint32_t node_lo, uint32_t node_hi, uint32_t child_base,
+                  Tile* tiles, LevelCounters* ctr, cudaStream_t s);
+int launch_tile_hist(const Node* nodes, const Tile* tiles, uint32_t n_tiles,
+                     const uint64_t* A, const uint64_t* B, uint32_t* TH, cudaStream_t s);
+int launch_node_scan(Node* nodes, uint32_t node_lo, uint32_t node_hi, const Tile* tiles,
+                     uint32_t* TH, cudaStream_t s);
+int launch_tile_scatter(const Node* nodes, const Tile* tiles, uint32_t n_tiles, uint64_t* A,
+                        uint64_t* B, const uint32_t* TH, cudaStream_t s);
+int launch_bin_count(Node* nodes, const uint32_t* final_list, uint32_t n_final, uint64_t* A,
+                     uint64_t* B, uint32_t* C, int variant, int* overflow, cudaStream_t s);
+int launch_aggregate(Node* nodes, uint32_t node_lo, uint32_t node_hi, cudaStream_t s);
+int launch_l1_offsets(Node* nodes, uint32_t n1, unsigned long long* total_d, cudaStream_t s);
+int launch_child_offsets(Node* nodes, uint32_t node_lo, uint32_t node_hi, cudaStream_t s);
+int launch_compact(const Node* nodes, const uint32_t* final_list, uint32_t n_final,
+                   const uint64_t* A, const uint64_t* B, const uint32_t* C, uint64_t* out_k,
+                   uint32_t* out_c, cudaStream_t s);
+
+int bin_count_smem_bytes(int variant);
+
+}  // namespace dk

@@ -1,0 +1,155 @@
+/*
+ * dakc_gb300.h -- C ABI of the GB300 k-mer counting engine.
+ *
+ * A drop-in for DAKC's k-mer counting entry point: DAKC's counter is the
+ * constructor
+ *     kmercounter(char* read_chunk, std::vector<kmer_t>& vectordbg)
+ * (dakc/src/kcounter/kcounter.hpp:84-99), which parses a NUL-terminated chunk
+ * of fixed-width read lines, counts every k-mer (k = KMERLEN, line width =
+ * READLEN, both compile-time there: dakc/src/common/common.hpp:34-40) and
+ * leaves the per-PE sorted (kmer, count) table in the public member lightdbg
+ * (kcounter.cpp:385-414).  dk_count takes the same read buffer, k and line
+ * width at run time and returns the globally sorted table -- the merge of all
+ * PEs' lightdbg tables -- in one call on one GPU.
+ *
+ * Convention (bit-exact with the reference):
+ *   - base codes C=0, A=1, T=2, G=3, upper or lower case
+ *     (char2base, common.hpp:72-92);
+ *   - a k-mer is packed MSB-first into the low 2k bits of a uint64
+ *     (set_kmer_fast/update_kmer_fast, kcounter_funcs.cpp:25-38);
+ *   - forward strand only, no canonical form;
+ *   - a line is line_width bytes followed by one terminator byte that is never
+ *     examined (the last terminator may be missing); 'M'/'m' ends the line;
+ *     any other non-ACGT byte splits it; a run of L bases yields L-k+1 k-mers
+ *     (read_till_buf_max, kcounter_funcs.cpp:69-111, including its rule that
+ *     the last run is emitted only when it starts before line_width-1);
+ *   - parsing stops before the first line (after line 0) whose first byte is
+ *     NUL, as the reference stops at rchunk[read_idx] == '\0' (one PE).
+ *
+ * All entry points return 0 (DK_OK) or a negative DK_ERR_* status; nothing
+ * throws across this boundary.  No call takes torch or C++ types.
+ */
+#ifndef DAKC_GB300_H
+#define DAKC_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DK_ABI_VERSION 1
+
+/* status codes */
+#define DK_OK 0
+#define DK_ERR_INVALID_ARG (-1)     /* bad k, line width, sizes or pointers        */
+#define DK_ERR_OOM (-2)             /* device or host allocation failed            */
+#define DK_ERR_COUNT_OVERFLOW (-3)  /* a count does not fit 32 bits                */
+#define DK_ERR_CUDA (-4)            /* a CUDA call failed (see dk_last_error_string)*/
+#define DK_ERR_TIMEOUT (-5)         /* a bounded device or host wait ran out       */
+#define DK_ERR_ADMISSION (-6)       /* job larger than the context's memory budget */
+#define DK_ERR_PENDING (-7)         /* dk_poll: the job has not finished yet        */
+#define DK_ERR_NOT_FOUND (-8)       /* unknown ticket                              */
+#define DK_ERR_CANCELLED (-9)       /* job cancelled before it ran                 */
+#define DK_ERR_NO_DEVICE (-10)      /* no CUDA device / engine not built for it    */
+
+/* per-bucket count variants */
+#define DK_VARIANT_AUTO 0  /* picked per workload                                 */
+#define DK_VARIANT_SORT 1  /* partition + shared-memory sort + run-length reduce  */
+#define DK_VARIANT_HASH 2  /* partition + shared-memory hash aggregation          */
+
+/* k-mer conventions */
+#define DK_CONV_DAKC 0     /* the only one: see above                              */
+
+/* where dk_count leaves the table */
+#define DK_RESIDENT_HOST 0   /* kmers/counts are host arrays owned by the context  */
+#define DK_RESIDENT_DEVICE 1 /* kmers/counts are device pointers owned by the ctx  */
+
+typedef struct dk_ctx dk_ctx;
+
+typedef struct {
+  int device;          /* CUDA device ordinal                                    */
+  int reserved0;
+  uint64_t mem_budget; /* device bytes the context may hold; 0 = 80% of free    */
+  uint64_t flags;      /* reserved, 0                                            */
+} dk_config;
+
+typedef struct {
+  int line_width;  /* READLEN: bytes per line before the terminator (>= 1)      */
+  int k;           /* KMERLEN: 1..32                                            */
+  int convention;  /* DK_CONV_DAKC                                               */
+  int variant;     /* DK_VARIANT_*                                               */
+  int residency;   /* DK_RESIDENT_*                                              */
+  int reserved[3];
+} dk_input_desc;
+
+typedef struct {
+  uint64_t* kmers;   /* n distinct k-mers, ascending                           */
+  uint32_t* counts;  /* occurrences of kmers[i]                                */
+  uint64_t n;        /* distinct k-mers (DAKC's global_distinct_kmers)         */
+  uint64_t n_kmers;  /* k-mer occurrences (DAKC's global_kmers)                */
+  int on_device;     /* 1 when kmers/counts are device pointers                */
+  int variant_used;  /* DK_VARIANT_SORT or DK_VARIANT_HASH                     */
+  uint64_t handle;   /* owner token, pass back to dk_table_free                */
+} dk_table;
+
+/* timings of the last dk_count/dk_count_device on a context (CUDA events on
+ * the context's stream) */
+typedef struct {
+  double ms_device;     /* first kernel to table complete in device memory     */
+  double ms_h2d;        /* host -> device copy of the reads (dk_count only)    */
+  double ms_d2h;        /* device -> host copy of the table (host residency)   */
+  double ms_wall;       /* host wall time of the whole call                    */
+  double ms_stage[8];   /* extract+count, scatter, partition, bin count,
+                           output, hash, reserved, reserved                    */
+  uint64_t n_kmers, n_distinct, n_lines;
+  uint64_t kernel_launches;  /* engine kernels launched by the call            */
+  uint64_t dev_bytes_peak;   /* device bytes held by the context               */
+  int variant_used;
+  int partition_levels;
+  uint64_t n_bins;
+} dk_stats;
+
+/* One read set of a batch (dk_count_batch). */
+typedef struct {
+  const char* text;  /* host pointer (pinned or pageable)                       */
+  uint64_t nbytes;
+} dk_job;
+
+/* --- context ---------------------------------------------------------- */
+int dk_create(const dk_config* cfg, dk_ctx** out);
+int dk_destroy(dk_ctx* ctx);
+const char* dk_strerror(int status);
+const char* dk_last_error_string(dk_ctx* ctx);
+int dk_abi_version(void);
+
+/* --- plain count ------------------------------------------------------ */
+/* Replaces kmercounter(read_chunk, vectordbg) + reading lightdbg
+ * (kcounter.hpp:84-99, kcounter.cpp:385-414): `text` is a host buffer of
+ * nbytes (pinned or pageable; borrowed for the call).  On success *out holds
+ * the sorted table; release it with dk_table_free. */
+int dk_count(dk_ctx* ctx, const char* text, uint64_t nbytes, const dk_input_desc* desc,
+             dk_table* out);
+
+/* Same, with the reads already in device memory (d_text: device pointer). */
+int dk_count_device(dk_ctx* ctx, const char* d_text, uint64_t nbytes, const dk_input_desc* desc,
+                    dk_table* out);
+
+int dk_table_free(dk_ctx* ctx, dk_table* t);
+int dk_last_stats(dk_ctx* ctx, dk_stats* out);
+
+/* Number of lines dk_count will parse for this buffer under the framing rules
+ * above (host-side, no GPU work); negative status for a malformed size. */
+int64_t dk_num_lines(const char* text, uint64_t nbytes, int line_width);
+
+/* Page-locked host memory for read buffers (dk_count then copies it with one
+ * DMA instead of staging it).  Replaces the reference's malloc'd read chunk
+ * (dakc/src/fqreader/fqreader.cpp:59). */
+int dk_host_alloc(uint64_t nbytes, void** out);
+int dk_host_free(void* p);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* DAKC_GB300_H */

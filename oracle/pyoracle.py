@@ -1,0 +1,179 @@
+"""ctypes wrapper of the CPU oracle -- TEST INFRASTRUCTURE ONLY.
+
+Only the tests, the smoke check and the benchmark's CPU-baseline leg import
+this module, and only as the checker / the timed CPU baseline; the engine
+never calls it.
+
+* ``count``      -- dk_oracle.c's single-threaded restatement (extract, LSD
+                    radix sort, run-length), the parity checker.
+* ``dakc_port``  -- DAKC's two phases on P host threads (owner hash
+                    MurmurHash64A % P, per-owner sort + run-length), timed as
+                    the CPU baseline.
+* ``ref_table``  -- runs the reference's own kcounter sources, compiled
+                    unmodified against the shim (oracle/_ref), on P forked PEs.
+                    Only available where the reference tree was present to
+                    compile them.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "_build", "libdk_oracle.so")
+REF_DIR = os.path.join(HERE, "_ref")
+REFERENCE_TREE = "/root/reference"
+
+
+class _Table(ctypes.Structure):
+    _fields_ = [("kmers", ctypes.POINTER(ctypes.c_uint64)),
+                ("counts", ctypes.POINTER(ctypes.c_uint32)),
+                ("n", ctypes.c_uint64),
+                ("n_kmers", ctypes.c_uint64)]
+
+
+_lib = None
+
+
+def build_lib() -> None:
+    subprocess.run(["make", "-s", "-C", HERE, "lib"], check=True)
+
+
+def _load():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB):
+            build_lib()
+        lib = ctypes.CDLL(LIB)
+        vp, u64, i32 = ctypes.c_void_p, ctypes.c_uint64, ctypes.c_int
+        lib.dko_count.argtypes = [vp, u64, i32, i32, ctypes.POINTER(_Table)]
+        lib.dko_dakc_port.argtypes = [vp, u64, i32, i32, i32, i32, ctypes.POINTER(_Table),
+                                      ctypes.POINTER(ctypes.c_double)]
+        lib.dko_free.argtypes = [ctypes.POINTER(_Table)]
+        lib.dko_num_lines.argtypes = [vp, u64, i32]
+        lib.dko_num_lines.restype = ctypes.c_int64
+        lib.dko_murmur64a.argtypes = [u64, u64]
+        lib.dko_murmur64a.restype = u64
+        lib.dko_code_table.restype = ctypes.POINTER(ctypes.c_uint8)
+        _lib = lib
+    return _lib
+
+
+class OracleError(RuntimeError):
+    pass
+
+
+def _as_bytes(text) -> np.ndarray:
+    if isinstance(text, (bytes, bytearray)):
+        return np.frombuffer(bytes(text), dtype=np.uint8)
+    return np.ascontiguousarray(text, dtype=np.uint8)
+
+
+def _take(t: _Table):
+    n = int(t.n)
+    if n:
+        keys = np.ctypeslib.as_array(t.kmers, shape=(n,)).copy()
+        counts = np.ctypeslib.as_array(t.counts, shape=(n,)).copy()
+    else:
+        keys = np.zeros(0, np.uint64)
+        counts = np.zeros(0, np.uint32)
+    return keys, counts, int(t.n_kmers)
+
+
+def count(text, line_width: int, k: int):
+    """(keys uint64 sorted, counts uint32, n_kmers) by the single-threaded restatement."""
+    buf = _as_bytes(text)
+    lib = _load()
+    t = _Table()
+    rc = lib.dko_count(buf.ctypes.data, buf.size, line_width, k, ctypes.byref(t))
+    try:
+        if rc == -1:
+            raise OracleError("invalid arguments")
+        out = _take(t)
+        if rc == -2:
+            raise OracleError("count overflows 32 bits")
+        return out
+    finally:
+        lib.dko_free(ctypes.byref(t))
+
+
+def dakc_port(text, line_width: int, k: int, pes: int, merge: bool = True):
+    """Run the P-thread DAKC port; returns ((keys, counts, n_kmers) or None, seconds)."""
+    buf = _as_bytes(text)
+    lib = _load()
+    t = _Table()
+    secs = ctypes.c_double(0)
+    rc = lib.dko_dakc_port(buf.ctypes.data, buf.size, line_width, k, pes, 1 if merge else 0,
+                           ctypes.byref(t), ctypes.byref(secs))
+    try:
+        if rc == -1:
+            raise OracleError("invalid arguments")
+        if merge:
+            return _take(t), secs.value
+        return (None, None, int(t.n_kmers)), secs.value
+    finally:
+        lib.dko_free(ctypes.byref(t))
+
+
+def num_lines(text, line_width: int) -> int:
+    buf = _as_bytes(text)
+    return int(_load().dko_num_lines(buf.ctypes.data, buf.size, line_width))
+
+
+def murmur64a(key: int, seed: int = 0x9E3779B97F4A7C15) -> int:
+    return int(_load().dko_murmur64a(key, seed))
+
+
+def code_table() -> np.ndarray:
+    p = _load().dko_code_table()
+    return np.ctypeslib.as_array(p, shape=(256,)).copy()
+
+
+# ------------------------------------------------------- reference (shim)
+def ref_binary(k: int, line_width: int, hitter: int = 0, build: bool = True) -> str | None:
+    """Path of the shim-built reference binary for (k, READLEN, HITTER), building it
+    from the reference tree when that tree is present; None when unavailable."""
+    path = os.path.join(REF_DIR, f"dakc_ref_k{k}_r{line_width}_h{hitter}")
+    if os.path.exists(path):
+        return path
+    if not build or not os.path.isdir(os.path.join(REFERENCE_TREE, "dakc", "src")):
+        return None
+    subprocess.run(["make", "-s", "-C", HERE, "ref", f"K={k}", f"R={line_width}", f"H={hitter}",
+                    f"REF={REFERENCE_TREE}"], check=True)
+    return path
+
+
+def read_table_file(path: str):
+    with open(path, "rb") as f:
+        raw = f.read()
+    if raw[:4] != b"DKT1":
+        raise OracleError("bad table file")
+    n = int(np.frombuffer(raw, np.uint64, 1, 4)[0])
+    nk = int(np.frombuffer(raw, np.uint64, 1, 12)[0])
+    keys = np.frombuffer(raw, np.uint64, n, 20).copy()
+    counts = np.frombuffer(raw, np.uint32, n, 20 + 8 * n).copy()
+    return keys, counts, nk
+
+
+def ref_table(text, line_width: int, k: int, pes: int = 1, hitter: int = 0, timeout: float = 600):
+    """Run the reference's own counting code on `pes` forked PEs.
+
+    Returns ((keys, counts, n_kmers), stdout).  Raises OracleError when the
+    binary is unavailable or when the reference's behaviour is undefined for
+    this input (a PE that receives no k-mer)."""
+    exe = ref_binary(k, line_width, hitter)
+    if exe is None:
+        raise OracleError("reference binary unavailable (reference tree absent)")
+    buf = _as_bytes(text)
+    with tempfile.TemporaryDirectory() as d:
+        inp = os.path.join(d, "reads.txt")
+        out = os.path.join(d, "table.bin")
+        buf.tofile(inp)
+        p = subprocess.run([exe, inp, str(pes), out], capture_output=True, text=True, timeout=timeout)
+        if p.returncode != 0:
+            raise OracleError(f"reference exited {p.returncode}: {p.stderr.strip()[:200]}")
+        return read_table_file(out), p.stdout

@@ -1,0 +1,160 @@
+"""GPU engine vs the CPU oracle, bit for bit, through the C ABI.
+
+Every case compares the full table (sorted distinct k-mers, their uint32
+counts) and the occurrence total.  Integer work: the bar is exact equality.
+"""
+import numpy as np
+import pytest
+
+import dakc_gb300 as dk
+from dakc_gb300 import synth
+from oracle import pyoracle
+
+pytestmark = pytest.mark.gpu
+
+VARIANTS = [dk.VARIANT_SORT]
+
+
+def check(engine, text, W, k, variant=dk.VARIANT_SORT):
+    got = engine.count(text, W, k, variant)
+    keys, counts, nk = pyoracle.count(text, W, k)
+    assert got.n_kmers == nk
+    assert got.kmers.size == keys.size, (got.kmers.size, keys.size)
+    assert np.array_equal(got.kmers, keys)
+    assert np.array_equal(got.counts, counts)
+    return got
+
+
+def lines(*rows, W):
+    out = b""
+    for r in rows:
+        assert len(r) <= W
+        out += r + b"M" * (W - len(r)) + b"\n"
+    return out
+
+
+# ------------------------------------------------------------ known answers
+@pytest.mark.parametrize("variant", VARIANTS)
+def test_known_answers(engine, variant):
+    assert engine.count(b"CAT\n", 3, 3, variant).kmers.tolist() == [6]
+    assert engine.count(b"GGG\n", 3, 3, variant).kmers.tolist() == [63]
+    assert engine.count(b"ACG\n", 3, 3, variant).kmers.tolist() == [19]
+    assert engine.count(b"CANTG\n", 5, 3, variant).kmers.size == 0
+    r = engine.count(b"CATMAAA\n", 7, 3, variant)
+    assert r.kmers.tolist() == [6] and r.counts.tolist() == [1]
+    r = engine.count(b"G" * 32 + b"\n", 32, 32, variant)
+    assert r.kmers.tolist() == [0xFFFFFFFFFFFFFFFF]
+
+
+@pytest.mark.parametrize("variant", VARIANTS)
+def test_empty_and_short(engine, variant):
+    for text, W, k in [(b"", 150, 31), (b"ACG\n", 3, 4), (b"NNNN\n", 4, 2), (b"MMMM\n", 4, 1),
+                       (b"AC\nGT\n", 2, 3)]:
+        r = engine.count(text, W, k, variant)
+        assert r.kmers.size == 0 and r.n_kmers == 0
+
+
+@pytest.mark.parametrize("variant", VARIANTS)
+def test_framing_rules(engine, variant):
+    W = 20
+    rows = [b"ACGTACGTACGTACGTACGT", b"acgtNacgtacgtACGT", b"ACGTACGM", b"ACGTAC\nGTAC",
+            b"AAAAAAAAAAAAAAAAAAAA", b"TTTT TTTT-TTTTTTT", b"CCCCMCCCCCCCCC"]
+    text = lines(*rows, W=W)
+    for k in (1, 2, 3, 5, 8, 13, 20):
+        check(engine, text, W, k, variant)
+    # last terminator missing
+    check(engine, text[:-1], W, 5, variant)
+    # the terminator byte is never examined
+    t2 = bytearray(text)
+    t2[W] = ord("A")
+    check(engine, bytes(t2), W, 5, variant)
+
+
+@pytest.mark.parametrize("variant", VARIANTS)
+def test_k1_last_run_rule(engine, variant):
+    # k=1: a final run starting at W-1 is dropped (kcounter_funcs.cpp:97)
+    W = 6
+    text = lines(b"ACGTNA", b"ACGTAA", b"NNNNNA", b"ACGTAN", b"ACMGTA", W=W)
+    got = check(engine, text, W, 1, variant)
+    assert got.n_kmers == 4 + 6 + 0 + 5 + 2
+    check(engine, b"A\nC\nG\n", 1, 1, variant)  # W=1: nothing is emitted
+
+
+@pytest.mark.parametrize("variant", VARIANTS)
+def test_nul_line_stops_parsing(engine, variant):
+    W = 10
+    rows = [b"ACGTACGTAC", b"CCCCCCCCCC", b"\0GGGGGGGGG", b"TTTTTTTTTT"]
+    text = lines(*rows, W=W)
+    got = check(engine, text, W, 4, variant)
+    assert got.n_kmers == 14  # lines 0 and 1 only
+    # NUL inside a line is just a break; NUL as the first byte of line 0 too
+    text = lines(b"\0CGTACGTAC", b"CCCC\0CCCCC", W=W)
+    check(engine, text, W, 4, variant)
+
+
+@pytest.mark.parametrize("variant", VARIANTS)
+@pytest.mark.parametrize("W,k", [(1, 1), (2, 1), (31, 31), (32, 31), (33, 17), (64, 32),
+                                 (100, 21), (150, 31), (150, 17), (250, 31), (257, 25),
+                                 (500, 31), (1000, 15)])
+def test_random_shapes(engine, variant, W, k):
+    text = synth.random_lines(W * 7 + k, 3000, W, b"ACGTACGTACGTacgtNM")
+    check(engine, text, W, k, variant)
+
+
+@pytest.mark.parametrize("variant", VARIANTS)
+@pytest.mark.parametrize("k", [1, 2, 5, 6, 7, 11, 12, 13, 16, 21, 27, 32])
+def test_k_sweep(engine, variant, k):
+    g = synth.genome_uniform(100 + k, 50_000)
+    text = synth.reads(200 + k, g, 5000, 80, 100, 100, rc_frac=0.5, err_rate=0.01)
+    check(engine, text, 100, k, variant)
+
+
+@pytest.mark.parametrize("variant", VARIANTS)
+def test_plain_1m_workload(engine, variant):
+    rs = synth.plain_1m()
+    got = check(engine, rs.text, rs.line_width, rs.k, variant)
+    assert got.n_kmers == 12_000_000
+
+
+@pytest.mark.parametrize("variant", VARIANTS)
+def test_skew_heavy_hitters(engine, variant):
+    # a few reads repeated very many times: giant buckets, dense and deep paths
+    W = 150
+    g = synth.genome_uniform(7, 20_000)
+    hot = synth.reads(8, g, 3, 150, 150, W, rc_frac=0.0)
+    bg = synth.reads(9, g, 20_000, 150, 150, W, rc_frac=0.5, err_rate=0.01)
+    text = np.concatenate([np.tile(hot, 40_000), bg])
+    got = check(engine, text, W, 31, variant)
+    assert got.counts.max() >= 40_000
+    # one k-mer only: every count lands in one key
+    text = np.frombuffer(lines(b"A" * 150, W=150) * 20_000, dtype=np.uint8)
+    got = check(engine, text, W, 31, variant)
+    assert got.kmers.size == 1 and got.counts[0] == 120 * 20_000
+
+
+@pytest.mark.parametrize("variant", VARIANTS)
+def test_two_partition_levels(engine, variant):
+    # > 4096 * 6144 k-mers forces the 8-bit partition level below level 1
+    g = synth.genome_uniform(21, 30_000_000)
+    text = synth.reads(22, g, 300_000, 150, 150, 150, rc_frac=0.5, err_rate=0.005)
+    check(engine, text, 150, 31, variant)
+    st = engine.stats()
+    assert st["partition_levels"] >= 2
+
+
+def test_table_device_residency(engine):
+    text = synth.random_lines(5, 1000, 150)
+    d = dk.Engine.desc(150, 21, dk.VARIANT_SORT, dk.RESIDENT_DEVICE)
+    ptr = text.ctypes.data
+    t = engine.count_raw(ptr, text.size, d)
+    try:
+        assert t.on_device == 1 and t.n > 0
+    finally:
+        engine.free_table(t)
+
+
+def test_invalid_arguments(engine):
+    for W, k, n in [(150, 0, 151), (150, 33, 151), (0, 3, 1), (150, 31, 100)]:
+        with pytest.raises(dk.DkError) as e:
+            engine.count(b"A" * n, W, k)
+        assert e.value.status == dk.DK_ERR_INVALID_ARG
