@@ -1,0 +1,356 @@
+#!/usr/bin/env python
+"""Benchmark: k-mer counting throughput on one GB300 (and N independent replicas).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl engine|reference]
+
+Workload (default ``large_100m``): seeded synthetic 100 Mbp genome, 20% of it
+in 200 repeat families (1-5 kbp, 10-100 copies, 2% divergence), 30x coverage
+of 150 bp reads (20,000,000 reads, 3.02 GB of DAKC text), 1% substitutions,
+50/50 strand; k = 31.  A "step" counts the whole read set once.
+
+* ``value``  -- k-mers/s with the reads resident in HBM, table left in HBM:
+  total k-mer occurrences / the step's device time (CUDA events on the
+  engine's stream, first kernel to table complete).  The 3 GB input is far
+  larger than L2 (135 MB), so no flush is needed between steps.
+* ``e2e``    -- the same metric through dk_count with host buffers: pinned
+  host reads -> H2D -> count -> D2H of the full table into host memory.
+* ``roofline`` -- the dominant kernel's algorithmic bytes / its event time,
+  against the measured HBM copy peak; ``pipeline_roofline`` does the same
+  for the whole step with B_alg = text + 16 N_k + 12 N_d.
+* ``cpu_baseline`` -- DAKC's two phases (owner hash, per-owner sort +
+  run-length) on all host threads, on a bounded sample of the same reads.
+
+``--impl reference`` times that CPU implementation alone (rank 0 only).
+For N > 1 (torchrun) every rank counts its own copy of the workload: the path
+has no exchange step on one GPU, so ranks are independent replicas.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "k-mers/sec k=31 on 1 GB300, % HBM roofline; p50/p99 job latency batched vs plain"
+UNIT = "k-mers/s"
+KERNEL_NAMES = ["extract_count", "extract_scatter", "partition_hist", "partition_scatter",
+                "bin_count", "compact", "hash_insert", "other"]
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class Dist:
+    """Barrier / max / sum over ranks (gloo over the host; no GPU collective)."""
+
+    def __init__(self, rank, world):
+        self.rank, self.world = rank, world
+        self.dist = None
+        if world > 1:
+            import torch.distributed as dist
+            dist.init_process_group("gloo")
+            self.dist = dist
+
+    def barrier(self):
+        if self.dist:
+            self.dist.barrier()
+
+    def reduce(self, x: float, op: str) -> float:
+        if not self.dist:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX if op == "max" else self.dist.ReduceOp.SUM)
+        return float(t.item())
+
+    def close(self):
+        if self.dist:
+            self.dist.destroy_process_group()
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled while the timed region runs."""
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "50"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def stop(self) -> dict:
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.06)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 7:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx.append(float(f[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[3:7]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_workload(name: str, scale: float):
+    from dakc_gb300 import synth
+    if name == "large_100m":
+        g = int(100_000_000 * scale)
+        rs = synth.large_100m(genome_len=g)
+        cfg = {"workload": "large_100m", "genome_bp": g, "reads": rs.n_lines, "read_len": 150,
+               "k": 31, "coverage": 30, "error_rate": 0.01, "repeat_frac": 0.2,
+               "repeat_families": 200}
+    elif name == "plain_1m":
+        rs = synth.plain_1m()
+        cfg = {"workload": "plain_1m", "genome_bp": 1_000_000, "reads": rs.n_lines,
+               "read_len": 150, "k": 31, "error_rate": 0.001}
+    elif name.startswith("zipf_skew"):
+        k = int(name.split("_k")[-1]) if "_k" in name else 31
+        rs = synth.zipf_skew(k=k, nreads=int(10_000_000 * scale),
+                             background_len=int(50_000_000 * scale), check=scale >= 1.0)
+        cfg = {"workload": rs.name, "reads": rs.n_lines, "read_len": 150, "k": k,
+               "zipf_s": 1.1, "hot_frac": synth.ZIPF_HOT_FRAC, "templates": synth.ZIPF_TEMPLATES}
+    else:
+        raise SystemExit(f"unknown workload {name}")
+    return rs, cfg
+
+
+def cpu_sample(rs, cap_reads: int):
+    n = min(rs.n_lines, cap_reads)
+    return rs.text[: n * (rs.line_width + 1)], n
+
+
+def run_cpu(rs, cap_reads: int, steps: int, warmup: int, threads: int):
+    """DAKC's two phases (the oracle port) on `threads` host threads."""
+    from oracle import pyoracle
+    text, n = cpu_sample(rs, cap_reads)
+    times, nk = [], 0
+    for i in range(warmup + steps):
+        (_, _, nk), secs = pyoracle.dakc_port(text, rs.line_width, rs.k, threads, merge=False)
+        if i >= warmup:
+            times.append(secs)
+    t = float(np.mean(times))
+    return {"value": nk / t, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"first {n:,} of {rs.n_lines:,} reads ({nk:,} k-mers), {threads} PEs as "
+                      f"threads, phase 1 + phase 2 as DAKC times them, mean of {steps}",
+            "seconds": t}
+
+
+def alg_bytes(st: dict, nbytes: int) -> list[float]:
+    nk, nd, npart = st["n_kmers"], st["n_distinct"], st["n_partitioned"]
+    return [nbytes,                    # extract_count: read the text
+            nbytes + 8 * nk,           # extract_scatter: read text, write keys
+            8 * npart,                 # partition_hist: read keys
+            16 * npart,                # partition_scatter: read + write keys
+            8 * nk + 12 * nd,          # bin_count: read keys, write staged pairs
+            24 * nd,                   # compact: read + write pairs
+            0, 0]
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
+    ap.add_argument("--workload", default="large_100m")
+    ap.add_argument("--scale", type=float, default=1.0)
+    ap.add_argument("--variant", default="sort", choices=["auto", "sort", "hash"])
+    ap.add_argument("--cpu-reads", type=int, default=4_000_000,
+                    help="reads in the CPU baseline's bounded sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    args = ap.parse_args()
+    rank, world, local = dist_env()
+
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        rs, cfg = make_workload(args.workload, args.scale)
+        threads = os.cpu_count() or 1
+        cb = run_cpu(rs, args.cpu_reads, args.steps, args.warmup, threads)
+        line = {"metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": args.gpus,
+                "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": cb["seconds"] * 1000.0, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic",
+                "config": dict(cfg, sample_reads=min(rs.n_lines, args.cpu_reads)),
+                "impl": "reference",
+                "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
+                "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return 0
+
+    import torch
+    import dakc_gb300 as dk
+
+    dist = Dist(rank, world)
+    torch.cuda.set_device(local)
+    rs, cfg = make_workload(args.workload, args.scale)
+    nbytes = rs.text.size
+    variant = {"auto": dk.VARIANT_AUTO, "sort": dk.VARIANT_SORT, "hash": dk.VARIANT_HASH}[args.variant]
+
+    # CPU baseline first (rank 0, N=1 only), before the GPU is busy
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = run_cpu(rs, args.cpu_reads, 1, 0, os.cpu_count() or 1)
+
+    eng = dk.Engine(local)
+    d_text = torch.empty(nbytes + 64, dtype=torch.uint8, device=f"cuda:{local}")
+    d_text[:nbytes].copy_(torch.from_numpy(rs.text))
+    torch.cuda.synchronize()
+    desc = dk.Engine.desc(rs.line_width, rs.k, variant, dk.RESIDENT_DEVICE)
+
+    def step():
+        t = eng.count_raw(d_text.data_ptr(), nbytes, desc, on_device=True)
+        st = eng.stats()
+        eng.free_table(t)
+        return st
+
+    for _ in range(args.warmup):
+        step()
+    clocks = ClockSampler(local)
+    clocks.start()
+    dist.barrier()
+    torch.cuda.synchronize()
+    w0 = time.perf_counter()
+    sts = [step() for _ in range(args.steps)]
+    torch.cuda.synchronize()
+    dist.barrier()
+    w1 = time.perf_counter()
+    clk = clocks.stop()
+
+    dev_ms = float(sum(s["ms_device"] for s in sts))
+    nk = sts[0]["n_kmers"]
+    nd = sts[0]["n_distinct"]
+    t_max = dist.reduce(dev_ms, "max")
+    units = dist.reduce(float(nk * args.steps), "sum")
+    value = units / (t_max / 1000.0)
+    ms_per_step = t_max / args.steps
+    launches = int(sum(s["kernel_launches"] for s in sts))
+
+    # kernel roofline from the engine's per-kernel CUDA events
+    hbm_peak, peak_kind = peaks()
+    kms = np.sum([s["ms_kernel"] for s in sts], axis=0) / args.steps
+    kl = np.sum([s["launches_kernel"] for s in sts], axis=0) / args.steps
+    ab = alg_bytes(sts[0], nbytes)
+    top = int(np.argmax(kms[:7]))
+    achieved = ab[top] / (kms[top] / 1000.0) / 1e9 if kms[top] > 0 else 0.0
+    traffic = None
+    tp = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tp):
+        with open(tp) as f:
+            tj = json.load(f)
+        ent = tj.get(KERNEL_NAMES[top])
+        if ent and ent.get("bytes_per_kmer"):
+            traffic = ent["bytes_per_kmer"] * nk
+    b_alg = nbytes + 16 * nk + 12 * nd
+    pipe = b_alg / (ms_per_step / 1000.0) / 1e9
+
+    # end to end through dk_count: pinned host reads in, host table out
+    e2e = None
+    if rank == 0 and args.e2e_steps > 0:
+        pin = dk.PinnedBuffer(nbytes)
+        pin.array[:] = rs.text
+        hdesc = dk.Engine.desc(rs.line_width, rs.k, variant, dk.RESIDENT_HOST)
+        for _ in range(1):
+            eng.free_table(eng.count_raw(pin.ptr, nbytes, hdesc))
+        walls = []
+        for _ in range(args.e2e_steps):
+            t0 = time.perf_counter()
+            t = eng.count_raw(pin.ptr, nbytes, hdesc)
+            walls.append(time.perf_counter() - t0)
+            n_out = int(t.n)
+            eng.free_table(t)
+        st = eng.stats()
+        w = float(np.mean(walls))
+        e2e = {"value": nk / w, "unit": UNIT, "h2d_bytes_per_step": nbytes,
+               "d2h_bytes_per_step": n_out * 12, "ms_per_step": w * 1000.0,
+               "ms_h2d": st["ms_h2d"], "ms_d2h": st["ms_d2h"]}
+        pin.free()
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u64",
+            "data": "synthetic (seeded generator; ART-simulated datasets are not available)",
+            "config": dict(cfg, variant=args.variant, l2_flush="inputs (3.02 GB) larger than L2",
+                           parallelism=f"replicas x{world}"),
+            "gpu_launches": launches,
+            "roofline": {"bound": "hbm", "kernel": KERNEL_NAMES[top], "achieved": achieved,
+                         "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
+                         "traffic": traffic, "peak_kind": peak_kind,
+                         "alg_bytes_per_launch": ab[top] / max(kl[top], 1),
+                         "ms_per_launch": kms[top] / max(kl[top], 1)},
+            "pipeline_roofline": {"b_alg": b_alg, "achieved": pipe, "peak": hbm_peak,
+                                  "unit": "GB/s", "frac": pipe / hbm_peak,
+                                  "frac_nominal_8tbs": pipe / 8000.0},
+            "kernels_ms_per_step": {KERNEL_NAMES[i]: float(kms[i]) for i in range(8)},
+            "n_kmers": nk, "n_distinct": nd, "partition_levels": sts[0]["partition_levels"],
+            "wall_ms_per_step": (w1 - w0) * 1000.0 / args.steps,
+            "clocks": clk,
+            "e2e": e2e,
+            "cpu_baseline": ({k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")}
+                             if cpu else None),
+        }
+        print(json.dumps(line), flush=True)
+    eng.close()
+    dist.close()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -80,11 +80,18 @@ class Stats(ctypes.Structure):
                 ("n_kmers", ctypes.c_uint64), ("n_distinct", ctypes.c_uint64),
                 ("n_lines", ctypes.c_uint64), ("kernel_launches", ctypes.c_uint64),
                 ("dev_bytes_peak", ctypes.c_uint64), ("variant_used", ctypes.c_int),
-                ("partition_levels", ctypes.c_int), ("n_bins", ctypes.c_uint64)]
+                ("partition_levels", ctypes.c_int), ("n_bins", ctypes.c_uint64),
+                ("ms_kernel", ctypes.c_double * 8), ("launches_kernel", ctypes.c_uint64 * 8),
+                ("n_partitioned", ctypes.c_uint64)]
+
+    KERNEL_NAMES = ["extract_count", "extract_scatter", "partition_hist", "partition_scatter",
+                    "bin_count", "compact", "hash_insert", "other"]
 
     def as_dict(self) -> dict:
-        d = {f: getattr(self, f) for f, _ in self._fields_ if f != "ms_stage"}
-        d["ms_stage"] = list(self.ms_stage)
+        arrays = ("ms_stage", "ms_kernel", "launches_kernel")
+        d = {f: getattr(self, f) for f, _ in self._fields_ if f not in arrays}
+        for a in arrays:
+            d[a] = list(getattr(self, a))
         return d
 
 

@@ -88,6 +88,42 @@ void Arena::release(Engine* e, DevBuf& b) {
 
 void Engine::set_error(const std::string& m) { last_error = m; }
 
+// per-kernel CUDA-event timing on the engine stream; resolved after the final sync
+int Engine::kbegin() {
+  if (kev_next >= kKEvents) return -1;
+  const int i = kev_next++;
+  cudaEventRecord(kev_pool[i], stream);
+  return i;
+}
+
+void Engine::kend(int slot, int i0, int n) {
+  if (i0 < 0 || kev_next >= kKEvents || n == 0) return;
+  const int i1 = kev_next++;
+  cudaEventRecord(kev_pool[i1], stream);
+  kev.push_back({slot, i0, i1, n});
+}
+
+void Engine::kresolve() {
+  for (const auto& r : kev) {
+    float ms = 0;
+    if (cudaEventElapsedTime(&ms, kev_pool[r.e0], kev_pool[r.e1]) == cudaSuccess) {
+      stats.ms_kernel[r.slot] += ms;
+      stats.launches_kernel[r.slot] += (uint64_t)r.n;
+    }
+  }
+  cudaGetLastError();
+  kev.clear();
+  kev_next = 0;
+}
+
+#define TIMED(slot, expr)              \
+  do {                                 \
+    const int _i0 = kbegin();          \
+    const int _n = (expr);             \
+    launches += (uint64_t)_n;          \
+    kend((slot), _i0, _n);             \
+  } while (0)
+
 int Engine::init(const dk_config* cfg) {
   Engine* e = this;
   device = cfg ? cfg->device : 0;
@@ -110,6 +146,7 @@ int Engine::init(const dk_config* cfg) {
   budget = (cfg && cfg->mem_budget) ? cfg->mem_budget : (uint64_t)(0.8 * (double)fr);
   DK_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
   for (auto& ev : ev_stage) DK_CUDA(cudaEventCreate(&ev));
+  for (auto& ev : kev_pool) DK_CUDA(cudaEventCreate(&ev));
   DK_CUDA(cudaEventCreate(&ev_h2d0));
   DK_CUDA(cudaEventCreate(&ev_d2h1));
   DK_CUDA(cudaMallocHost(&h_scratch, 256));
@@ -130,6 +167,8 @@ Engine::~Engine() {
     }
   }
   for (auto& ev : ev_stage)
+    if (ev) cudaEventDestroy(ev);
+  for (auto& ev : kev_pool)
     if (ev) cudaEventDestroy(ev);
   if (ev_h2d0) cudaEventDestroy(ev_h2d0);
   if (ev_d2h1) cudaEventDestroy(ev_d2h1);
@@ -257,6 +296,8 @@ int Engine::count_device(const uint8_t* d_text, uint64_t nbytes, const dk_input_
   }
   uint64_t L = (uint64_t)L0;
   launches = 0;
+  kev.clear();
+  kev_next = 0;
   DK_CUDA(cudaEventRecord(ev_stage[0], stream));
   const uint64_t per_line = (W >= k) ? (uint64_t)(W - k + 1) : 0;
   if (L == 0 || per_line == 0) {
@@ -302,7 +343,7 @@ int Engine::count_device(const uint8_t* d_text, uint64_t nbytes, const dk_input_
   for (int attempt = 0; attempt < 2; ++attempt) {
     a.n_lines = L;
     DK_CUDA(cudaMemsetAsync(ctrs.p, 0, 256, stream));
-    launches += launch_l1_count(a, G, (uint32_t*)H.p, c64, stream);
+    TIMED(0, launch_l1_count(a, G, (uint32_t*)H.p, c64, stream));
     uint64_t hc[2];
     DK_TRY(sync_read(c64, 16, hc));
     if (hc[1] == 0) {
@@ -324,11 +365,11 @@ int Engine::count_device(const uint8_t* d_text, uint64_t nbytes, const dk_input_
   // level-1 nodes and offsets
   node_cap_needed = (size_t)F1;
   DK_TRY(Arena::ensure(this, nodes, node_cap_needed * sizeof(Node)));
-  launches += launch_l1_scan((uint32_t*)H.p, G, F1, (uint64_t*)O.p, (Node*)nodes.p, shift1, stream);
+  TIMED(7, launch_l1_scan((uint32_t*)H.p, G, F1, (uint64_t*)O.p, (Node*)nodes.p, shift1, stream));
   DK_TRY(Arena::ensure(this, keysA, n_kmers * 8));
   DK_TRY(Arena::ensure(this, keysB, n_kmers * 8));
   DK_TRY(Arena::ensure(this, cnt, n_kmers * 4));
-  launches += launch_l1_scatter(a, G, (const uint64_t*)O.p, (uint64_t*)keysA.p, stream);
+  TIMED(1, launch_l1_scatter(a, G, (const uint64_t*)O.p, (uint64_t*)keysA.p, stream));
   DK_CUDA(cudaEventRecord(ev_stage[2], stream));
 
   // partition levels
@@ -355,7 +396,7 @@ int Engine::count_device(const uint8_t* d_text, uint64_t nbytes, const dk_input_
       }
     }
     DK_CUDA(cudaMemsetAsync((char*)lc + 4, 0, 28, stream));  // keep n_final
-    launches += launch_classify((Node*)nodes.p, lo, hi, (uint32_t*)finals.p, lc, kBinCap, stream);
+    TIMED(7, launch_classify((Node*)nodes.p, lo, hi, (uint32_t*)finals.p, lc, kBinCap, stream));
     DK_TRY(sync_read(lc, 32, hc));
     const uint32_t n_split = hc[1], n_tiles = hc[2];
     if (hc[3]) {
@@ -363,6 +404,9 @@ int Engine::count_device(const uint8_t* d_text, uint64_t nbytes, const dk_input_
       return DK_ERR_INVALID_ARG;
     }
     if (n_split == 0) break;
+    uint64_t split_keys = 0;
+    std::memcpy(&split_keys, &hc[6], 8);
+    stats.n_partitioned += split_keys;
     // grow node storage for the children (copying existing nodes)
     const size_t need_nodes = (size_t)hi + (size_t)n_split * kFanout;
     if (nodes.cap < need_nodes * sizeof(Node)) {
@@ -374,12 +418,12 @@ int Engine::count_device(const uint8_t* d_text, uint64_t nbytes, const dk_input_
     }
     DK_TRY(Arena::ensure(this, tiles, (size_t)n_tiles * sizeof(Tile)));
     DK_TRY(Arena::ensure(this, TH, (size_t)n_tiles * kFanout * 4));
-    launches += launch_assign((Node*)nodes.p, lo, hi, hi, (Tile*)tiles.p, lc, stream);
-    launches += launch_tile_hist((Node*)nodes.p, (Tile*)tiles.p, n_tiles, (uint64_t*)keysA.p,
-                                 (uint64_t*)keysB.p, (uint32_t*)TH.p, stream);
-    launches += launch_node_scan((Node*)nodes.p, lo, hi, (Tile*)tiles.p, (uint32_t*)TH.p, stream);
-    launches += launch_tile_scatter((Node*)nodes.p, (Tile*)tiles.p, n_tiles, (uint64_t*)keysA.p,
-                                    (uint64_t*)keysB.p, (uint32_t*)TH.p, stream);
+    TIMED(7, launch_assign((Node*)nodes.p, lo, hi, hi, (Tile*)tiles.p, lc, stream));
+    TIMED(2, launch_tile_hist((Node*)nodes.p, (Tile*)tiles.p, n_tiles, (uint64_t*)keysA.p,
+                              (uint64_t*)keysB.p, (uint32_t*)TH.p, stream));
+    TIMED(7, launch_node_scan((Node*)nodes.p, lo, hi, (Tile*)tiles.p, (uint32_t*)TH.p, stream));
+    TIMED(3, launch_tile_scatter((Node*)nodes.p, (Tile*)tiles.p, n_tiles, (uint64_t*)keysA.p,
+                                 (uint64_t*)keysB.p, (uint32_t*)TH.p, stream));
     lo = hi;
     hi = hi + n_split * kFanout;
   }
@@ -389,15 +433,15 @@ int Engine::count_device(const uint8_t* d_text, uint64_t nbytes, const dk_input_
   DK_TRY(sync_read(lc, 32, hc));
   const uint32_t n_final = hc[0];
   stats.n_bins = n_final;
-  launches += launch_bin_count((Node*)nodes.p, (uint32_t*)finals.p, n_final, (uint64_t*)keysA.p,
-                               (uint64_t*)keysB.p, (uint32_t*)cnt.p, desc.variant, overflow, stream);
+  TIMED(4, launch_bin_count((Node*)nodes.p, (uint32_t*)finals.p, n_final, (uint64_t*)keysA.p,
+                            (uint64_t*)keysB.p, (uint32_t*)cnt.p, desc.variant, overflow, stream));
   DK_CUDA(cudaEventRecord(ev_stage[4], stream));
   // distinct counts up the tree, offsets down
   for (int l = (int)levels.size() - 2; l >= 0; --l)
-    launches += launch_aggregate((Node*)nodes.p, levels[l].first, levels[l].second, stream);
-  launches += launch_l1_offsets((Node*)nodes.p, (uint32_t)F1, c64 + 2, stream);
+    TIMED(7, launch_aggregate((Node*)nodes.p, levels[l].first, levels[l].second, stream));
+  TIMED(7, launch_l1_offsets((Node*)nodes.p, (uint32_t)F1, c64 + 2, stream));
   for (size_t l = 0; l + 1 < levels.size(); ++l)
-    launches += launch_child_offsets((Node*)nodes.p, levels[l].first, levels[l].second, stream);
+    TIMED(7, launch_child_offsets((Node*)nodes.p, levels[l].first, levels[l].second, stream));
   uint64_t tail[2];
   DK_TRY(sync_read(c64 + 2, 16, tail));
   const uint64_t n_distinct = tail[0];
@@ -415,8 +459,8 @@ int Engine::count_device(const uint8_t* d_text, uint64_t nbytes, const dk_input_
     set_error("internal: no output buffers");
     return DK_ERR_INVALID_ARG;
   }
-  launches += launch_compact((Node*)nodes.p, (uint32_t*)finals.p, n_final, (uint64_t*)keysA.p,
-                             (uint64_t*)keysB.p, (uint32_t*)cnt.p, out_k, out_c, stream);
+  TIMED(5, launch_compact((Node*)nodes.p, (uint32_t*)finals.p, n_final, (uint64_t*)keysA.p,
+                          (uint64_t*)keysB.p, (uint32_t*)cnt.p, out_k, out_c, stream));
   DK_CUDA(cudaGetLastError());
   DK_CUDA(cudaEventRecord(ev_stage[5], stream));
   DK_CUDA(cudaEventSynchronize(ev_stage[5]));
@@ -432,6 +476,7 @@ int Engine::count_device(const uint8_t* d_text, uint64_t nbytes, const dk_input_
   stats.n_kmers = n_kmers;
   stats.n_distinct = n_distinct;
   stats.kernel_launches = launches;
+  kresolve();
   return DK_OK;
 }
 

@@ -5,6 +5,7 @@
 #include <mutex>
 #include <string>
 #include <deque>
+#include <vector>
 
 #include "../../include/dakc_gb300.h"
 
@@ -62,6 +63,14 @@ struct Engine {
   uint64_t table_ids = 0;
 
   cudaEvent_t ev_stage[8] = {};
+  static constexpr int kKEvents = 128;
+  struct KEv { int slot, e0, e1, n; };
+  cudaEvent_t kev_pool[kKEvents] = {};
+  std::vector<KEv> kev;
+  int kev_next = 0;
+  int kbegin();
+  void kend(int slot, int i0, int n);
+  void kresolve();
   cudaEvent_t ev_h2d0 = nullptr, ev_d2h1 = nullptr;
   void* h_scratch = nullptr;
   void* stage_pinned[2] = {nullptr, nullptr};

@@ -40,8 +40,9 @@ struct LevelCounters {
   uint32_t too_big;  // a split node holds >= 2^32 keys
   uint32_t n_children;
   uint32_t n_tiles_assigned;
-  uint32_t pad[2];
+  unsigned long long split_keys;  // keys held by this level's split nodes
 };
+static_assert(sizeof(LevelCounters) == 32, "LevelCounters is read back as 32 bytes");
 
 constexpr int kDigitBits = 8;           // fan-out of partition levels 2+
 constexpr int kFanout = 1 << kDigitBits;

@@ -326,6 +326,7 @@ __global__ void k_classify(Node* nodes, uint32_t lo, uint32_t hi, uint32_t* fina
   }
   nodes[i].state = NODE_SPLIT;
   atomicAdd(&ctr->n_split, 1u);
+  atomicAdd(&ctr->split_keys, (unsigned long long)nd.n);
   atomicAdd(&ctr->n_tiles, (uint32_t)((nd.n + kTileKeys - 1) / kTileKeys));
   if (nd.n >= (1ull << 32)) atomicOr(&ctr->too_big, 1u);
 }

@@ -109,6 +109,13 @@ typedef struct {
   int variant_used;
   int partition_levels;
   uint64_t n_bins;
+  /* CUDA-event time of the main kernels (ms, summed over launches):
+     [0] extract+count  [1] extract+scatter  [2] partition histogram
+     [3] partition scatter  [4] bin count  [5] compact  [6] hash insert
+     [7] everything else (scans, classify, tree offsets) */
+  double ms_kernel[8];
+  uint64_t launches_kernel[8];
+  uint64_t n_partitioned;  /* keys moved by partition levels below level 1    */
 } dk_stats;
 
 /* One read set of a batch (dk_count_batch). */
