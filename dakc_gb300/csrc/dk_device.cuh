@@ -1,0 +1,180 @@
+// Device helpers shared by the engine kernels (warp-per-line k-mer
+// extraction, block scans, shared-memory bitonic sort).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace dk {
+namespace dev {
+
+__device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31; }
+
+// base code of one text byte: C=0 A=1 T=2 G=3 (either case), M/m=0xF0, else 0xFF
+__device__ __forceinline__ void init_lut(uint8_t* lut) {
+  for (int c = threadIdx.x; c < 256; c += blockDim.x) {
+    uint8_t v = 0xFF;
+    const int u = c | 0x20;  // exact case fold for the five letters below
+    if (u == 'c') v = 0;
+    else if (u == 'a') v = 1;
+    else if (u == 't') v = 2;
+    else if (u == 'g') v = 3;
+    else if (u == 'm') v = 0xF0;
+    lut[c] = v;
+  }
+}
+
+// Walk one line with one warp.  Lane i owns positions seg + i*C .. seg + i*C + C-1.
+// f(t, key, valid) is called for t = 0..C-1 (once per segment of 32*C positions).
+template <int C, typename F>
+__device__ __forceinline__ void warp_line_kmers(const uint8_t* __restrict__ line, int W, int k,
+                                                uint64_t kmask, const uint8_t* __restrict__ lut,
+                                                F&& f) {
+  const uint32_t lane = lane_id();
+  constexpr int B = 2 * C;  // bits per lane chunk
+  uint64_t carry_win = 0;
+  int carry_lb = -1;
+  int carry_stop = W;
+  // k = 1 keeps a final run only if it starts before W-1 (kcounter_funcs.cpp:97)
+  const bool k1_drop_last = (k == 1) && (W == 1 || lut[line[W - 2]] == 0xFF);
+  for (int seg = 0; seg < W; seg += 32 * C) {
+    const int p0 = seg + (int)lane * C;
+    uint64_t chunk = 0;
+    int lb_lane = -1, firstM = 0x7FFFFFFF;
+    uint32_t bad_mask = 0;  // bit t: position p0+t is not a base
+#pragma unroll
+    for (int t = 0; t < C; ++t) {
+      const int p = p0 + t;
+      uint8_t c = 0xFF;
+      if (p < W) c = lut[__ldg(line + p)];
+      chunk = (chunk << 2) | (c & 3u);
+      if (c >= 4) { lb_lane = p; bad_mask |= (1u << t); }
+      if (c == 0xF0 && firstM == 0x7FFFFFFF) firstM = p;
+    }
+    // first 'M' over the warp
+    int m = firstM;
+#pragma unroll
+    for (int o = 16; o; o >>= 1) m = min(m, __shfl_xor_sync(0xFFFFFFFFu, m, o));
+    const int stop = min(carry_stop, m);
+    // last non-base position before this lane's chunk (exclusive max scan)
+    int lb_inc = lb_lane;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int v = __shfl_up_sync(0xFFFFFFFFu, lb_inc, o);
+      if ((int)lane >= o) lb_inc = max(lb_inc, v);
+    }
+    int lb_exc = __shfl_up_sync(0xFFFFFFFFu, lb_inc, 1);
+    if (lane == 0) lb_exc = -1;
+    lb_exc = max(lb_exc, carry_lb);
+    // 2-bit window of all bases before this lane's chunk (exclusive shift-or scan)
+    uint64_t w_inc = chunk;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint64_t v = __shfl_up_sync(0xFFFFFFFFu, w_inc, o);
+      if ((int)lane >= o && B * o < 64) w_inc |= v << (B * o);
+    }
+    uint64_t w_exc = __shfl_up_sync(0xFFFFFFFFu, w_inc, 1);
+    if (lane == 0) w_exc = 0;
+    if (B * (int)lane < 64) w_exc |= carry_win << (B * lane);
+    // k-mers ending at each of this lane's positions
+    int lb = lb_exc;
+#pragma unroll
+    for (int t = 0; t < C; ++t) {
+      const int p = p0 + t;
+      if (bad_mask & (1u << t)) lb = p;
+      const int up = 2 * (t + 1);
+      const uint64_t win = (up < 64 ? (w_exc << up) : 0ull) | (chunk >> (2 * (C - 1 - t)));
+      const uint64_t key = win & kmask;
+      bool valid = (p < stop) && (p - lb >= k);
+      if (k1_drop_last && p == W - 1) valid = false;
+      f(t, key, valid);
+    }
+    // carry to the next segment
+    const uint64_t win_all = __shfl_sync(0xFFFFFFFFu, w_inc, 31);
+    carry_win = (B * 32 < 64) ? ((carry_win << (B * 32)) | win_all) : win_all;
+    carry_lb = max(carry_lb, __shfl_sync(0xFFFFFFFFu, lb_inc, 31));
+    carry_stop = stop;
+  }
+}
+
+// block-wide exclusive scan of one value per thread; returns exclusive prefix,
+// *total receives the block sum.  `tmp` needs 32 slots.
+template <typename T>
+__device__ __forceinline__ T block_excl_scan(T v, T* tmp, T* total) {
+  const uint32_t lane = lane_id(), warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  T x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const T y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+    if ((int)lane >= o) x += y;
+  }
+  if (lane == 31) tmp[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    T w = (lane < nw) ? tmp[lane] : T(0);
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const T y = __shfl_up_sync(0xFFFFFFFFu, w, o);
+      if ((int)lane >= o) w += y;
+    }
+    if (lane < nw) tmp[lane] = w;  // inclusive warp totals
+  }
+  __syncthreads();
+  const T warp_base = warp ? tmp[warp - 1] : T(0);
+  if (total) *total = tmp[nw - 1];
+  __syncthreads();
+  return warp_base + x - v;
+}
+
+// exclusive scan of arr[0..len) in shared memory by the whole block; returns the total
+template <typename T>
+__device__ T block_scan_array(T* arr, int len, T* tmp) {
+  const int per = (len + blockDim.x - 1) / blockDim.x;
+  const int lo = min(len, (int)threadIdx.x * per), hi = min(len, lo + per);
+  T s = 0;
+  for (int i = lo; i < hi; ++i) s += arr[i];
+  T total;
+  T base = block_excl_scan<T>(s, tmp, &total);
+  for (int i = lo; i < hi; ++i) { const T c = arr[i]; arr[i] = base; base += c; }
+  __syncthreads();
+  return total;
+}
+
+__device__ __forceinline__ void lines_of_block(uint64_t n_lines, uint64_t* lo, uint64_t* hi) {
+  *lo = n_lines * blockIdx.x / gridDim.x;
+  *hi = n_lines * (blockIdx.x + 1) / gridDim.x;
+}
+
+__device__ __forceinline__ int ceil_log2_u64(uint64_t x) { return x <= 1 ? 0 : 64 - __clzll(x - 1); }
+
+// sort skeys[lo, lo+m) ascending with the whole block (always-ascending
+// bitonic network; out-of-range partners act as +inf and never move)
+__device__ inline void block_bitonic(unsigned long long* s, uint32_t m) {
+  uint32_t P = 1;
+  while (P < m) P <<= 1;
+  for (uint32_t size = 2; size <= P; size <<= 1) {
+    const uint32_t half = size >> 1;
+    for (uint32_t i = threadIdx.x; i < P / 2; i += blockDim.x) {
+      const uint32_t a = (i / half) * size + (i % half);
+      const uint32_t b = a ^ (size - 1);
+      if (b < m) {
+        const unsigned long long x = s[a], y = s[b];
+        if (y < x) { s[a] = y; s[b] = x; }
+      }
+    }
+    __syncthreads();
+    for (uint32_t st = half >> 1; st > 0; st >>= 1) {
+      for (uint32_t i = threadIdx.x; i < P / 2; i += blockDim.x) {
+        const uint32_t a = (i / st) * 2 * st + (i % st);
+        const uint32_t b = a + st;
+        if (b < m) {
+          const unsigned long long x = s[a], y = s[b];
+          if (y < x) { s[a] = y; s[b] = x; }
+        }
+      }
+      __syncthreads();
+    }
+  }
+}
+
+}  // namespace dev
+}  // namespace dk

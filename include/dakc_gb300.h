@@ -156,6 +156,36 @@ int64_t dk_num_lines(const char* text, uint64_t nbytes, int line_width);
 int dk_host_alloc(uint64_t nbytes, void** out);
 int dk_host_free(void* p);
 
+/* --- counting without any allocation ------------------------------------
+ * No counterpart in the reference: DAKC always allocates its buffers.
+ *
+ * For callers that cannot allocate memory at the point where they need a
+ * count -- code running inside a memory allocator's callback, latency-bound
+ * serving or real-time loops that must not take the allocator's locks or its
+ * device-wide synchronisation, or programs that own all device memory
+ * through their own pool.  dk_count needs a context whose work buffers are
+ * allocated on demand; this call needs none.  The caller passes the reads
+ * (d_text, device memory), the output table (d_kmers / d_counts, device
+ * memory, at least `capacity` entries) and d_summary (device memory, 3
+ * uint64: distinct k-mers, k-mer occurrences, status 0 = ok).  The call is
+ * asynchronous on `stream` (a cudaStream_t, NULL for the default stream) on
+ * the current device and allocates nothing: its only scratch is one fixed
+ * array of 147,712 bytes that the library reserves on every GPU that loads
+ * it, until the process exits.
+ *   - Inputs whose k-mer upper bound, lines * (line_width - k + 1), exceeds
+ *     12,288 are rejected with DK_ERR_ADMISSION before any launch;
+ *     capacity must be at least that bound (else DK_ERR_INVALID_ARG).
+ *   - Every call shares the scratch array and leaves its contents behind;
+ *     calls whose kernels overlap on the GPU (different streams or threads)
+ *     race on it: serialise them on one stream.
+ *   - The first call on a device does a one-time set-up (it looks up the
+ *     array's device address and sets the kernel's shared-memory limit);
+ *     make that first call before any stream capture on that device.
+ * Results equal dk_count's table for the same reads. */
+int dk_count_small_noalloc(const char* d_text, uint64_t nbytes, int line_width, int k,
+                           uint64_t* d_kmers, uint32_t* d_counts, uint64_t capacity,
+                           uint64_t* d_summary, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
