@@ -44,7 +44,7 @@ CONV_DAKC = 0
 ABI_SYMBOLS = [
     "dk_create", "dk_destroy", "dk_strerror", "dk_last_error_string", "dk_abi_version",
     "dk_count", "dk_count_device", "dk_table_free", "dk_last_stats", "dk_num_lines",
-    "dk_host_alloc", "dk_host_free",
+    "dk_host_alloc", "dk_host_free", "dk_count_small_noalloc",
 ]
 
 

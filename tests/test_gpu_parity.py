@@ -3,6 +3,11 @@
 Every case compares the full table (sorted distinct k-mers, their uint32
 counts) and the occurrence total.  Integer work: the bar is exact equality.
 """
+import glob
+import hashlib
+import json
+import os
+
 import numpy as np
 import pytest
 
@@ -31,6 +36,31 @@ def lines(*rows, W):
         assert len(r) <= W
         out += r + b"M" * (W - len(r)) + b"\n"
     return out
+
+
+# ------------------------------------------- the reference's own tables
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+FIXTURES = sorted(glob.glob(os.path.join(GOLDEN, "*.npz")))
+
+
+@pytest.mark.parametrize("variant", VARIANTS)
+@pytest.mark.parametrize("path", FIXTURES, ids=[os.path.basename(p)[:-4] for p in FIXTURES])
+def test_reference_fixture(engine, variant, path):
+    z = np.load(path)
+    got = engine.count(z["text"], int(z["W"]), int(z["k"]), variant)
+    assert got.n_kmers == int(z["n_kmers"])
+    assert np.array_equal(got.kmers, z["keys"])
+    assert np.array_equal(got.counts, z["counts"])
+
+
+@pytest.mark.parametrize("variant", VARIANTS)
+def test_reference_digest_plain_1m(engine, variant):
+    with open(os.path.join(GOLDEN, "index.json")) as f:
+        ent = json.load(f)["cases"]["plain_1m"]
+    rs = synth.plain_1m()
+    got = engine.count(rs.text, 150, 31, variant)
+    h = hashlib.sha256(got.kmers.tobytes() + got.counts.tobytes()).hexdigest()
+    assert got.n_kmers == ent["n_kmers"] and h == ent["table_sha256"]
 
 
 # ------------------------------------------------------------ known answers

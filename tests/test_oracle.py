@@ -1,0 +1,133 @@
+"""The CPU oracle, pinned against the reference's own output (CPU only).
+
+tests/golden/*.npz hold tables produced by the reference's counting sources
+(see tests/golden/make_golden.py).  The oracle must reproduce every one bit
+for bit before it is trusted as the GPU engine's checker.
+"""
+import glob
+import hashlib
+import json
+import os
+
+import numpy as np
+import pytest
+
+from dakc_gb300 import synth
+from oracle import pyoracle
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+FIXTURES = sorted(glob.glob(os.path.join(GOLDEN, "*.npz")))
+
+
+def load(path):
+    z = np.load(path)
+    return z["text"], int(z["W"]), int(z["k"]), z["keys"], z["counts"], int(z["n_kmers"])
+
+
+def test_fixtures_present():
+    assert len(FIXTURES) >= 10
+    with open(os.path.join(GOLDEN, "index.json")) as f:
+        idx = json.load(f)["cases"]
+    for p in FIXTURES:
+        name = os.path.basename(p)[:-4]
+        text, W, k, keys, counts, nk = load(p)
+        assert idx[name]["text_sha256"] == hashlib.sha256(text.tobytes()).hexdigest()
+        assert idx[name]["n_distinct"] == keys.size and idx[name]["n_kmers"] == nk
+
+
+@pytest.mark.parametrize("path", FIXTURES, ids=[os.path.basename(p)[:-4] for p in FIXTURES])
+def test_oracle_matches_reference_fixture(path):
+    text, W, k, keys, counts, nk = load(path)
+    got_k, got_c, got_n = pyoracle.count(text, W, k)
+    assert got_n == nk
+    assert np.array_equal(got_k, keys)
+    assert np.array_equal(got_c, counts)
+    assert int(counts.astype(np.uint64).sum()) == nk
+
+
+@pytest.mark.parametrize("path", FIXTURES[:6], ids=[os.path.basename(p)[:-4] for p in FIXTURES[:6]])
+def test_port_matches_reference_fixture(path):
+    text, W, k, keys, counts, nk = load(path)
+    for pes in (1, 3):
+        (gk, gc, gn), secs = pyoracle.dakc_port(text, W, k, pes)
+        assert gn == nk and np.array_equal(gk, keys) and np.array_equal(gc, counts)
+
+
+def test_plain_1m_digest():
+    with open(os.path.join(GOLDEN, "index.json")) as f:
+        ent = json.load(f)["cases"]["plain_1m"]
+    rs = synth.plain_1m()
+    assert hashlib.sha256(rs.text.tobytes()).hexdigest() == ent["text_sha256"]
+    keys, counts, nk = pyoracle.count(rs.text, 150, 31)
+    assert nk == ent["n_kmers"] and keys.size == ent["n_distinct"]
+    assert hashlib.sha256(keys.tobytes() + counts.tobytes()).hexdigest() == ent["table_sha256"]
+
+
+def test_known_answers():
+    # hand-derived from the convention: C=0 A=1 T=2 G=3, MSB-first
+    assert pyoracle.count(b"CAT\n", 3, 3)[0].tolist() == [6]
+    assert pyoracle.count(b"GGG\n", 3, 3)[0].tolist() == [63]
+    assert pyoracle.count(b"ACG\n", 3, 3)[0].tolist() == [19]
+    assert pyoracle.count(b"CANTG\n", 5, 3)[0].size == 0
+    assert pyoracle.count(b"CATMAAA\n", 7, 3)[0].tolist() == [6]
+    assert pyoracle.count(b"G" * 32 + b"\n", 32, 32)[0].tolist() == [2 ** 64 - 1]
+    keys, counts, nk = pyoracle.count(b"AAAAA\nAAAAA\n", 5, 3)
+    assert keys.tolist() == [0b010101] and counts.tolist() == [6] and nk == 6
+
+
+def test_code_table():
+    t = pyoracle.code_table()
+    expect = np.full(256, 0xFF, np.uint8)
+    for chars, v in ((b"Cc", 0), (b"Aa", 1), (b"Tt", 2), (b"Gg", 3), (b"Mm", 0xF0)):
+        for c in chars:
+            expect[c] = v
+    assert np.array_equal(t, expect)
+
+
+def test_framing():
+    W = 5
+    assert pyoracle.num_lines(b"", W) == 0
+    assert pyoracle.num_lines(b"ACGTA\nACGTA\n", W) == 2
+    assert pyoracle.num_lines(b"ACGTA\nACGTA", W) == 2       # last terminator missing
+    assert pyoracle.num_lines(b"ACGTA\nACG", W) == -1        # partial line
+    assert pyoracle.num_lines(b"ACGTA\n\0CGTA\nACGTA\n", W) == 1  # NUL-led line stops parsing
+    assert pyoracle.num_lines(b"\0CGTA\nACGTA\n", W) == 2    # line 0 is always parsed
+    with pytest.raises(pyoracle.OracleError):
+        pyoracle.count(b"ACGTA\nACG", W, 3)
+
+
+def test_k1_last_run_rule():
+    # a final run starting at W-1 is not emitted (kcounter_funcs.cpp:97)
+    assert pyoracle.count(b"ACGTNA\n", 6, 1)[2] == 4
+    assert pyoracle.count(b"ACGTAA\n", 6, 1)[2] == 6
+    assert pyoracle.count(b"A\n", 1, 1)[2] == 0
+
+
+def test_port_equals_oracle_random():
+    text = synth.random_lines(11, 3000, 150, b"ACGTACGTACGTN")
+    ref = pyoracle.count(text, 150, 21)
+    for pes in (1, 2, 5, 8):
+        (k, c, n), _ = pyoracle.dakc_port(text, 150, 21, pes)
+        assert n == ref[2] and np.array_equal(k, ref[0]) and np.array_equal(c, ref[1])
+
+
+def test_murmur_owner_spreads_keys():
+    # DAKC's owner hash (kcounter.cpp:29-54) must spread consecutive keys over PEs
+    owners = [pyoracle.murmur64a(i) % 16 for i in range(4096)]
+    counts = np.bincount(owners, minlength=16)
+    assert counts.min() > 180 and counts.max() < 340
+
+
+def _reference_available():
+    return pyoracle.ref_binary(31, 150, 0, build=True) is not None
+
+
+@pytest.mark.skipif(not os.path.isdir(pyoracle.REFERENCE_TREE), reason="reference tree absent")
+def test_oracle_matches_live_reference():
+    assert _reference_available()
+    g = synth.genome_uniform(51, 100_000)
+    text = synth.reads(52, g, 3000, 150, 150, 150, rc_frac=0.5, err_rate=0.02)
+    ref, out = pyoracle.ref_table(text, 150, 31, pes=3)
+    mine = pyoracle.count(text, 150, 31)
+    assert "kmer counting time" in out
+    assert ref[2] == mine[2] and np.array_equal(ref[0], mine[0]) and np.array_equal(ref[1], mine[1])
