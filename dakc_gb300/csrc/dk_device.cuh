@@ -45,7 +45,7 @@ __device__ __forceinline__ void warp_line_kmers(const uint8_t* __restrict__ line
     for (int t = 0; t < C; ++t) {
       const int p = p0 + t;
       uint8_t c = 0xFF;
-      if (p < W) c = lut[__ldg(line + p)];
+      if (p < W) c = lut[line[p]];  // shared-memory tile or global line
       chunk = (chunk << 2) | (c & 3u);
       if (c >= 4) { lb_lane = p; bad_mask |= (1u << t); }
       if (c == 0xF0 && firstM == 0x7FFFFFFF) firstM = p;
@@ -149,23 +149,25 @@ __device__ __forceinline__ int ceil_log2_u64(uint64_t x) { return x <= 1 ? 0 : 6
 // sort skeys[lo, lo+m) ascending with the whole block (always-ascending
 // bitonic network; out-of-range partners act as +inf and never move)
 __device__ inline void block_bitonic(unsigned long long* s, uint32_t m) {
-  uint32_t P = 1;
-  while (P < m) P <<= 1;
-  for (uint32_t size = 2; size <= P; size <<= 1) {
-    const uint32_t half = size >> 1;
+  int lg = 0;
+  while ((1u << lg) < m) ++lg;
+  const uint32_t P = 1u << lg;
+  for (int sz = 1; sz <= lg; ++sz) {  // merge blocks of 2^sz
+    const uint32_t hmask = (1u << (sz - 1)) - 1;
     for (uint32_t i = threadIdx.x; i < P / 2; i += blockDim.x) {
-      const uint32_t a = (i / half) * size + (i % half);
-      const uint32_t b = a ^ (size - 1);
+      const uint32_t a = ((i >> (sz - 1)) << sz) | (i & hmask);
+      const uint32_t b = a ^ ((1u << sz) - 1);
       if (b < m) {
         const unsigned long long x = s[a], y = s[b];
         if (y < x) { s[a] = y; s[b] = x; }
       }
     }
     __syncthreads();
-    for (uint32_t st = half >> 1; st > 0; st >>= 1) {
+    for (int st = sz - 2; st >= 0; --st) {
+      const uint32_t smask = (1u << st) - 1;
       for (uint32_t i = threadIdx.x; i < P / 2; i += blockDim.x) {
-        const uint32_t a = (i / st) * 2 * st + (i % st);
-        const uint32_t b = a + st;
+        const uint32_t a = ((i >> st) << (st + 1)) | (i & smask);
+        const uint32_t b = a + (1u << st);
         if (b < m) {
           const unsigned long long x = s[a], y = s[b];
           if (y < x) { s[a] = y; s[b] = x; }
@@ -174,6 +176,98 @@ __device__ inline void block_bitonic(unsigned long long* s, uint32_t m) {
       __syncthreads();
     }
   }
+}
+
+// ------------------------------------------------ TMA bulk copy + mbarrier
+// 1-D bulk copies (cp.async.bulk) global -> shared, completed on an mbarrier.
+// Addresses must be 16-byte aligned and sizes multiples of 16.
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count)
+               : "memory");
+}
+
+// make initialised barriers visible to the async (TMA) proxy
+__device__ __forceinline__ void fence_barrier_init() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ void tma_load_1d(void* dst, const void* src, uint32_t bytes,
+                                            uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ bool mbar_test(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Wait for phase `parity` of `bar` for at most `limit_ns`; false on timeout.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity,
+                                                  uint64_t limit_ns = 2000000000ull) {
+  if (mbar_test(bar, parity)) return true;
+  const uint64_t t0 = global_ns();
+  while (!mbar_test(bar, parity))
+    if (global_ns() - t0 > limit_ns) return false;
+  return true;
+}
+
+// Stage bytes [src, src+len) of global memory into shared memory at dst16
+// (16-byte aligned, at least len + 32 bytes).  The bulk copy covers the
+// 16-byte-aligned middle; bytes that a whole-16-byte copy would take beyond
+// `limit` (end of the readable global buffer) are loaded by plain loads after
+// the wait.  Returns the offset in dst16 where src's first byte lands.  Call
+// with the whole block; one thread issues the copy.
+struct StagedCopy {
+  uint32_t lead;     // dst16 + lead == copy of src
+  uint32_t bulk;     // bytes moved by the bulk copy
+  const uint8_t* tail_src;
+  uint32_t tail_dst;  // offset in dst16
+  uint32_t tail_len;
+};
+
+__device__ __forceinline__ StagedCopy plan_stage(const uint8_t* src, uint64_t len,
+                                                 const uint8_t* limit) {
+  StagedCopy c;
+  const uintptr_t s = reinterpret_cast<uintptr_t>(src);
+  const uintptr_t a = s & ~uintptr_t(15);
+  c.lead = static_cast<uint32_t>(s - a);
+  const uintptr_t want_end = (s + len + 15) & ~uintptr_t(15);
+  const uintptr_t lim = reinterpret_cast<uintptr_t>(limit) & ~uintptr_t(15);
+  const uintptr_t bulk_end = want_end <= reinterpret_cast<uintptr_t>(limit) ? want_end
+                                                                            : (lim > a ? lim : a);
+  c.bulk = static_cast<uint32_t>(bulk_end - a);
+  const uintptr_t need_end = s + len;
+  c.tail_src = reinterpret_cast<const uint8_t*>(bulk_end);
+  c.tail_dst = c.bulk;
+  c.tail_len = need_end > bulk_end ? static_cast<uint32_t>(need_end - bulk_end) : 0u;
+  return c;
 }
 
 }  // namespace dev

@@ -288,7 +288,9 @@ int Engine::count_device(const uint8_t* d_text, uint64_t nbytes, const dk_input_
   out->k = nullptr;
   out->c = nullptr;
   stats = dk_stats();
-  stats.variant_used = DK_VARIANT_SORT;
+  // the hash-first bin count needs a free sentinel key, i.e. k <= 31
+  const bool use_hash = desc.variant != DK_VARIANT_SORT && desc.k <= 31;
+  stats.variant_used = use_hash ? DK_VARIANT_HASH : DK_VARIANT_SORT;
   int64_t L0 = frame_lines(nbytes, W);
   if (L0 < 0) {
     set_error("buffer size is not a whole number of lines");
@@ -326,6 +328,7 @@ int Engine::count_device(const uint8_t* d_text, uint64_t nbytes, const dk_input_
 
   ExtractArgs a;
   a.text = d_text;
+  a.nbytes = nbytes;
   a.W = W;
   a.k = k;
   a.kmask = (~0ull) >> (64 - 2 * k);
@@ -335,9 +338,11 @@ int Engine::count_device(const uint8_t* d_text, uint64_t nbytes, const dk_input_
   DK_TRY(Arena::ensure(this, H, (size_t)G * F1 * 4));
   DK_TRY(Arena::ensure(this, O, (size_t)G * F1 * 8));
   DK_TRY(Arena::ensure(this, ctrs, 256));
-  unsigned long long* c64 = (unsigned long long*)ctrs.p;        // [0]=n_kmers [1]=nul [2]=total_d
+  // device counters: [0] k-mers, [1] NUL-led line marker, [2] distinct total,
+  // [3] device error (a bounded wait ran out), [4] bin ticket, [5] count overflow;
+  // LevelCounters at byte 64
+  unsigned long long* c64 = (unsigned long long*)ctrs.p;
   LevelCounters* lc = (LevelCounters*)((char*)ctrs.p + 64);
-  int* overflow = (int*)((char*)ctrs.p + 128);
 
   uint64_t n_kmers = 0;
   for (int attempt = 0; attempt < 2; ++attempt) {
@@ -369,7 +374,7 @@ int Engine::count_device(const uint8_t* d_text, uint64_t nbytes, const dk_input_
   DK_TRY(Arena::ensure(this, keysA, n_kmers * 8));
   DK_TRY(Arena::ensure(this, keysB, n_kmers * 8));
   DK_TRY(Arena::ensure(this, cnt, n_kmers * 4));
-  TIMED(1, launch_l1_scatter(a, G, (const uint64_t*)O.p, (uint64_t*)keysA.p, stream));
+  TIMED(1, launch_l1_scatter(a, G, (const uint64_t*)O.p, (uint64_t*)keysA.p, c64, stream));
   DK_CUDA(cudaEventRecord(ev_stage[2], stream));
 
   // partition levels
@@ -434,7 +439,8 @@ int Engine::count_device(const uint8_t* d_text, uint64_t nbytes, const dk_input_
   const uint32_t n_final = hc[0];
   stats.n_bins = n_final;
   TIMED(4, launch_bin_count((Node*)nodes.p, (uint32_t*)finals.p, n_final, (uint64_t*)keysA.p,
-                            (uint64_t*)keysB.p, (uint32_t*)cnt.p, desc.variant, overflow, stream));
+                            (uint64_t*)keysB.p, (uint32_t*)cnt.p, use_hash ? 1 : 0, c64, sm_count,
+                            stream));
   DK_CUDA(cudaEventRecord(ev_stage[4], stream));
   // distinct counts up the tree, offsets down
   for (int l = (int)levels.size() - 2; l >= 0; --l)
@@ -442,12 +448,14 @@ int Engine::count_device(const uint8_t* d_text, uint64_t nbytes, const dk_input_
   TIMED(7, launch_l1_offsets((Node*)nodes.p, (uint32_t)F1, c64 + 2, stream));
   for (size_t l = 0; l + 1 < levels.size(); ++l)
     TIMED(7, launch_child_offsets((Node*)nodes.p, levels[l].first, levels[l].second, stream));
-  uint64_t tail[2];
-  DK_TRY(sync_read(c64 + 2, 16, tail));
+  uint64_t tail[4];
+  DK_TRY(sync_read(c64 + 2, 32, tail));
   const uint64_t n_distinct = tail[0];
-  int ovf = 0;
-  DK_TRY(sync_read(overflow, 4, &ovf));
-  if (ovf) {
+  if (tail[1]) {
+    set_error("a bounded device wait (TMA copy) timed out");
+    return DK_ERR_TIMEOUT;
+  }
+  if (tail[3]) {
     set_error("a k-mer count does not fit 32 bits");
     return DK_ERR_COUNT_OVERFLOW;
   }
@@ -502,6 +510,10 @@ int Engine::count(const char* text, uint64_t nbytes, bool text_on_device, const 
   }
   if (frame_lines(nbytes, desc->line_width) < 0) {
     set_error("buffer size is not a whole number of lines");
+    return DK_ERR_INVALID_ARG;
+  }
+  if (text_on_device && (reinterpret_cast<uintptr_t>(text) & 15)) {
+    set_error("device text must be 16-byte aligned");
     return DK_ERR_INVALID_ARG;
   }
   DK_CUDA(cudaSetDevice(device));

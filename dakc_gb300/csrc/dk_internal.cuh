@@ -47,13 +47,14 @@ static_assert(sizeof(LevelCounters) == 32, "LevelCounters is read back as 32 byt
 constexpr int kDigitBits = 8;           // fan-out of partition levels 2+
 constexpr int kFanout = 1 << kDigitBits;
 constexpr int kTileKeys = 8192;         // keys per partition tile
-constexpr int kBinCap = 12288;          // keys a bin-count CTA sorts in shared memory
+constexpr int kBinCap = 12000;          // keys a bin-count CTA sorts in shared memory
 constexpr int kDenseBits = 12;          // nodes with <= this many free bits are counted densely
 constexpr int kBinThreads = 512;
 constexpr int kMaxL1Bits = 12;          // level-1 fan-out <= 4096 buckets
 
 struct ExtractArgs {
-  const uint8_t* text;  // device text (padded)
+  const uint8_t* text;  // device text, 16-byte aligned
+  uint64_t nbytes;      // readable bytes at text
   uint64_t n_lines;
   int W;
   int k;
@@ -69,7 +70,7 @@ int launch_l1_count(const ExtractArgs& a, int grid, uint32_t* H, unsigned long l
 int launch_l1_scan(const uint32_t* H, int grid, int F1, uint64_t* O, Node* nodes, int shift1,
                    cudaStream_t s);
 int launch_l1_scatter(const ExtractArgs& a, int grid, const uint64_t* O, uint64_t* keys,
-                      cudaStream_t s);
+                      unsigned long long* counters, cudaStream_t s);
 int launch_classify(Node* nodes, uint32_t node_lo, uint32_t node_hi, uint32_t* final_list,
                     LevelCounters* ctr, int bin_cap, cudaStream_t s);
 int launch_assign(Node* nodes, uint32_t node_lo, uint32_t node_hi, uint32_t child_base,
@@ -80,8 +81,11 @@ int launch_node_scan(Node* nodes, uint32_t node_lo, uint32_t node_hi, const Tile
                      uint32_t* TH, cudaStream_t s);
 int launch_tile_scatter(const Node* nodes, const Tile* tiles, uint32_t n_tiles, uint64_t* A,
                         uint64_t* B, const uint32_t* TH, cudaStream_t s);
+// ctr: [4] (low 32 bits) = bin ticket, [5] = count overflow flag, [6] = hash bins that fell
+// back to sorting (all zeroed by the caller); use_hash selects the hash-first bin count
 int launch_bin_count(Node* nodes, const uint32_t* final_list, uint32_t n_final, uint64_t* A,
-                     uint64_t* B, uint32_t* C, int variant, int* overflow, cudaStream_t s);
+                     uint64_t* B, uint32_t* C, int use_hash, unsigned long long* ctr, int sm_count,
+                     cudaStream_t s);
 int launch_aggregate(Node* nodes, uint32_t node_lo, uint32_t node_hi, cudaStream_t s);
 int launch_l1_offsets(Node* nodes, uint32_t n1, unsigned long long* total_d, cudaStream_t s);
 int launch_child_offsets(Node* nodes, uint32_t node_lo, uint32_t node_hi, cudaStream_t s);

@@ -26,6 +26,7 @@
 // the first 'M' (min) across lanes, so every k-mer is formed in registers.
 #include "dk_internal.cuh"
 #include "dk_device.cuh"
+#include <algorithm>
 #include <cstdio>
 
 namespace dk {
@@ -34,28 +35,148 @@ namespace {
 
 using namespace dev;
 
+// Optional bounds self-checks (build with -DDK_BOUNDS_CHECK): a failed check
+// records (code, detail) in g_check and skips the access.
+#ifdef DK_BOUNDS_CHECK
+__device__ unsigned long long g_check[4];
+#define DK_OK_IDX(cond, code, detail)                                                  \
+  ((cond) ? true                                                                       \
+          : (atomicCAS(&g_check[0], 0ull, (unsigned long long)(code)) == 0ull          \
+                 ? (g_check[1] = (unsigned long long)(detail), false)                  \
+                 : false))
+#else
+#define DK_OK_IDX(cond, code, detail) true
+#endif
+
+// Optional per-phase cycle counters for the bin kernel (build with
+// -DDK_PHASE_TIMING; read them with dk_debug_phases).  Compiled out otherwise.
+#ifdef DK_PHASE_TIMING
+__device__ unsigned long long g_phase[16];
+#define DK_PHASE_BEGIN() unsigned long long _ph_t = clock64()
+#define DK_PHASE(k)                                                    \
+  do {                                                                 \
+    __syncthreads();                                                   \
+    if (threadIdx.x == 0) {                                            \
+      const unsigned long long _u = clock64();                         \
+      atomicAdd(&g_phase[k], _u - _ph_t);                              \
+      _ph_t = _u;                                                      \
+    }                                                                  \
+  } while (0)
+#define DK_PHASE_ADD(k, v) do { if (threadIdx.x == 0) atomicAdd(&g_phase[k], (unsigned long long)(v)); } while (0)
+#define DK_WARP_ADD(k, v) do { if ((threadIdx.x & 31) == 0) atomicAdd(&g_phase[k], (unsigned long long)(v)); } while (0)
+#else
+#define DK_WARP_ADD(k, v) do {} while (0)
+#define DK_PHASE_BEGIN() do {} while (0)
+#define DK_PHASE(k) do {} while (0)
+#define DK_PHASE_ADD(k, v) do {} while (0)
+#endif
+
 
 // ------------------------------------------------------------- level 1
+// Text tiles of a CTA's line range, staged into shared memory by 1-D TMA bulk
+// copies (double-buffered: tile t+1 streams in while tile t is parsed).
+struct TextTiles {
+  const uint8_t* text;
+  uint64_t nbytes, stride, lo, hi;
+  uint32_t lt;  // lines per tile
+  uint8_t* buf[2];
+  uint64_t* bar;  // 2 mbarriers
+
+  __device__ uint32_t ntiles() const { return (uint32_t)((hi - lo + lt - 1) / lt); }
+  __device__ void range(uint32_t t, uint64_t* l0, uint64_t* l1) const {
+    *l0 = lo + (uint64_t)t * lt;
+    *l1 = min(hi, *l0 + lt);
+  }
+  __device__ StagedCopy plan(uint32_t t) const {
+    uint64_t l0, l1;
+    range(t, &l0, &l1);
+    const uint64_t b0 = l0 * stride, b1 = min(l1 * stride, nbytes);
+    return plan_stage(text + b0, b1 - b0, text + nbytes);
+  }
+  // one thread: start the copy of tile t into buffer t&1
+  __device__ void issue(uint32_t t) const {
+    uint64_t l0, l1;
+    range(t, &l0, &l1);
+    const StagedCopy c = plan(t);
+    uint64_t* b = &bar[t & 1];
+    fence_barrier_init();  // order earlier generic writes of the buffer before the async copy
+    mbar_arrive_expect_tx(b, c.bulk);
+    if (c.bulk) tma_load_1d(buf[t & 1], text + l0 * stride - c.lead, c.bulk, b);
+  }
+  // whole block: wait for tile t, fetch its unaligned tail, return its first
+  // line in shared memory (nullptr, with *err set, when the copy timed out)
+  __device__ const uint8_t* acquire(uint32_t t, unsigned long long* err) const {
+    const StagedCopy c = plan(t);
+    const bool ok = mbar_wait_bounded(&bar[t & 1], (t >> 1) & 1);
+    for (uint32_t i = threadIdx.x; i < c.tail_len; i += blockDim.x)
+      buf[t & 1][c.tail_dst + i] = c.tail_src[i];
+    if (__syncthreads_or(!ok)) {
+      if (threadIdx.x == 0) atomicMax(err, 1ull);
+      return nullptr;
+    }
+    return buf[t & 1] + c.lead;
+  }
+  // after a timeout: bounded wait for a copy still in flight into our smem
+  __device__ void drain(uint32_t t_next) const {
+    if (threadIdx.x == 0 && t_next < ntiles()) mbar_wait_bounded(&bar[t_next & 1], (t_next >> 1) & 1);
+    __syncthreads();
+  }
+};
+
+__host__ __device__ inline uint32_t tile_buf_bytes(uint32_t lt, uint64_t stride) {
+  return (uint32_t)(((uint64_t)lt * stride + 32 + 127) & ~127ull);
+}
+
+// counters[0] = k-mers, [1] = n_lines - (first NUL-led line), [3] = device error
 template <int C>
 __global__ void __launch_bounds__(512) k_l1_count(ExtractArgs a, uint32_t* __restrict__ H,
-                                                  unsigned long long* __restrict__ counters) {
-  extern __shared__ uint32_t sh[];
-  uint32_t* hist = sh;
-  uint8_t* lut = reinterpret_cast<uint8_t*>(sh + a.F1);
+                                                  unsigned long long* __restrict__ counters,
+                                                  uint32_t lt) {
+  extern __shared__ __align__(128) uint8_t smraw[];
+  const uint64_t stride = (uint64_t)a.W + 1;
+  const uint32_t bb = tile_buf_bytes(lt, stride);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smraw);
+  uint8_t* tb = smraw + 128;
+  uint32_t* hist = reinterpret_cast<uint32_t*>(tb + 2 * bb);
+  uint8_t* lut = reinterpret_cast<uint8_t*>(hist + a.F1);
+  TextTiles T;
+  T.text = a.text;
+  T.nbytes = a.nbytes;
+  T.stride = stride;
+  lines_of_block(a.n_lines, &T.lo, &T.hi);
+  T.lt = lt;
+  T.buf[0] = tb;
+  T.buf[1] = tb + bb;
+  T.bar = bar;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    fence_barrier_init();
+  }
   for (int b = threadIdx.x; b < a.F1; b += blockDim.x) hist[b] = 0;
   init_lut(lut);
   __syncthreads();
-  uint64_t lo, hi;
-  lines_of_block(a.n_lines, &lo, &hi);
   const uint32_t warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-  const uint64_t stride = (uint64_t)a.W + 1;
+  const uint32_t nt = T.ntiles();
   uint32_t mine = 0;
-  for (uint64_t l = lo + warp; l < hi; l += nwarps) {
-    const uint8_t* line = a.text + l * stride;
-    if (lane_id() == 0 && l > 0 && line[0] == 0) atomicMax(&counters[1], a.n_lines - l);
-    warp_line_kmers<C>(line, a.W, a.k, a.kmask, lut, [&](int, uint64_t key, bool valid) {
-      if (valid) { atomicAdd(&hist[key >> a.shift1], 1u); ++mine; }
-    });
+  if (threadIdx.x == 0 && nt) T.issue(0);
+  for (uint32_t t = 0; t < nt; ++t) {
+    if (threadIdx.x == 0 && t + 1 < nt) T.issue(t + 1);
+    const uint8_t* base = T.acquire(t, &counters[3]);
+    if (!base) {
+      T.drain(t + 1);
+      return;
+    }
+    uint64_t l0, l1;
+    T.range(t, &l0, &l1);
+    for (uint64_t l = l0 + warp; l < l1; l += nwarps) {
+      const uint8_t* line = base + (l - l0) * stride;
+      if (lane_id() == 0 && l > 0 && line[0] == 0) atomicMax(&counters[1], a.n_lines - l);
+      warp_line_kmers<C>(line, a.W, a.k, a.kmask, lut, [&](int, uint64_t key, bool valid) {
+        if (valid) { atomicAdd(&hist[key >> a.shift1], 1u); ++mine; }
+      });
+    }
+    __syncthreads();
   }
 #pragma unroll
   for (int o = 16; o; o >>= 1) mine += __shfl_xor_sync(0xFFFFFFFFu, mine, o);
@@ -110,36 +231,63 @@ __global__ void k_l1_offsets_rows(const uint32_t* __restrict__ H, int G, int F1,
 }
 
 template <int C, int LPW>
-__global__ void __launch_bounds__(512) k_l1_scatter(ExtractArgs a, const uint64_t* __restrict__ O,
+__global__ void __launch_bounds__(512, 2) k_l1_scatter(ExtractArgs a, const uint64_t* __restrict__ O,
                                                     uint64_t* __restrict__ keys_out,
-                                                    int stage_cap) {
-  extern __shared__ unsigned long long shs[];
+                                                    int stage_cap,
+                                                    unsigned long long* __restrict__ counters) {
+  extern __shared__ __align__(128) uint8_t smraw[];
   const int F1 = a.F1;
-  unsigned long long* cursor = shs;                                  // F1
-  unsigned long long* staging = cursor + F1;                         // stage_cap
+  const uint32_t nwarps = blockDim.x >> 5;
+  const uint32_t lt = nwarps * LPW;
+  const uint64_t stride = (uint64_t)a.W + 1;
+  const uint32_t bb = tile_buf_bytes(lt, stride);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smraw);
+  uint8_t* tb = smraw + 128;
+  unsigned long long* cursor = reinterpret_cast<unsigned long long*>(tb + 2 * bb);  // F1
+  unsigned long long* staging = cursor + F1;                              // stage_cap
   uint32_t* tile_hist = reinterpret_cast<uint32_t*>(staging + stage_cap);  // F1
-  uint32_t* tile_off = tile_hist + F1;                                // F1
-  uint32_t* tmp = tile_off + F1;                                      // 32
-  uint8_t* lut = reinterpret_cast<uint8_t*>(tmp + 32);                // 256
+  uint32_t* tile_off = tile_hist + F1;                                    // F1
+  uint32_t* tmp = tile_off + F1;                                          // 32
+  uint8_t* lut = reinterpret_cast<uint8_t*>(tmp + 32);                    // 256
+  TextTiles T;
+  T.text = a.text;
+  T.nbytes = a.nbytes;
+  T.stride = stride;
+  lines_of_block(a.n_lines, &T.lo, &T.hi);
+  T.lt = lt;
+  T.buf[0] = tb;
+  T.buf[1] = tb + bb;
+  T.bar = bar;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    fence_barrier_init();
+  }
   for (int b = threadIdx.x; b < F1; b += blockDim.x) {
     cursor[b] = O[(size_t)blockIdx.x * F1 + b];
     tile_hist[b] = 0;
   }
   init_lut(lut);
   __syncthreads();
-  uint64_t lo, hi;
-  lines_of_block(a.n_lines, &lo, &hi);
-  const uint32_t warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-  const uint64_t stride = (uint64_t)a.W + 1;
-  const uint64_t lines_per_tile = (uint64_t)nwarps * LPW;
-  for (uint64_t t0 = lo; t0 < hi; t0 += lines_per_tile) {
+  const uint32_t warp = threadIdx.x >> 5;
+  const uint32_t nt = T.ntiles();
+  if (threadIdx.x == 0 && nt) T.issue(0);
+  for (uint32_t ti = 0; ti < nt; ++ti) {
+    if (threadIdx.x == 0 && ti + 1 < nt) T.issue(ti + 1);
+    const uint8_t* base = T.acquire(ti, &counters[3]);
+    if (!base) {
+      T.drain(ti + 1);
+      return;
+    }
+    uint64_t t0, t1;
+    T.range(ti, &t0, &t1);
     uint64_t kr[LPW][C];
     uint32_t sr[LPW][C];
 #pragma unroll
     for (int j = 0; j < LPW; ++j) {
       const uint64_t l = t0 + (uint64_t)j * nwarps + warp;
-      if (l < hi) {
-        warp_line_kmers<C>(a.text + l * stride, a.W, a.k, a.kmask, lut,
+      if (l < t1) {
+        warp_line_kmers<C>(base + (l - t0) * stride, a.W, a.k, a.kmask, lut,
                            [&](int t, uint64_t key, bool valid) {
                              kr[j][t] = key;
                              sr[j][t] = valid ? atomicAdd(&tile_hist[key >> a.shift1], 1u)
@@ -153,14 +301,14 @@ __global__ void __launch_bounds__(512) k_l1_scatter(ExtractArgs a, const uint64_
     __syncthreads();
     for (int b = threadIdx.x; b < F1; b += blockDim.x) tile_off[b] = tile_hist[b];
     __syncthreads();
-    const uint32_t T = block_scan_array<uint32_t>(tile_off, F1, tmp);
+    const uint32_t Tn = block_scan_array<uint32_t>(tile_off, F1, tmp);
 #pragma unroll
     for (int j = 0; j < LPW; ++j)
 #pragma unroll
       for (int t = 0; t < C; ++t)
         if (sr[j][t] != 0xFFFFFFFFu) staging[tile_off[kr[j][t] >> a.shift1] + sr[j][t]] = kr[j][t];
     __syncthreads();
-    for (uint32_t i = threadIdx.x; i < T; i += blockDim.x) {
+    for (uint32_t i = threadIdx.x; i < Tn; i += blockDim.x) {
       const uint64_t key = staging[i];
       const uint32_t b = (uint32_t)(key >> a.shift1);
       keys_out[cursor[b] + (i - tile_off[b])] = key;
@@ -271,40 +419,120 @@ __global__ void __launch_bounds__(256) k_node_scan(Node* nodes, uint32_t lo, con
   nodes[nd.first_child + j] = ch;
 }
 
-__global__ void __launch_bounds__(256) k_tile_scatter(const Node* nodes, const Tile* tiles,
-                                                      uint64_t* A, uint64_t* B,
-                                                      const uint32_t* TH) {
-  __shared__ unsigned long long cursor[kFanout];
+// Partition one tile by the next 8 bits.  Pass 1 ranks every key within its
+// digit (shared atomics); the tile is then laid out digit by digit in shared
+// memory (keys re-read from L2) so each digit's keys leave as one contiguous,
+// coalesced run at the tile's offset inside the child.
+constexpr int kTileThreads = 512;
+constexpr int kTileKeysPerThread = kTileKeys / kTileThreads;
+
+__global__ void __launch_bounds__(kTileThreads, 3) k_tile_scatter(const Node* nodes,
+                                                                  const Tile* tiles, uint64_t* A,
+                                                                  uint64_t* B,
+                                                                  const uint32_t* TH) {
+  extern __shared__ __align__(16) unsigned long long stage[];  // kTileKeys
+  __shared__ unsigned long long gbase[kFanout];
+  __shared__ uint32_t cnt[kFanout], loc[kFanout];
+  __shared__ uint32_t tmp[32];
   const Tile tl = tiles[blockIdx.x];
   const Node nd = nodes[tl.node];
   const uint64_t* src = (nd.buf ? B : A) + tl.start;
   uint64_t* dst = nd.buf ? A : B;
-  cursor[threadIdx.x] = nodes[nd.first_child + threadIdx.x].start +
-                        TH[(size_t)blockIdx.x * kFanout + threadIdx.x];
+  for (uint32_t j = threadIdx.x; j < kFanout; j += blockDim.x) {
+    gbase[j] = nodes[nd.first_child + j].start + TH[(size_t)blockIdx.x * kFanout + j];
+    cnt[j] = 0;
+  }
+  __syncthreads();
+  uint16_t rank[kTileKeysPerThread];
+#pragma unroll
+  for (int u = 0; u < kTileKeysPerThread; ++u) {
+    const uint32_t i = threadIdx.x + u * kTileThreads;
+    if (i < tl.n) rank[u] = (uint16_t)atomicAdd(&cnt[digit_of(__ldg(src + i), nd.shift)], 1u);
+  }
+  __syncthreads();
+  for (uint32_t j = threadIdx.x; j < kFanout; j += blockDim.x) loc[j] = cnt[j];
+  __syncthreads();
+  block_scan_array<uint32_t>(loc, kFanout, tmp);
+#pragma unroll
+  for (int u = 0; u < kTileKeysPerThread; ++u) {
+    const uint32_t i = threadIdx.x + u * kTileThreads;
+    if (i < tl.n) {
+      const uint64_t key = __ldg(src + i);
+      stage[loc[digit_of(key, nd.shift)] + rank[u]] = key;
+    }
+  }
   __syncthreads();
   for (uint32_t i = threadIdx.x; i < tl.n; i += blockDim.x) {
-    const uint64_t key = src[i];
-    const unsigned long long pos = atomicAdd(&cursor[digit_of(key, nd.shift)], 1ull);
-    dst[pos] = key;
+    const uint64_t key = stage[i];
+    const uint32_t d = digit_of(key, nd.shift);
+    dst[gbase[d] + (i - loc[d])] = key;
   }
 }
 
 // ------------------------------------------------------------ bin count
 
+// Block-wide exclusive scan of (sum, max) pairs; returns both exclusive
+// values and the block totals.  `tmp` needs 64 u32 slots.
+__device__ __forceinline__ void block_scan_sum_max(uint32_t v, int m, uint32_t* tmp,
+                                                   uint32_t* ex_sum, int* ex_max,
+                                                   uint32_t* tot_sum) {
+  const uint32_t lane = lane_id(), warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  uint32_t xs = v;
+  int xm = m;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t ys = __shfl_up_sync(0xFFFFFFFFu, xs, o);
+    const int ym = __shfl_up_sync(0xFFFFFFFFu, xm, o);
+    if ((int)lane >= o) { xs += ys; xm = max(xm, ym); }
+  }
+  if (lane == 31) { tmp[warp] = xs; tmp[32 + warp] = (uint32_t)xm; }
+  __syncthreads();
+  if (warp == 0) {
+    uint32_t ws = lane < nw ? tmp[lane] : 0u;
+    int wm = lane < nw ? (int)tmp[32 + lane] : -1;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t ys = __shfl_up_sync(0xFFFFFFFFu, ws, o);
+      const int ym = __shfl_up_sync(0xFFFFFFFFu, wm, o);
+      if ((int)lane >= o) { ws += ys; wm = max(wm, ym); }
+    }
+    if (lane < nw) { tmp[lane] = ws; tmp[32 + lane] = (uint32_t)wm; }
+  }
+  __syncthreads();
+  const uint32_t bs = warp ? tmp[warp - 1] : 0u;
+  const int bm = warp ? (int)tmp[32 + warp - 1] : -1;
+  *ex_sum = bs + xs - v;
+  // exclusive max within the warp: inclusive max of the previous lane
+  int pm = __shfl_up_sync(0xFFFFFFFFu, xm, 1);
+  if (lane == 0) pm = -1;
+  *ex_max = max(bm, pm);
+  *tot_sum = tmp[nw - 1];
+  __syncthreads();
+}
+
 // Dense count of a node with shift <= 12 free bits: the histogram over the
-// free bits is already the sorted run-length table.
+// free bits is already the sorted run-length table.  hist64 holds 4096 u64.
 __device__ void bin_dense(Node* nodes, uint32_t ni, const Node& nd, uint64_t* keys, uint32_t* cnt,
-                          unsigned long long* hist, unsigned long long* tmp, int* overflow) {
+                          unsigned long long* hist, unsigned long long* tmp,
+                          unsigned long long* overflow) {
   const int s = nd.shift;
   const uint32_t R = 1u << s;
   const uint64_t mask = (uint64_t)R - 1;
   for (uint32_t j = threadIdx.x; j < R; j += blockDim.x) hist[j] = 0;
   __syncthreads();
   const uint64_t prefix = (keys[0] >> s) << s;
-  for (uint64_t i = threadIdx.x; i < nd.n; i += blockDim.x)
-    atomicAdd(&hist[__ldg(keys + i) & mask], 1ull);
+  const uint64_t T = blockDim.x;
+  uint64_t i = threadIdx.x;
+  for (; i + 3 * T < nd.n; i += 4 * T) {
+    const uint64_t k0 = __ldg(keys + i), k1 = __ldg(keys + i + T), k2 = __ldg(keys + i + 2 * T),
+                   k3 = __ldg(keys + i + 3 * T);
+    atomicAdd(&hist[k0 & mask], 1ull);
+    atomicAdd(&hist[k1 & mask], 1ull);
+    atomicAdd(&hist[k2 & mask], 1ull);
+    atomicAdd(&hist[k3 & mask], 1ull);
+  }
+  for (; i < nd.n; i += T) atomicAdd(&hist[__ldg(keys + i) & mask], 1ull);
   __syncthreads();
-  // rank nonzero digits
   const uint32_t per = (R + blockDim.x - 1) / blockDim.x;
   const uint32_t lo = min(R, threadIdx.x * per), hi = min(R, lo + per);
   unsigned long long c = 0;
@@ -315,7 +543,7 @@ __device__ void bin_dense(Node* nodes, uint32_t ni, const Node& nd, uint64_t* ke
     const unsigned long long h = hist[j];
     if (h) {
       keys[r] = prefix | j;
-      if (h > 0xFFFFFFFFull) *overflow = 1;
+      if (h > 0xFFFFFFFFull) atomicMax(overflow, 1ull);
       cnt[r] = (uint32_t)h;
       ++r;
     }
@@ -323,93 +551,488 @@ __device__ void bin_dense(Node* nodes, uint32_t ni, const Node& nd, uint64_t* ke
   if (threadIdx.x == 0) nodes[ni].d = total;
 }
 
-__global__ void __launch_bounds__(kBinThreads) k_bin_sort(Node* nodes,
-                                                          const uint32_t* __restrict__ finals,
-                                                          uint64_t* A, uint64_t* B, uint32_t* C,
-                                                          int* overflow) {
-  extern __shared__ unsigned long long skeys[];               // kBinCap
-  __shared__ unsigned long long hist64[1u << kDenseBits];     // 32 KB (u32 view for the sort path)
-  __shared__ unsigned long long tmp[32];
-  __shared__ uint16_t long_list[512];
-  __shared__ uint32_t n_long;
-  const uint32_t ni = finals[blockIdx.x];
-  const Node nd = nodes[ni];
-  uint64_t* keys = (nd.buf ? B : A) + nd.start;
-  uint32_t* cnt = C + nd.start;
-  if (nd.shift <= kDenseBits) {
-    bin_dense(nodes, ni, nd, keys, cnt, hist64, tmp, overflow);
-    return;
+// Sort s[0, m) in place with one warp when it holds at most 32*K distinct
+// keys: gather (key, count) pairs with __match_any_sync (entry e lives in
+// lane e%32, slot e/32), sort them with a bitonic network across lanes
+// (shuffles) and slots (registers), and rewrite the range.  Returns false,
+// leaving the range untouched, when there are more distinct keys.
+template <int K>
+__device__ bool warp_sort_few_distinct(unsigned long long* s, uint32_t m) {
+  const uint32_t lane = lane_id();
+  unsigned long long dk[K];
+  uint32_t dc[K];
+#pragma unroll
+  for (int u = 0; u < K; ++u) { dk[u] = 0; dc[u] = 0; }
+  uint32_t nd = 0;
+  for (uint32_t base = 0; base < m; base += 32) {
+    const uint32_t i = base + lane;
+    const bool valid = i < m;
+    const unsigned long long key = valid ? s[i] : 0ull;
+    const uint32_t active = __ballot_sync(0xFFFFFFFFu, valid);
+    uint32_t peers = 0;
+    if (valid) peers = __match_any_sync(active, key);
+    const bool leader = valid && (__ffs(peers) - 1 == (int)lane);
+    uint32_t leaders = __ballot_sync(0xFFFFFFFFu, leader);
+    while (leaders) {
+      const int l = __ffs(leaders) - 1;
+      leaders &= leaders - 1;
+      const unsigned long long kl = __shfl_sync(0xFFFFFFFFu, key, l);
+      const uint32_t cl = __shfl_sync(0xFFFFFFFFu, (uint32_t)__popc(peers), l);
+      bool found = false;
+#pragma unroll
+      for (int u = 0; u < K; ++u) {
+        const uint32_t hit = __ballot_sync(0xFFFFFFFFu, (u * 32 + lane) < nd && dk[u] == kl);
+        if (hit) {
+          if (!found && (int)lane == __ffs(hit) - 1) dc[u] += cl;
+          found = true;
+        }
+      }
+      if (!found) {
+        if (nd == 32u * K) return false;
+#pragma unroll
+        for (int u = 0; u < K; ++u)
+          if (nd == u * 32 + lane) { dk[u] = kl; dc[u] = cl; }
+        ++nd;
+      }
+    }
   }
-  // ---- shared-memory sort path (nd.n <= kBinCap)
+  // bitonic sort of the 32*K entries (index e = u*32 + lane; e >= nd is +inf)
+  bool inf[K];
+#pragma unroll
+  for (int u = 0; u < K; ++u) inf[u] = (u * 32 + lane) >= nd;
+#pragma unroll
+  for (int size = 2; size <= 32 * K; size <<= 1) {
+#pragma unroll
+    for (int st = size >> 1; st > 0; st >>= 1) {
+      if (st >= 32) {  // partner in another slot of the same lane
+        const int su = st >> 5;
+#pragma unroll
+        for (int u = 0; u < K; ++u) {
+          if (u & su) continue;
+          const int v = u | su;
+          const uint32_t e = u * 32 + lane;
+          const bool up = (e & size) == 0;
+          const bool v_less = !inf[v] && (inf[u] || dk[v] < dk[u]);
+          const bool u_less = !inf[u] && (inf[v] || dk[u] < dk[v]);
+          if (up ? v_less : u_less) {
+            const unsigned long long tk = dk[u]; dk[u] = dk[v]; dk[v] = tk;
+            const uint32_t tc = dc[u]; dc[u] = dc[v]; dc[v] = tc;
+            const bool ti = inf[u]; inf[u] = inf[v]; inf[v] = ti;
+          }
+        }
+      } else {  // partner in another lane, same slot
+#pragma unroll
+        for (int u = 0; u < K; ++u) {
+          const unsigned long long ok = __shfl_xor_sync(0xFFFFFFFFu, dk[u], st);
+          const uint32_t oc = __shfl_xor_sync(0xFFFFFFFFu, dc[u], st);
+          const bool oinf = __shfl_xor_sync(0xFFFFFFFFu, (int)inf[u], st) != 0;
+          const uint32_t e = u * 32 + lane;
+          const bool up = (e & size) == 0;
+          const bool lower = (lane & st) == 0;
+          const bool other_less = !oinf && (inf[u] || ok < dk[u]);
+          const bool other_greater = !inf[u] && (oinf || dk[u] < ok);
+          const bool take = (lower == up) ? other_less : other_greater;
+          if (take) { dk[u] = ok; dc[u] = oc; inf[u] = oinf; }
+        }
+      }
+    }
+  }
+  // offsets in entry order, then all lanes write each key's run
+  uint32_t off[K];
+  uint32_t run = 0;
+#pragma unroll
+  for (int u = 0; u < K; ++u) {
+    uint32_t x = inf[u] ? 0u : dc[u];
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+      if ((int)lane >= o) x += y;
+    }
+    off[u] = run + x - (inf[u] ? 0u : dc[u]);
+    run += __shfl_sync(0xFFFFFFFFu, x, 31);
+  }
+  __syncwarp();
+#pragma unroll
+  for (int u = 0; u < K; ++u) {
+    const uint32_t lim = nd > (uint32_t)(u * 32) ? min(32u, nd - u * 32) : 0u;
+    for (uint32_t q = 0; q < lim; ++q) {
+      const unsigned long long kq = __shfl_sync(0xFFFFFFFFu, dk[u], q);
+      const uint32_t oq = __shfl_sync(0xFFFFFFFFu, off[u], q), cq = __shfl_sync(0xFFFFFFFFu, dc[u], q);
+      for (uint32_t t = lane; t < cq; t += 32)
+        if (DK_OK_IDX(oq + t < m, 21, ((uint64_t)(oq + t) << 32) | m)) s[oq + t] = kq;
+    }
+  }
+  __syncwarp();
+  return true;
+}
+
+// one-warp sort of m <= 32 keys in place: each lane ranks its key against all
+// others (stable for equal keys) and writes it to its final slot
+__device__ void warp_rank_sort(unsigned long long* s, uint32_t m) {
+  const uint32_t lane = lane_id();
+  const unsigned long long v = lane < m ? s[lane] : 0ull;
+  uint32_t rank = 0;
+  for (uint32_t j = 0; j < m; ++j) {
+    const unsigned long long o = __shfl_sync(0xFFFFFFFFu, v, j);
+    rank += (o < v) || (o == v && j < lane);
+  }
+  __syncwarp();
+  if (lane < m && DK_OK_IDX(rank < m, 22, ((uint64_t)rank << 32) | m)) s[rank] = v;
+  __syncwarp();
+}
+
+// one-warp bitonic sort of s[0, m) in shared memory (out-of-range partners
+// act as +inf and never move)
+__device__ void warp_bitonic(unsigned long long* s, uint32_t m) {
+  int lg = 0;
+  while ((1u << lg) < m) ++lg;
+  const uint32_t P = 1u << lg;
+  for (int sz = 1; sz <= lg; ++sz) {  // merge blocks of 2^sz
+    const uint32_t hmask = (1u << (sz - 1)) - 1;
+    for (uint32_t i = lane_id(); i < P / 2; i += 32) {
+      const uint32_t a = ((i >> (sz - 1)) << sz) | (i & hmask);
+      const uint32_t b = a ^ ((1u << sz) - 1);
+      if (b < m) {
+        const unsigned long long x = s[a], y = s[b];
+        if (y < x) { s[a] = y; s[b] = x; }
+      }
+    }
+    __syncwarp();
+    for (int st = sz - 2; st >= 0; --st) {
+      const uint32_t smask = (1u << st) - 1;
+      for (uint32_t i = lane_id(); i < P / 2; i += 32) {
+        const uint32_t a = ((i >> st) << (st + 1)) | (i & smask);
+        const uint32_t b = a + (1u << st);
+        if (b < m) {
+          const unsigned long long x = s[a], y = s[b];
+          if (y < x) { s[a] = y; s[b] = x; }
+        }
+      }
+      __syncwarp();
+    }
+  }
+}
+
+constexpr uint32_t kDeferMax = 64;  // ranges per bin left to the block-wide sort
+
+// Shared-memory sort + run-length reduce of one bin (n <= kBinCap keys,
+// more than kDenseBits free bits).  Counting sort on the top D free bits,
+// then each digit range is finished by insertion sort (<= 32 keys) or a
+// block bitonic sort; the run-length pass finds head/tail positions with one
+// block scan and writes (key, count) over the bin's own key range.
+__device__ void bin_sorted(Node* nodes, uint32_t ni, const Node& nd, uint64_t* keys, uint32_t* cnt,
+                           unsigned long long* skeys, uint32_t* hist, uint32_t* tmp,
+                           uint32_t* mark, uint16_t* defer, uint32_t* n_defer) {
   const uint32_t n = (uint32_t)nd.n;
+  DK_PHASE_BEGIN();
   int D = ceil_log2_u64(n);
   D = max(4, min(D, kDenseBits));
   D = min(D, (int)nd.shift);
   const int sh = nd.shift - D;
-  const uint32_t R = 1u << D;
-  uint32_t* hist = reinterpret_cast<uint32_t*>(hist64);
-  for (uint32_t j = threadIdx.x; j < R; j += blockDim.x) hist[j] = 0;
-  if (threadIdx.x == 0) n_long = 0;
+  const uint32_t R = 1u << D, M = R - 1;
+  const uint32_t T = blockDim.x;
+  for (uint32_t j = threadIdx.x; j < R; j += T) hist[j] = 0;
   __syncthreads();
-  for (uint32_t i = threadIdx.x; i < n; i += blockDim.x)
-    atomicAdd(&hist[(uint32_t)(__ldg(keys + i) >> sh) & (R - 1)], 1u);
-  __syncthreads();
-  block_scan_array<uint32_t>(hist, (int)R, reinterpret_cast<uint32_t*>(tmp));
-  for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
-    const uint64_t key = keys[i];
-    const uint32_t pos = atomicAdd(&hist[(uint32_t)(key >> sh) & (R - 1)], 1u);
-    skeys[pos] = key;
+  DK_PHASE(0);
+  uint32_t i = threadIdx.x;
+  for (; i + 3 * T < n; i += 4 * T) {
+    const uint64_t k0 = __ldg(keys + i), k1 = __ldg(keys + i + T), k2 = __ldg(keys + i + 2 * T),
+                   k3 = __ldg(keys + i + 3 * T);
+    atomicAdd(&hist[(uint32_t)(k0 >> sh) & M], 1u);
+    atomicAdd(&hist[(uint32_t)(k1 >> sh) & M], 1u);
+    atomicAdd(&hist[(uint32_t)(k2 >> sh) & M], 1u);
+    atomicAdd(&hist[(uint32_t)(k3 >> sh) & M], 1u);
   }
+  for (; i < n; i += T) atomicAdd(&hist[(uint32_t)(__ldg(keys + i) >> sh) & M], 1u);
   __syncthreads();
-  // hist[j] is now the end of digit range j
-  for (uint32_t j = threadIdx.x; j < R; j += blockDim.x) {
-    const uint32_t lo = j ? hist[j - 1] : 0, hi = hist[j];
-    const uint32_t len = hi - lo;
-    if (len <= 1) continue;
-    if (len <= 32) {
-      for (uint32_t x = lo + 1; x < hi; ++x) {
-        const unsigned long long v = skeys[x];
-        uint32_t y = x;
-        while (y > lo && skeys[y - 1] > v) { skeys[y] = skeys[y - 1]; --y; }
-        skeys[y] = v;
-      }
-    } else {
-      long_list[atomicAdd(&n_long, 1u)] = (uint16_t)j;
+  DK_PHASE(1);
+  block_scan_array<uint32_t>(hist, (int)R, tmp);
+  DK_PHASE(2);
+  i = threadIdx.x;
+  for (; i + 3 * T < n; i += 4 * T) {
+    const uint64_t k0 = __ldg(keys + i), k1 = __ldg(keys + i + T), k2 = __ldg(keys + i + 2 * T),
+                   k3 = __ldg(keys + i + 3 * T);
+    uint32_t p0 = atomicAdd(&hist[(uint32_t)(k0 >> sh) & M], 1u);
+    uint32_t p1 = atomicAdd(&hist[(uint32_t)(k1 >> sh) & M], 1u);
+    uint32_t p2 = atomicAdd(&hist[(uint32_t)(k2 >> sh) & M], 1u);
+    uint32_t p3 = atomicAdd(&hist[(uint32_t)(k3 >> sh) & M], 1u);
+    if (DK_OK_IDX(p0 < n && p1 < n && p2 < n && p3 < n, 11, n)) {
+      skeys[p0] = k0; skeys[p1] = k1; skeys[p2] = k2; skeys[p3] = k3;
     }
   }
-  __syncthreads();
-  const uint32_t nl = n_long;
-  for (uint32_t q = 0; q < nl; ++q) {
-    const uint32_t j = long_list[q];
-    const uint32_t lo = j ? hist[j - 1] : 0, hi = hist[j];
-    block_bitonic(skeys + lo, hi - lo);
+  for (; i < n; i += T) {
+    const uint64_t k0 = __ldg(keys + i);
+    const uint32_t p0 = atomicAdd(&hist[(uint32_t)(k0 >> sh) & M], 1u);
+    if (DK_OK_IDX(p0 < n, 12, n)) skeys[p0] = k0;
   }
   __syncthreads();
-  // run-length reduce: heads write key + head position, tails turn it into a count
-  const uint32_t per = (n + blockDim.x - 1) / blockDim.x;
+  DK_PHASE(3);
+  // hist[j] is now the end of digit range j.  Within a range the keys are in
+  // arbitrary order; mark the ranges that hold a descent (a key smaller than
+  // its predecessor in the same range) and sort only those, one warp each.
+  // A range made of one repeated k-mer has no descent and costs nothing.
+  if (sh > 0) {
+    for (uint32_t w = threadIdx.x; w < (R + 31) / 32; w += T) mark[w] = 0;
+    if (threadIdx.x == 0) *n_defer = 0;
+    __syncthreads();
+    const uint32_t per_e = (n + T - 1) / T;
+    const uint32_t e0 = min(n, threadIdx.x * per_e), e1 = min(n, e0 + per_e);
+    unsigned long long prev = e0 ? skeys[e0 - 1] : 0ull;
+    for (uint32_t x = e0; x < e1; ++x) {
+      const unsigned long long v = skeys[x];
+      if (x > 0 && (v >> sh) == (prev >> sh) && v < prev) {
+        const uint32_t d = (uint32_t)(v >> sh) & M;
+        atomicOr(&mark[d >> 5], 1u << (d & 31));
+      }
+      prev = v;
+    }
+    __syncthreads();
+    DK_PHASE(4);
+    const uint32_t warp = threadIdx.x >> 5, nwarps = T >> 5;
+    for (uint32_t w = warp; w < (R + 31) / 32; w += nwarps) {
+      uint32_t bits = mark[w];
+      while (bits) {
+        const uint32_t j = w * 32 + (__ffs(bits) - 1);
+        bits &= bits - 1;
+        const uint32_t lo = j ? hist[j - 1] : 0, hi = hist[j];
+        const uint32_t m = hi - lo;
+        if (!DK_OK_IDX(lo <= hi && hi <= n && j < R, 13, ((uint64_t)lo << 32) | hi)) continue;
+        if (m <= 32) {
+          warp_rank_sort(skeys + lo, m);
+          DK_WARP_ADD(11, 1);
+        } else if (!warp_sort_few_distinct<1>(skeys + lo, m)) {
+          // many distinct keys: sorted below by the whole block
+          uint32_t q = 0;
+          if (lane_id() == 0) q = atomicAdd(n_defer, 1u);
+          q = __shfl_sync(0xFFFFFFFFu, q, 0);
+          if (q < kDeferMax) {
+            if (lane_id() == 0) defer[q] = (uint16_t)j;
+          } else {
+            warp_bitonic(skeys + lo, m);
+          }
+          DK_WARP_ADD(13, 1);
+          DK_WARP_ADD(14, m);
+        } else {
+          DK_WARP_ADD(12, 1);
+          DK_WARP_ADD(15, m);
+        }
+      }
+    }
+    __syncthreads();
+    const uint32_t nd_ = min(*n_defer, (uint32_t)kDeferMax);
+    for (uint32_t q = 0; q < nd_; ++q) {
+      const uint32_t j = defer[q];
+      const uint32_t lo = j ? hist[j - 1] : 0, hi = hist[j];
+      block_bitonic(skeys + lo, hi - lo);
+    }
+    __syncthreads();
+    DK_PHASE(5);
+  }
+  // run-length reduce
+  const uint32_t per = (n + T - 1) / T;
   const uint32_t lo = min(n, threadIdx.x * per), hi = min(n, lo + per);
   uint32_t heads = 0;
-  for (uint32_t i = lo; i < hi; ++i) heads += (i == 0 || skeys[i] != skeys[i - 1]);
-  uint32_t total;
-  const uint32_t r0 = block_excl_scan<uint32_t>(heads, reinterpret_cast<uint32_t*>(tmp), &total);
-  uint32_t r = r0;
-  for (uint32_t i = lo; i < hi; ++i) {
-    if (i == 0 || skeys[i] != skeys[i - 1]) {
-      keys[r] = skeys[i];
-      __stcg(cnt + r, i);
+  int last_head = -1;
+  for (uint32_t x = lo; x < hi; ++x)
+    if (x == 0 || skeys[x] != skeys[x - 1]) { ++heads; last_head = (int)x; }
+  uint32_t r0, total;
+  int cur;
+  DK_PHASE(6);
+  block_scan_sum_max(heads, last_head, tmp, &r0, &cur, &total);
+  DK_PHASE(7);
+  int r = (int)r0 - 1;  // rank of the run that contains lo (when lo is not a head)
+  for (uint32_t x = lo; x < hi; ++x) {
+    const unsigned long long v = skeys[x];
+    if (x == 0 || v != skeys[x - 1]) {
       ++r;
+      cur = (int)x;
+      if (DK_OK_IDX(r >= 0 && (uint32_t)r < n, 14, r)) keys[r] = v;
+    }
+    if (x == n - 1 || skeys[x + 1] != v)
+      if (DK_OK_IDX(r >= 0 && (uint32_t)r < n && cur >= 0 && (uint32_t)cur <= x, 15, ((uint64_t)(uint32_t)r << 32) | (uint32_t)cur))
+        cnt[r] = x - (uint32_t)cur + 1;
+  }
+  DK_PHASE(8);
+  DK_PHASE_ADD(9, 1);
+  DK_PHASE_ADD(10, n);
+  if (threadIdx.x == 0) nodes[ni].d = total;
+}
+
+// ---- hash variant: aggregate the bin in a shared-memory hash table first
+constexpr uint32_t kHashSlots = 4096;                 // table slots per bin
+constexpr uint32_t kHashMaxDistinct = 3072;           // 75% load; more falls back to sorting
+constexpr unsigned long long kEmptyKey = ~0ull;       // never a k-mer when k <= 31
+
+// (key, count) pair versions of the small in-place sorts
+__device__ void warp_rank_sort_pairs(unsigned long long* s, uint32_t* c, uint32_t m) {
+  const uint32_t lane = lane_id();
+  const unsigned long long v = lane < m ? s[lane] : 0ull;
+  const uint32_t vc = lane < m ? c[lane] : 0u;
+  uint32_t rank = 0;
+  for (uint32_t j = 0; j < m; ++j) {
+    const unsigned long long o = __shfl_sync(0xFFFFFFFFu, v, j);
+    rank += (o < v) || (o == v && j < lane);
+  }
+  __syncwarp();
+  if (lane < m) { s[rank] = v; c[rank] = vc; }
+  __syncwarp();
+}
+
+__device__ void warp_bitonic_pairs(unsigned long long* s, uint32_t* c, uint32_t m) {
+  int lg = 0;
+  while ((1u << lg) < m) ++lg;
+  const uint32_t P = 1u << lg;
+  for (int sz = 1; sz <= lg; ++sz) {
+    const uint32_t hmask = (1u << (sz - 1)) - 1;
+    for (uint32_t i = lane_id(); i < P / 2; i += 32) {
+      const uint32_t a = ((i >> (sz - 1)) << sz) | (i & hmask);
+      const uint32_t b = a ^ ((1u << sz) - 1);
+      if (b < m && s[b] < s[a]) {
+        const unsigned long long x = s[a]; s[a] = s[b]; s[b] = x;
+        const uint32_t y = c[a]; c[a] = c[b]; c[b] = y;
+      }
+    }
+    __syncwarp();
+    for (int st = sz - 2; st >= 0; --st) {
+      const uint32_t smask = (1u << st) - 1;
+      for (uint32_t i = lane_id(); i < P / 2; i += 32) {
+        const uint32_t a = ((i >> st) << (st + 1)) | (i & smask);
+        const uint32_t b = a + (1u << st);
+        if (b < m && s[b] < s[a]) {
+          const unsigned long long x = s[a]; s[a] = s[b]; s[b] = x;
+          const uint32_t y = c[a]; c[a] = c[b]; c[b] = y;
+        }
+      }
+      __syncwarp();
+    }
+  }
+}
+
+// Aggregate the bin's keys in a shared-memory open-addressing table (linear
+// probing, 64-bit atomicCAS on the key, atomicAdd on its count), then
+// counting-sort the distinct (key, count) pairs on their top free bits and
+// finish the few out-of-order digit ranges.  Returns false (nothing written)
+// when the bin holds more than kHashMaxDistinct distinct keys.
+__device__ bool bin_hashed(Node* nodes, uint32_t ni, const Node& nd, uint64_t* keys, uint32_t* cnt,
+                           unsigned long long* region, uint32_t* hist, uint32_t* tmp,
+                           uint32_t* mark, uint32_t* flags) {
+  unsigned long long* tk = region;                                  // kHashSlots keys
+  uint32_t* tc = reinterpret_cast<uint32_t*>(tk + kHashSlots);       // kHashSlots counts
+  unsigned long long* sk = reinterpret_cast<unsigned long long*>(tc + kHashSlots);  // sorted keys
+  uint32_t* sc = reinterpret_cast<uint32_t*>(sk + kHashMaxDistinct);                // sorted counts
+  const uint32_t n = (uint32_t)nd.n;
+  const uint32_t T = blockDim.x;
+  for (uint32_t j = threadIdx.x; j < kHashSlots; j += T) { tk[j] = kEmptyKey; tc[j] = 0; }
+  if (threadIdx.x == 0) { flags[0] = 0; flags[1] = 0; }
+  __syncthreads();
+  for (uint32_t i = threadIdx.x; i < n; i += T) {
+    const unsigned long long key = __ldg(keys + i);
+    uint32_t slot = (uint32_t)((key * 0x9E3779B97F4A7C15ull) >> 52);  // 12 bits = kHashSlots
+    for (uint32_t probe = 0; probe < kHashSlots; ++probe) {
+      const unsigned long long prev = atomicCAS(&tk[slot], kEmptyKey, key);
+      if (prev == kEmptyKey || prev == key) {
+        atomicAdd(&tc[slot], 1u);
+        if (prev == kEmptyKey && atomicAdd(&flags[0], 1u) + 1 > kHashMaxDistinct) flags[1] = 1;
+        break;
+      }
+      slot = (slot + 1) & (kHashSlots - 1);
     }
   }
   __syncthreads();
-  r = r0;
-  for (uint32_t i = lo; i < hi; ++i) {
-    if (i == 0 || skeys[i] != skeys[i - 1]) ++r;
-    if (i == n - 1 || skeys[i] != skeys[i + 1]) {
-      const uint32_t head = __ldcg(cnt + (r - 1));
-      __stcg(cnt + (r - 1), i - head + 1);
+  if (flags[1]) return false;
+  const uint32_t d = flags[0];
+  // counting sort of the distinct pairs on the top D free bits
+  int D = ceil_log2_u64(d);
+  D = max(4, min(D, kDenseBits));
+  D = min(D, (int)nd.shift);
+  const int sh = nd.shift - D;
+  const uint32_t R = 1u << D, M = R - 1;
+  for (uint32_t j = threadIdx.x; j < R; j += T) hist[j] = 0;
+  __syncthreads();
+  for (uint32_t j = threadIdx.x; j < kHashSlots; j += T)
+    if (tk[j] != kEmptyKey) atomicAdd(&hist[(uint32_t)(tk[j] >> sh) & M], 1u);
+  __syncthreads();
+  block_scan_array<uint32_t>(hist, (int)R, tmp);
+  for (uint32_t j = threadIdx.x; j < kHashSlots; j += T) {
+    const unsigned long long key = tk[j];
+    if (key != kEmptyKey) {
+      const uint32_t pos = atomicAdd(&hist[(uint32_t)(key >> sh) & M], 1u);
+      if (DK_OK_IDX(pos < d, 31, pos)) { sk[pos] = key; sc[pos] = tc[j]; }
     }
   }
-  if (threadIdx.x == 0) nodes[ni].d = total;
+  __syncthreads();
+  // ranges with a descent hold several distinct keys out of order
+  if (sh > 0) {
+    for (uint32_t w = threadIdx.x; w < (R + 31) / 32; w += T) mark[w] = 0;
+    __syncthreads();
+    for (uint32_t x = threadIdx.x + 1; x < d; x += T) {
+      const unsigned long long v = sk[x], p = sk[x - 1];
+      if ((v >> sh) == (p >> sh) && v < p) {
+        const uint32_t dg = (uint32_t)(v >> sh) & M;
+        atomicOr(&mark[dg >> 5], 1u << (dg & 31));
+      }
+    }
+    __syncthreads();
+    const uint32_t warp = threadIdx.x >> 5, nwarps = T >> 5;
+    for (uint32_t w = warp; w < (R + 31) / 32; w += nwarps) {
+      uint32_t bits = mark[w];
+      while (bits) {
+        const uint32_t j = w * 32 + (__ffs(bits) - 1);
+        bits &= bits - 1;
+        const uint32_t lo = j ? hist[j - 1] : 0, hi = hist[j];
+        if (!DK_OK_IDX(lo <= hi && hi <= d, 32, ((uint64_t)lo << 32) | hi)) continue;
+        if (hi - lo <= 32) warp_rank_sort_pairs(sk + lo, sc + lo, hi - lo);
+        else warp_bitonic_pairs(sk + lo, sc + lo, hi - lo);
+      }
+    }
+    __syncthreads();
+  }
+  for (uint32_t x = threadIdx.x; x < d; x += T) {
+    keys[x] = sk[x];
+    cnt[x] = sc[x];
+  }
+  if (threadIdx.x == 0) nodes[ni].d = d;
+  return true;
+}
+
+// Persistent bin counter: CTAs take final nodes from a ticket until none are
+// left.  Two CTAs fit per SM (96 KB keys + 16 KB histogram each).
+__global__ void __launch_bounds__(kBinThreads, 2) k_bin_count(Node* nodes,
+                                                              const uint32_t* __restrict__ finals,
+                                                              uint32_t n_final, uint64_t* A,
+                                                              uint64_t* B, uint32_t* C,
+                                                              unsigned long long* ctr,
+                                                              int use_hash) {
+  extern __shared__ __align__(16) unsigned long long skeys[];  // kBinCap keys / 4096 u64 counts
+  __shared__ uint32_t hist[1u << kDenseBits];
+  __shared__ uint32_t tmp[64];
+  __shared__ uint32_t mark[(1u << kDenseBits) / 32];
+  __shared__ uint16_t defer[kDeferMax];
+  __shared__ uint32_t s_bin, n_defer;
+  __shared__ uint32_t hflags[2];
+  for (;;) {
+    if (threadIdx.x == 0) s_bin = atomicAdd(reinterpret_cast<unsigned int*>(&ctr[4]), 1u);
+    __syncthreads();
+    const uint32_t b = s_bin;
+    if (b >= n_final) break;
+    const uint32_t ni = finals[b];
+    const Node nd = nodes[ni];
+    uint64_t* keys = (nd.buf ? B : A) + nd.start;
+    uint32_t* cnt = C + nd.start;
+    if (nd.shift <= kDenseBits) {
+      bin_dense(nodes, ni, nd, keys, cnt, skeys, reinterpret_cast<unsigned long long*>(tmp),
+                &ctr[5]);
+    } else {
+      bool done = false;
+      if (use_hash) {
+        done = bin_hashed(nodes, ni, nd, keys, cnt, skeys, hist, tmp, mark, hflags);
+        if (!done && threadIdx.x == 0) atomicAdd(&ctr[6], 1ull);  // bins that fell back
+        __syncthreads();
+      }
+      if (!done) bin_sorted(nodes, ni, nd, keys, cnt, skeys, hist, tmp, mark, defer, &n_defer);
+    }
+    __syncthreads();
+  }
 }
 
 // ----------------------------------------------------- tree reductions
@@ -476,17 +1099,26 @@ static int choose_c(int W) {
   return 32;
 }
 
+template <int C>
+static void count_launch(const ExtractArgs& a, int grid, uint32_t* H, unsigned long long* counters,
+                         cudaStream_t s) {
+  const uint64_t stride = (uint64_t)a.W + 1;
+  const uint32_t lt = (uint32_t)std::max<uint64_t>(16, std::min<uint64_t>(128, 16384 / stride));
+  const size_t smem = 128 + 2 * (size_t)tile_buf_bytes(lt, stride) + (size_t)a.F1 * 4 + 256;
+  cudaFuncSetAttribute(k_l1_count<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  k_l1_count<C><<<grid, 512, smem, s>>>(a, H, counters, lt);
+}
+
 int launch_l1_count(const ExtractArgs& a, int grid, uint32_t* H, unsigned long long* counters,
                     cudaStream_t s) {
-  const size_t smem = (size_t)a.F1 * 4 + 256;
   switch (choose_c(a.W)) {
-    case 1: k_l1_count<1><<<grid, 512, smem, s>>>(a, H, counters); break;
-    case 2: k_l1_count<2><<<grid, 512, smem, s>>>(a, H, counters); break;
-    case 4: k_l1_count<4><<<grid, 512, smem, s>>>(a, H, counters); break;
-    case 5: k_l1_count<5><<<grid, 512, smem, s>>>(a, H, counters); break;
-    case 8: k_l1_count<8><<<grid, 512, smem, s>>>(a, H, counters); break;
-    case 16: k_l1_count<16><<<grid, 512, smem, s>>>(a, H, counters); break;
-    default: k_l1_count<32><<<grid, 512, smem, s>>>(a, H, counters); break;
+    case 1: count_launch<1>(a, grid, H, counters, s); break;
+    case 2: count_launch<2>(a, grid, H, counters, s); break;
+    case 4: count_launch<4>(a, grid, H, counters, s); break;
+    case 5: count_launch<5>(a, grid, H, counters, s); break;
+    case 8: count_launch<8>(a, grid, H, counters, s); break;
+    case 16: count_launch<16>(a, grid, H, counters, s); break;
+    default: count_launch<32>(a, grid, H, counters, s); break;
   }
   return 1;
 }
@@ -502,29 +1134,26 @@ int launch_l1_scan(const uint32_t* H, int grid, int F1, uint64_t* O, Node* nodes
 
 template <int C, int LPW>
 static void scatter_launch(const ExtractArgs& a, int grid, const uint64_t* O, uint64_t* keys,
-                           cudaStream_t s) {
+                           unsigned long long* counters, cudaStream_t s) {
   const int threads = 512;
-  const int stage_cap = (threads / 32) * LPW * 32 * C;  // >= k-mers of one tile
-  const size_t smem = (size_t)a.F1 * 8 + (size_t)stage_cap * 8 + (size_t)a.F1 * 8 + 32 * 4 + 256;
-  static bool attr_set = false;
-  if (!attr_set) {
-    cudaFuncSetAttribute(k_l1_scatter<C, LPW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         232448);
-    attr_set = true;
-  }
-  k_l1_scatter<C, LPW><<<grid, threads, smem, s>>>(a, O, keys, stage_cap);
+  const uint32_t lt = (threads / 32) * LPW;
+  const int stage_cap = (int)lt * 32 * C;  // >= k-mers of one tile
+  const size_t smem = 128 + 2 * (size_t)tile_buf_bytes(lt, (uint64_t)a.W + 1) +
+                      (size_t)a.F1 * 8 + (size_t)stage_cap * 8 + (size_t)a.F1 * 8 + 32 * 4 + 256;
+  cudaFuncSetAttribute(k_l1_scatter<C, LPW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  k_l1_scatter<C, LPW><<<grid, threads, smem, s>>>(a, O, keys, stage_cap, counters);
 }
 
 int launch_l1_scatter(const ExtractArgs& a, int grid, const uint64_t* O, uint64_t* keys,
-                      cudaStream_t s) {
+                      unsigned long long* counters, cudaStream_t s) {
   switch (choose_c(a.W)) {
-    case 1: scatter_launch<1, 4>(a, grid, O, keys, s); break;
-    case 2: scatter_launch<2, 4>(a, grid, O, keys, s); break;
-    case 4: scatter_launch<4, 2>(a, grid, O, keys, s); break;
-    case 5: scatter_launch<5, 2>(a, grid, O, keys, s); break;
-    case 8: scatter_launch<8, 2>(a, grid, O, keys, s); break;
-    case 16: scatter_launch<16, 1>(a, grid, O, keys, s); break;
-    default: scatter_launch<32, 1>(a, grid, O, keys, s); break;
+    case 1: scatter_launch<1, 4>(a, grid, O, keys, counters, s); break;
+    case 2: scatter_launch<2, 4>(a, grid, O, keys, counters, s); break;
+    case 4: scatter_launch<4, 2>(a, grid, O, keys, counters, s); break;
+    case 5: scatter_launch<5, 2>(a, grid, O, keys, counters, s); break;
+    case 8: scatter_launch<8, 2>(a, grid, O, keys, counters, s); break;
+    case 16: scatter_launch<16, 1>(a, grid, O, keys, counters, s); break;
+    default: scatter_launch<32, 1>(a, grid, O, keys, counters, s); break;
   }
   return 1;
 }
@@ -562,21 +1191,21 @@ int launch_node_scan(Node* nodes, uint32_t lo, uint32_t hi, const Tile* tiles, u
 int launch_tile_scatter(const Node* nodes, const Tile* tiles, uint32_t n_tiles, uint64_t* A,
                         uint64_t* B, const uint32_t* TH, cudaStream_t s) {
   if (!n_tiles) return 0;
-  k_tile_scatter<<<n_tiles, 256, 0, s>>>(nodes, tiles, A, B, TH);
+  cudaFuncSetAttribute(k_tile_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize, kTileKeys * 8);
+  k_tile_scatter<<<n_tiles, kTileThreads, kTileKeys * 8, s>>>(nodes, tiles, A, B, TH);
   return 1;
 }
 
 int bin_count_smem_bytes(int) { return kBinCap * 8; }
 
 int launch_bin_count(Node* nodes, const uint32_t* final_list, uint32_t n_final, uint64_t* A,
-                     uint64_t* B, uint32_t* C, int, int* overflow, cudaStream_t s) {
+                     uint64_t* B, uint32_t* C, int use_hash, unsigned long long* ctr, int sm_count,
+                     cudaStream_t s) {
   if (!n_final) return 0;
-  static bool attr_set = false;
-  if (!attr_set) {
-    cudaFuncSetAttribute(k_bin_sort, cudaFuncAttributeMaxDynamicSharedMemorySize, kBinCap * 8);
-    attr_set = true;
-  }
-  k_bin_sort<<<n_final, kBinThreads, kBinCap * 8, s>>>(nodes, final_list, A, B, C, overflow);
+  cudaFuncSetAttribute(k_bin_count, cudaFuncAttributeMaxDynamicSharedMemorySize, kBinCap * 8);
+  const uint32_t grid = std::min<uint32_t>(n_final, 2u * (uint32_t)sm_count);
+  k_bin_count<<<grid, kBinThreads, kBinCap * 8, s>>>(nodes, final_list, n_final, A, B, C, ctr,
+                                                     use_hash);
   return 1;
 }
 
@@ -608,3 +1237,19 @@ int launch_compact(const Node* nodes, const uint32_t* final_list, uint32_t n_fin
 }
 
 }  // namespace dk
+
+#ifdef DK_PHASE_TIMING
+extern "C" int dk_debug_phases(unsigned long long* out) {
+  return (int)cudaMemcpyFromSymbol(out, dk::g_phase, sizeof(unsigned long long) * 16);
+}
+extern "C" int dk_debug_reset() {
+  unsigned long long z[16] = {0};
+  return (int)cudaMemcpyToSymbol(dk::g_phase, z, sizeof(z));
+}
+#endif
+
+#ifdef DK_BOUNDS_CHECK
+extern "C" int dk_debug_check(unsigned long long* out) {
+  return (int)cudaMemcpyFromSymbol(out, dk::g_check, sizeof(unsigned long long) * 4);
+}
+#endif

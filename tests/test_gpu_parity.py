@@ -17,7 +17,7 @@ from oracle import pyoracle
 
 pytestmark = pytest.mark.gpu
 
-VARIANTS = [dk.VARIANT_SORT]
+VARIANTS = [dk.VARIANT_SORT, dk.VARIANT_HASH]
 
 
 def check(engine, text, W, k, variant=dk.VARIANT_SORT):
