@@ -44,7 +44,8 @@ CONV_DAKC = 0
 ABI_SYMBOLS = [
     "dk_create", "dk_destroy", "dk_strerror", "dk_last_error_string", "dk_abi_version",
     "dk_count", "dk_count_device", "dk_table_free", "dk_last_stats", "dk_num_lines",
-    "dk_host_alloc", "dk_host_free", "dk_count_small_noalloc",
+    "dk_host_alloc", "dk_host_free", "dk_count_small_noalloc", "dk_count_batch",
+    "dk_serve_start", "dk_submit", "dk_poll", "dk_wait", "dk_cancel", "dk_serve_stop",
 ]
 
 
@@ -73,6 +74,15 @@ class Table(ctypes.Structure):
                 ("handle", ctypes.c_uint64)]
 
 
+class Job(ctypes.Structure):
+    _fields_ = [("text", ctypes.c_void_p), ("nbytes", ctypes.c_uint64)]
+
+
+class JobInfo(ctypes.Structure):
+    _fields_ = [("queued_us", ctypes.c_double), ("run_us", ctypes.c_double),
+                ("batch_jobs", ctypes.c_int), ("worker", ctypes.c_int)]
+
+
 class Stats(ctypes.Structure):
     _fields_ = [("ms_device", ctypes.c_double), ("ms_h2d", ctypes.c_double),
                 ("ms_d2h", ctypes.c_double), ("ms_wall", ctypes.c_double),
@@ -82,7 +92,7 @@ class Stats(ctypes.Structure):
                 ("dev_bytes_peak", ctypes.c_uint64), ("variant_used", ctypes.c_int),
                 ("partition_levels", ctypes.c_int), ("n_bins", ctypes.c_uint64),
                 ("ms_kernel", ctypes.c_double * 8), ("launches_kernel", ctypes.c_uint64 * 8),
-                ("n_partitioned", ctypes.c_uint64)]
+                ("n_partitioned", ctypes.c_uint64), ("n_waves", ctypes.c_uint64)]
 
     KERNEL_NAMES = ["extract_count", "extract_scatter", "partition_hist", "partition_scatter",
                     "bin_count", "compact", "hash_insert", "other"]
@@ -120,6 +130,14 @@ def load_library(path: str = LIB_PATH):
     lib.dk_last_stats.argtypes = [vp, ctypes.POINTER(Stats)]
     lib.dk_num_lines.argtypes = [vp, u64, i32]
     lib.dk_num_lines.restype = ctypes.c_int64
+    lib.dk_count_batch.argtypes = [vp, ctypes.POINTER(Job), i32, ctypes.POINTER(InputDesc),
+                                   ctypes.POINTER(Table)]
+    lib.dk_serve_start.argtypes = [vp, i32, i32]
+    lib.dk_submit.argtypes = [vp, vp, u64, ctypes.POINTER(InputDesc), ctypes.POINTER(u64)]
+    lib.dk_poll.argtypes = [vp, u64, ctypes.POINTER(Table), ctypes.POINTER(JobInfo)]
+    lib.dk_wait.argtypes = [vp, u64, i32, ctypes.POINTER(Table), ctypes.POINTER(JobInfo)]
+    lib.dk_cancel.argtypes = [vp, u64]
+    lib.dk_serve_stop.argtypes = [vp]
     lib.dk_host_alloc.argtypes = [u64, ctypes.POINTER(vp)]
     lib.dk_host_free.argtypes = [vp]
     _lib = lib
@@ -237,6 +255,87 @@ class Engine:
         finally:
             self.free_table(t)
             del keep
+
+    def count_batch(self, texts, line_width: int, k: int, variant: int = VARIANT_AUTO
+                    ) -> list[CountResult]:
+        """Count each read set of `texts` (one pipeline, memory-bounded waves)."""
+        keep = [_buf_ptr(t) for t in texts]
+        jobs = (Job * max(1, len(texts)))()
+        for j, (ptr, n, _) in enumerate(keep):
+            jobs[j].text = ptr
+            jobs[j].nbytes = n
+        outs = (Table * max(1, len(texts)))()
+        d = self.desc(line_width, k, variant)
+        self._check(self.lib.dk_count_batch(self.h, jobs, len(texts), ctypes.byref(d), outs),
+                    "dk_count_batch")
+        res = []
+        try:
+            for j in range(len(texts)):
+                t = outs[j]
+                nd = int(t.n)
+                if nd:
+                    kmers = np.ctypeslib.as_array(t.kmers, shape=(nd,)).copy()
+                    counts = np.ctypeslib.as_array(t.counts, shape=(nd,)).copy()
+                else:
+                    kmers, counts = np.zeros(0, np.uint64), np.zeros(0, np.uint32)
+                res.append(CountResult(kmers, counts, int(t.n_kmers), int(t.variant_used)))
+        finally:
+            for j in range(len(texts)):
+                if outs[j].handle:
+                    self.free_table(outs[j])
+        return res
+
+    # ------------------------------------------------------------- serving
+    def serve_start(self, workers: int = 2, max_batch_jobs: int = 1024):
+        self._check(self.lib.dk_serve_start(self.h, workers, max_batch_jobs), "dk_serve_start")
+        self._inflight = {}
+
+    def serve_stop(self):
+        self._check(self.lib.dk_serve_stop(self.h), "dk_serve_stop")
+        self._inflight = {}
+
+    def submit(self, text, line_width: int, k: int, variant: int = VARIANT_AUTO) -> int:
+        ptr, n, keep = _buf_ptr(text)
+        t = ctypes.c_uint64(0)
+        d = self.desc(line_width, k, variant)
+        self._check(self.lib.dk_submit(self.h, ctypes.c_void_p(ptr), n, ctypes.byref(d),
+                                       ctypes.byref(t)), "dk_submit")
+        self._inflight[t.value] = keep  # the text is borrowed until the job completes
+        return t.value
+
+    def _take(self, ticket: int, rc: int, t: Table, info: JobInfo):
+        if rc == DK_ERR_PENDING or rc == DK_ERR_TIMEOUT:
+            return None
+        self._inflight.pop(ticket, None)
+        self._check(rc, "served job")
+        try:
+            nd = int(t.n)
+            if nd:
+                kmers = np.ctypeslib.as_array(t.kmers, shape=(nd,)).copy()
+                counts = np.ctypeslib.as_array(t.counts, shape=(nd,)).copy()
+            else:
+                kmers, counts = np.zeros(0, np.uint64), np.zeros(0, np.uint32)
+            res = CountResult(kmers, counts, int(t.n_kmers), int(t.variant_used))
+        finally:
+            if t.handle:
+                self.free_table(t)
+        return res, {"queued_us": info.queued_us, "run_us": info.run_us,
+                     "batch_jobs": info.batch_jobs, "worker": info.worker}
+
+    def poll(self, ticket: int):
+        t, info = Table(), JobInfo()
+        return self._take(ticket, self.lib.dk_poll(self.h, ticket, ctypes.byref(t),
+                                                   ctypes.byref(info)), t, info)
+
+    def wait(self, ticket: int, timeout_ms: int = 60_000):
+        t, info = Table(), JobInfo()
+        rc = self.lib.dk_wait(self.h, ticket, timeout_ms, ctypes.byref(t), ctypes.byref(info))
+        if rc == DK_ERR_TIMEOUT:
+            raise DkError(rc, "dk_wait timed out")
+        return self._take(ticket, rc, t, info)
+
+    def cancel(self, ticket: int) -> int:
+        return int(self.lib.dk_cancel(self.h, ticket))
 
     def stats(self) -> dict:
         s = Stats()

@@ -228,6 +228,7 @@ int Engine::acquire_table(uint64_t n, bool on_device, TableBuf** out) {
     best = &tables.back();
   }
   best->in_use = true;
+  best->refs = 1;
   *out = best;
   (void)e;
   return DK_OK;
@@ -236,10 +237,158 @@ int Engine::acquire_table(uint64_t n, bool on_device, TableBuf** out) {
 int Engine::release_table(uint64_t id) {
   for (auto& t : tables)
     if (t.id == id && t.in_use) {
-      t.in_use = false;
+      if (t.refs > 1) {
+        --t.refs;
+      } else {
+        t.refs = 0;
+        t.in_use = false;
+      }
       return DK_OK;
     }
   return DK_ERR_NOT_FOUND;
+}
+
+// ------------------------------------------------------------ batch mode
+int JobSet::upload_bounds(Engine* e) {
+  const size_t n = (size_t)njobs;
+  std::vector<uint64_t> nul(job_start.begin() + 1, job_start.end());
+  DK_CUDA(cudaMemcpyAsync(d_start, job_start.data(), (n + 1) * 8, cudaMemcpyHostToDevice, e->stream));
+  DK_CUDA(cudaMemcpyAsync(d_end, job_end.data(), n * 8, cudaMemcpyHostToDevice, e->stream));
+  DK_CUDA(cudaMemcpyAsync(d_nul, nul.data(), n * 8, cudaMemcpyHostToDevice, e->stream));
+  DK_CUDA(cudaStreamSynchronize(e->stream));  // host vectors are pageable and short-lived
+  return DK_OK;
+}
+
+int JobSet::apply_nul(Engine* e) {
+  std::vector<uint64_t> nul((size_t)njobs);
+  DK_CUDA(cudaMemcpyAsync(nul.data(), d_nul, (size_t)njobs * 8, cudaMemcpyDeviceToHost, e->stream));
+  DK_CUDA(cudaStreamSynchronize(e->stream));
+  for (int j = 0; j < njobs; ++j) job_end[j] = std::min(job_end[j], nul[j]);
+  return DK_OK;
+}
+
+// Count many read sets in memory-bounded waves; each wave is one pass of the
+// device pipeline in which every job is its own level-1 bucket.
+int Engine::count_batch(const dk_job* jobs, int njobs, const dk_input_desc* desc, dk_table* outs) {
+  Engine* e = this;
+  std::lock_guard<std::mutex> g(mu);
+  const auto w0 = std::chrono::steady_clock::now();
+  if (!jobs || njobs < 0 || !desc || !outs) {
+    set_error("null argument");
+    return DK_ERR_INVALID_ARG;
+  }
+  for (int j = 0; j < njobs; ++j) std::memset(&outs[j], 0, sizeof(dk_table));
+  if (desc->k < 1 || desc->k > 32 || desc->line_width < 1 || desc->line_width > 1024 ||
+      desc->convention != DK_CONV_DAKC || desc->variant < DK_VARIANT_AUTO ||
+      desc->variant > DK_VARIANT_HASH || desc->residency != DK_RESIDENT_HOST) {
+    set_error("invalid input descriptor (batch results are host-resident)");
+    return DK_ERR_INVALID_ARG;
+  }
+  const int W = desc->line_width, k = desc->k;
+  const uint64_t stride = (uint64_t)W + 1;
+  const uint64_t per_line = W >= k ? (uint64_t)(W - k + 1) : 0;
+  std::vector<uint64_t> lines(njobs);
+  for (int j = 0; j < njobs; ++j) {
+    const int64_t L = frame_lines(jobs[j].nbytes, W);
+    if (L < 0 || (!jobs[j].text && jobs[j].nbytes)) {
+      set_error("job " + std::to_string(j) + ": size is not a whole number of lines");
+      return DK_ERR_INVALID_ARG;
+    }
+    lines[j] = (uint64_t)L;
+  }
+  DK_CUDA(cudaSetDevice(device));
+  // device bytes per job: text + two key buffers + staged counts + table
+  auto est = [&](int j) { return lines[j] * stride + 32 * lines[j] * per_line + 4096; };
+  const uint64_t wave_cap = budget ? (uint64_t)(0.7 * (double)budget) : ~0ull;
+  stats_batch = dk_stats();
+  double ms_device = 0, ms_h2d = 0, ms_d2h = 0;
+  uint64_t launches_total = 0;
+  int j0 = 0;
+  while (j0 < njobs) {
+    // greedy wave: consecutive jobs while they fit the budget and the bucket limit
+    int j1 = j0;
+    uint64_t bytes = 0;
+    while (j1 < njobs && j1 - j0 < (1 << kMaxL1Bits) && (j1 == j0 || bytes + est(j1) <= wave_cap)) {
+      bytes += est(j1);
+      ++j1;
+    }
+    if (bytes > wave_cap) {
+      set_error("job " + std::to_string(j0) + " alone exceeds the memory budget");
+      return DK_ERR_ADMISSION;
+    }
+    const int nj = j1 - j0;
+    JobSet js;
+    js.njobs = nj;
+    js.job_start.assign(nj + 1, 0);
+    for (int j = 0; j < nj; ++j) js.job_start[j + 1] = js.job_start[j] + lines[j0 + j];
+    js.job_end.assign(js.job_start.begin() + 1, js.job_start.end());
+    const uint64_t total_lines = js.job_start[nj];
+    const uint64_t wave_bytes = total_lines * stride;
+    DK_TRY(Arena::ensure(this, text, wave_bytes + 64));
+    DK_TRY(Arena::ensure(this, jobmeta, (size_t)(3 * nj + 1) * 8));
+    js.d_start = (uint64_t*)jobmeta.p;
+    js.d_end = js.d_start + nj + 1;
+    js.d_nul = (unsigned long long*)(js.d_end + nj);
+    DK_CUDA(cudaEventRecord(ev_h2d0, stream));
+    for (int j = 0; j < nj; ++j)
+      if (jobs[j0 + j].nbytes)
+        DK_TRY(upload(jobs[j0 + j].text, jobs[j0 + j].nbytes,
+                      (uint8_t*)text.p + js.job_start[j] * stride));
+    TableBuf* dev_tb = nullptr;
+    DK_TRY(acquire_table(total_lines * per_line, true, &dev_tb));
+    out_k = (uint64_t*)dev_tb->k;
+    out_c = (uint32_t*)dev_tb->c;
+    DeviceTable dt;
+    int rc = count_device((const uint8_t*)text.p, wave_bytes, *desc, &dt, &js);
+    if (rc != DK_OK) {
+      release_table(dev_tb->id);
+      return rc;
+    }
+    float t_h2d = 0;
+    cudaEventElapsedTime(&t_h2d, ev_h2d0, ev_stage[0]);
+    ms_h2d += t_h2d;
+    ms_device += stats.ms_device;
+    launches_total += stats.kernel_launches;
+    TableBuf* h_tb = nullptr;
+    rc = acquire_table(std::max<uint64_t>(dt.n, 1), false, &h_tb);
+    if (rc != DK_OK) {
+      release_table(dev_tb->id);
+      return rc;
+    }
+    if (dt.n) {
+      DK_CUDA(cudaMemcpyAsync(h_tb->k, dev_tb->k, dt.n * 8, cudaMemcpyDeviceToHost, stream));
+      DK_CUDA(cudaMemcpyAsync(h_tb->c, dev_tb->c, dt.n * 4, cudaMemcpyDeviceToHost, stream));
+    }
+    DK_CUDA(cudaEventRecord(ev_d2h1, stream));
+    DK_CUDA(cudaEventSynchronize(ev_d2h1));
+    float t_d2h = 0;
+    cudaEventElapsedTime(&t_d2h, ev_stage[5], ev_d2h1);
+    if (dt.n) ms_d2h += t_d2h;
+    release_table(dev_tb->id);
+    h_tb->refs = (uint32_t)nj;
+    for (int j = 0; j < nj; ++j) {
+      dk_table& t = outs[j0 + j];
+      const bool has = !js.nodes.empty();
+      const uint64_t d = has ? js.nodes[j].d : 0, off = has ? js.nodes[j].out_off : 0;
+      t.kmers = (uint64_t*)h_tb->k + off;
+      t.counts = (uint32_t*)h_tb->c + off;
+      t.n = d;
+      t.n_kmers = has ? js.nodes[j].n : 0;
+      t.on_device = 0;
+      t.variant_used = stats.variant_used;
+      t.handle = h_tb->id;
+    }
+    j0 = j1;
+    ++stats_batch.n_waves;
+  }
+  stats_batch.ms_device = ms_device;
+  stats_batch.ms_h2d = ms_h2d;
+  stats_batch.ms_d2h = ms_d2h;
+  stats_batch.kernel_launches = launches_total;
+  stats_batch.ms_wall =
+      std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - w0).count();
+  stats = stats_batch;
+  return DK_OK;
 }
 
 // Copy host reads into device memory: one async copy when the buffer is
@@ -261,18 +410,18 @@ int Engine::upload(const char* h, uint64_t nbytes, uint8_t* d) {
     if (!stage_pinned[i]) DK_CUDA(cudaMallocHost(&stage_pinned[i], slot));
     if (!stage_ev[i]) DK_CUDA(cudaEventCreateWithFlags(&stage_ev[i], cudaEventDisableTiming));
   }
+  // a slot is refilled only after the copy that last read it has finished,
+  // also across calls (batches upload job after job)
   uint64_t off = 0;
-  int i = 0;
-  bool used[2] = {false, false};
   while (off < nbytes) {
+    const int i = stage_next;
     const size_t len = (size_t)std::min<uint64_t>(slot, nbytes - off);
-    if (used[i]) DK_CUDA(cudaEventSynchronize(stage_ev[i]));
+    DK_CUDA(cudaEventSynchronize(stage_ev[i]));
     std::memcpy(stage_pinned[i], h + off, len);
     DK_CUDA(cudaMemcpyAsync(d + off, stage_pinned[i], len, cudaMemcpyHostToDevice, stream));
     DK_CUDA(cudaEventRecord(stage_ev[i], stream));
-    used[i] = true;
     off += len;
-    i ^= 1;
+    stage_next ^= 1;
   }
   return DK_OK;
 }
@@ -280,7 +429,7 @@ int Engine::upload(const char* h, uint64_t nbytes, uint8_t* d) {
 // The device pipeline: reads at d_text (nbytes, padded by >= 64 bytes of
 // readable memory) -> sorted table in out (device).  Fills stats.
 int Engine::count_device(const uint8_t* d_text, uint64_t nbytes, const dk_input_desc& desc,
-                         DeviceTable* out) {
+                         DeviceTable* out, JobSet* js) {
   Engine* e = this;
   const int W = desc.line_width, k = desc.k;
   out->n = 0;
@@ -291,7 +440,7 @@ int Engine::count_device(const uint8_t* d_text, uint64_t nbytes, const dk_input_
   // the hash-first bin count needs a free sentinel key, i.e. k <= 31
   const bool use_hash = desc.variant != DK_VARIANT_SORT && desc.k <= 31;
   stats.variant_used = use_hash ? DK_VARIANT_HASH : DK_VARIANT_SORT;
-  int64_t L0 = frame_lines(nbytes, W);
+  int64_t L0 = js ? (int64_t)js->job_start.back() : frame_lines(nbytes, W);
   if (L0 < 0) {
     set_error("buffer size is not a whole number of lines");
     return DK_ERR_INVALID_ARG;
@@ -322,8 +471,9 @@ int Engine::count_device(const uint8_t* d_text, uint64_t nbytes, const dk_input_
     B1 = ceil_log2((uint64_t)((double)n_upper / (target * kFanout)) + 1);
   B1 = std::max(1, std::min(B1, kMaxL1Bits));
   B1 = std::min(B1, 2 * k);
-  const int F1 = 1 << B1;
-  const int shift1 = 2 * k - B1;
+  // batch mode: one level-1 bucket per job, all 2k bits still free
+  const int F1 = js ? js->njobs : (1 << B1);
+  const int shift1 = js ? 2 * k : 2 * k - B1;
   const int G = 2 * sm_count;
 
   ExtractArgs a;
@@ -334,6 +484,10 @@ int Engine::count_device(const uint8_t* d_text, uint64_t nbytes, const dk_input_
   a.kmask = (~0ull) >> (64 - 2 * k);
   a.shift1 = shift1;
   a.F1 = F1;
+  a.njobs = js ? js->njobs : 0;
+  a.job_start = js ? js->d_start : nullptr;
+  a.job_end = js ? js->d_end : nullptr;
+  a.job_nul = js ? js->d_nul : nullptr;
 
   DK_TRY(Arena::ensure(this, H, (size_t)G * F1 * 4));
   DK_TRY(Arena::ensure(this, O, (size_t)G * F1 * 8));
@@ -348,6 +502,7 @@ int Engine::count_device(const uint8_t* d_text, uint64_t nbytes, const dk_input_
   for (int attempt = 0; attempt < 2; ++attempt) {
     a.n_lines = L;
     DK_CUDA(cudaMemsetAsync(ctrs.p, 0, 256, stream));
+    if (js) DK_TRY(js->upload_bounds(this));
     TIMED(0, launch_l1_count(a, G, (uint32_t*)H.p, c64, stream));
     uint64_t hc[2];
     DK_TRY(sync_read(c64, 16, hc));
@@ -355,10 +510,15 @@ int Engine::count_device(const uint8_t* d_text, uint64_t nbytes, const dk_input_
       n_kmers = hc[0];
       break;
     }
-    L = L - hc[1];  // first line whose first byte is NUL
+    if (js) {
+      DK_TRY(js->apply_nul(this));  // each job stops before its first NUL-led line
+    } else {
+      L = L - hc[1];  // first line whose first byte is NUL
+    }
   }
   stats.n_lines = L;
   DK_CUDA(cudaEventRecord(ev_stage[1], stream));
+  if (n_kmers == 0 && js) js->clear_results();
   if (n_kmers == 0) {
     DK_CUDA(cudaEventRecord(ev_stage[6], stream));
     DK_CUDA(cudaEventSynchronize(ev_stage[6]));
@@ -470,6 +630,11 @@ int Engine::count_device(const uint8_t* d_text, uint64_t nbytes, const dk_input_
   TIMED(5, launch_compact((Node*)nodes.p, (uint32_t*)finals.p, n_final, (uint64_t*)keysA.p,
                           (uint64_t*)keysB.p, (uint32_t*)cnt.p, out_k, out_c, stream));
   DK_CUDA(cudaGetLastError());
+  if (js) {
+    js->nodes.resize(F1);
+    DK_CUDA(cudaMemcpyAsync(js->nodes.data(), nodes.p, (size_t)F1 * sizeof(Node),
+                            cudaMemcpyDeviceToHost, stream));
+  }
   DK_CUDA(cudaEventRecord(ev_stage[5], stream));
   DK_CUDA(cudaEventSynchronize(ev_stage[5]));
   float ms = 0;
@@ -584,12 +749,23 @@ int Engine::count(const char* text, uint64_t nbytes, bool text_on_device, const 
 
 // =================================================================== C ABI
 using dk::Engine;
+namespace dk { struct Server; }
 
 extern "C" {
 
 struct dk_ctx {
   Engine eng;
+  dk::Server* server = nullptr;
 };
+
+extern "C++" {
+namespace dk {
+Server* server_of(dk_ctx* ctx) { return ctx->server; }
+void set_server(dk_ctx* ctx, Server* s) { ctx->server = s; }
+Engine* engine_of(dk_ctx* ctx) { return &ctx->eng; }
+int serve_release(Server* s, uint64_t handle);
+}  // namespace dk
+}
 
 int dk_abi_version(void) { return DK_ABI_VERSION; }
 
@@ -626,6 +802,7 @@ int dk_create(const dk_config* cfg, dk_ctx** out) {
 
 int dk_destroy(dk_ctx* ctx) {
   if (!ctx) return DK_ERR_INVALID_ARG;
+  if (ctx->server) dk_serve_stop(ctx);
   delete ctx;
   return DK_OK;
 }
@@ -646,9 +823,20 @@ int dk_count_device(dk_ctx* ctx, const char* d_text, uint64_t nbytes, const dk_i
   return ctx->eng.count(d_text, nbytes, true, desc, out);
 }
 
+int dk_count_batch(dk_ctx* ctx, const dk_job* jobs, int njobs, const dk_input_desc* desc,
+                   dk_table* outs) {
+  if (!ctx) return DK_ERR_INVALID_ARG;
+  return ctx->eng.count_batch(jobs, njobs, desc, outs);
+}
+
 int dk_table_free(dk_ctx* ctx, dk_table* t) {
   if (!ctx || !t) return DK_ERR_INVALID_ARG;
   if (!t->handle) return DK_OK;  // empty table
+  if (t->handle >> 48) {  // a served table: owned by one of the serving workers
+    const int rc = dk::serve_release(ctx->server, t->handle);
+    std::memset(t, 0, sizeof(*t));
+    return rc;
+  }
   std::lock_guard<std::mutex> g(ctx->eng.mu);
   const int rc = ctx->eng.release_table(t->handle);
   std::memset(t, 0, sizeof(*t));

@@ -8,6 +8,7 @@
 #include <vector>
 
 #include "../../include/dakc_gb300.h"
+#include "dk_internal.cuh"
 
 namespace dk {
 
@@ -32,6 +33,7 @@ struct TableBuf {
   uint64_t id = 0;
   bool on_device = false;
   bool in_use = false;
+  uint32_t refs = 0;  // tables handed out on this buffer (batch results share one)
 };
 
 struct DeviceTable {
@@ -43,6 +45,23 @@ struct DeviceTable {
 
 int64_t frame_lines(uint64_t nbytes, int W);
 
+struct Engine;
+
+// Line ranges of the read sets counted together by dk_count_batch.  Host
+// copies plus device mirrors used by the level-1 kernels.
+struct JobSet {
+  int njobs = 0;
+  std::vector<uint64_t> job_start;  // njobs + 1 line offsets
+  std::vector<uint64_t> job_end;    // lines parsed per job end here
+  uint64_t* d_start = nullptr;      // device mirrors (inside the engine's job arena)
+  uint64_t* d_end = nullptr;
+  unsigned long long* d_nul = nullptr;
+  std::vector<Node> nodes;          // level-1 nodes read back after the count
+  int upload_bounds(Engine* e);     // job_end -> device, job_nul reset
+  int apply_nul(Engine* e);         // shorten job_end to each job's first NUL-led line
+  void clear_results() { nodes.clear(); }
+};
+
 struct Engine {
   int device = 0;
   int sm_count = 0;
@@ -52,6 +71,7 @@ struct Engine {
   std::mutex mu;
   std::string last_error;
   dk_stats stats{};
+  dk_stats stats_batch{};
   uint64_t launches = 0;
 
   // device arenas
@@ -75,6 +95,7 @@ struct Engine {
   void* h_scratch = nullptr;
   void* stage_pinned[2] = {nullptr, nullptr};
   cudaEvent_t stage_ev[2] = {nullptr, nullptr};
+  int stage_next = 0;
 
   int init(const dk_config* cfg);
   ~Engine();
@@ -84,7 +105,9 @@ struct Engine {
   int acquire_table(uint64_t n, bool on_device, TableBuf** out);
   int release_table(uint64_t id);
   int count_device(const uint8_t* d_text, uint64_t nbytes, const dk_input_desc& desc,
-                   DeviceTable* out);
+                   DeviceTable* out, JobSet* js = nullptr);
+  int count_batch(const dk_job* jobs, int njobs, const dk_input_desc* desc, dk_table* outs);
+  DevBuf jobmeta;  // device job_start / job_end / job_nul
   int count(const char* text, uint64_t nbytes, bool text_on_device, const dk_input_desc* desc,
             dk_table* out);
 };

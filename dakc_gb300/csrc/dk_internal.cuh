@@ -59,8 +59,17 @@ struct ExtractArgs {
   int W;
   int k;
   uint64_t kmask;
-  int shift1;  // level-1 bucket = key >> shift1
+  int shift1;  // level-1 bucket = key >> shift1 (plain mode)
   int F1;      // number of level-1 buckets
+  // batch ("jobs") mode when njobs > 0: the text is the concatenation of njobs
+  // read sets; job j owns lines [job_start[j], job_start[j+1]) of which lines
+  // >= job_end[j] are not parsed (a NUL-led line ends that job), and the
+  // level-1 bucket of a k-mer is its job.  job_nul[j] receives the first
+  // NUL-led line of job j (initialised to job_start[j+1]).
+  int njobs;
+  const uint64_t* job_start;
+  const uint64_t* job_end;
+  unsigned long long* job_nul;
 };
 
 // ---- launchers (dk_kernels.cu); every launcher returns the number of kernel

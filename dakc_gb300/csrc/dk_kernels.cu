@@ -127,6 +127,16 @@ __host__ __device__ inline uint32_t tile_buf_bytes(uint32_t lt, uint64_t stride)
   return (uint32_t)(((uint64_t)lt * stride + 32 + 127) & ~127ull);
 }
 
+// job that owns line l in batch mode (binary search over job_start)
+__device__ __forceinline__ uint32_t job_of_line(const ExtractArgs& a, uint64_t l) {
+  uint32_t lo = 0, hi = (uint32_t)a.njobs;
+  while (hi - lo > 1) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (__ldg(a.job_start + mid) <= l) lo = mid; else hi = mid;
+  }
+  return lo;
+}
+
 // counters[0] = k-mers, [1] = n_lines - (first NUL-led line), [3] = device error
 template <int C>
 __global__ void __launch_bounds__(512) k_l1_count(ExtractArgs a, uint32_t* __restrict__ H,
@@ -171,6 +181,18 @@ __global__ void __launch_bounds__(512) k_l1_count(ExtractArgs a, uint32_t* __res
     T.range(t, &l0, &l1);
     for (uint64_t l = l0 + warp; l < l1; l += nwarps) {
       const uint8_t* line = base + (l - l0) * stride;
+      if (a.njobs) {
+        const uint32_t job = job_of_line(a, l);
+        if (l >= __ldg(a.job_end + job)) continue;  // past the job's first NUL-led line
+        if (lane_id() == 0 && l > __ldg(a.job_start + job) && line[0] == 0) {
+          atomicMin(&a.job_nul[job], (unsigned long long)l);
+          atomicMax(&counters[1], 1ull);
+        }
+        warp_line_kmers<C>(line, a.W, a.k, a.kmask, lut, [&](int, uint64_t, bool valid) {
+          if (valid) { atomicAdd(&hist[job], 1u); ++mine; }
+        });
+        continue;
+      }
       if (lane_id() == 0 && l > 0 && line[0] == 0) atomicMax(&counters[1], a.n_lines - l);
       warp_line_kmers<C>(line, a.W, a.k, a.kmask, lut, [&](int, uint64_t key, bool valid) {
         if (valid) { atomicAdd(&hist[key >> a.shift1], 1u); ++mine; }
@@ -283,16 +305,24 @@ __global__ void __launch_bounds__(512, 2) k_l1_scatter(ExtractArgs a, const uint
     T.range(ti, &t0, &t1);
     uint64_t kr[LPW][C];
     uint32_t sr[LPW][C];
+    uint32_t jr[LPW];
 #pragma unroll
     for (int j = 0; j < LPW; ++j) {
       const uint64_t l = t0 + (uint64_t)j * nwarps + warp;
-      if (l < t1) {
+      uint32_t job = 0;
+      bool live = l < t1;
+      if (live && a.njobs) {
+        job = job_of_line(a, l);
+        live = l < __ldg(a.job_end + job);
+      }
+      if (live) {
         warp_line_kmers<C>(base + (l - t0) * stride, a.W, a.k, a.kmask, lut,
                            [&](int t, uint64_t key, bool valid) {
                              kr[j][t] = key;
-                             sr[j][t] = valid ? atomicAdd(&tile_hist[key >> a.shift1], 1u)
-                                              : 0xFFFFFFFFu;
+                             const uint32_t bkt = a.njobs ? job : (uint32_t)(key >> a.shift1);
+                             sr[j][t] = valid ? atomicAdd(&tile_hist[bkt], 1u) : 0xFFFFFFFFu;
                            });
+        jr[j] = job;
       } else {
 #pragma unroll
         for (int t = 0; t < C; ++t) { kr[j][t] = 0; sr[j][t] = 0xFFFFFFFFu; }
@@ -306,12 +336,28 @@ __global__ void __launch_bounds__(512, 2) k_l1_scatter(ExtractArgs a, const uint
     for (int j = 0; j < LPW; ++j)
 #pragma unroll
       for (int t = 0; t < C; ++t)
-        if (sr[j][t] != 0xFFFFFFFFu) staging[tile_off[kr[j][t] >> a.shift1] + sr[j][t]] = kr[j][t];
+        if (sr[j][t] != 0xFFFFFFFFu) {
+          const uint32_t bkt = a.njobs ? jr[j] : (uint32_t)(kr[j][t] >> a.shift1);
+          staging[tile_off[bkt] + sr[j][t]] = kr[j][t];
+        }
     __syncthreads();
-    for (uint32_t i = threadIdx.x; i < Tn; i += blockDim.x) {
-      const uint64_t key = staging[i];
-      const uint32_t b = (uint32_t)(key >> a.shift1);
-      keys_out[cursor[b] + (i - tile_off[b])] = key;
+    if (a.njobs) {
+      // batch mode: a staged key's bucket is the job whose run contains it
+      for (uint32_t i = threadIdx.x; i < Tn; i += blockDim.x) {
+        // the largest bucket whose run starts at or before i is the one that holds i
+        uint32_t lo = 0, hi = (uint32_t)F1;
+        while (hi - lo > 1) {
+          const uint32_t mid = (lo + hi) >> 1;
+          if (tile_off[mid] <= i) lo = mid; else hi = mid;
+        }
+        keys_out[cursor[lo] + (i - tile_off[lo])] = staging[i];
+      }
+    } else {
+      for (uint32_t i = threadIdx.x; i < Tn; i += blockDim.x) {
+        const uint64_t key = staging[i];
+        const uint32_t b = (uint32_t)(key >> a.shift1);
+        keys_out[cursor[b] + (i - tile_off[b])] = key;
+      }
     }
     __syncthreads();
     for (int b = threadIdx.x; b < F1; b += blockDim.x) {

@@ -116,6 +116,7 @@ typedef struct {
   double ms_kernel[8];
   uint64_t launches_kernel[8];
   uint64_t n_partitioned;  /* keys moved by partition levels below level 1    */
+  uint64_t n_waves;        /* dk_count_batch: memory-bounded waves run         */
 } dk_stats;
 
 /* One read set of a batch (dk_count_batch). */
@@ -146,6 +147,17 @@ int dk_count_device(dk_ctx* ctx, const char* d_text, uint64_t nbytes, const dk_i
 int dk_table_free(dk_ctx* ctx, dk_table* t);
 int dk_last_stats(dk_ctx* ctx, dk_stats* out);
 
+/* --- batched count ----------------------------------------------------- */
+/* Count njobs independent read sets (same line width and k) in one pipeline:
+ * the reference would run one kmercounter per set (kcounter.hpp:84-99); here
+ * every set is its own level-1 partition of one launch sequence, processed in
+ * waves sized to the context's memory budget (up to 4,096 sets per wave).
+ * outs[j] receives job j's sorted table (host-resident; tables of one wave
+ * share one allocation, each must still be released with dk_table_free).
+ * Per-job tables equal dk_count's on that job's text. */
+int dk_count_batch(dk_ctx* ctx, const dk_job* jobs, int njobs, const dk_input_desc* desc,
+                   dk_table* outs);
+
 /* Number of lines dk_count will parse for this buffer under the framing rules
  * above (host-side, no GPU work); negative status for a malformed size. */
 int64_t dk_num_lines(const char* text, uint64_t nbytes, int line_width);
@@ -155,6 +167,31 @@ int64_t dk_num_lines(const char* text, uint64_t nbytes, int line_width);
  * (dakc/src/fqreader/fqreader.cpp:59). */
 int dk_host_alloc(uint64_t nbytes, void** out);
 int dk_host_free(void* p);
+
+/* --- serving ----------------------------------------------------------- */
+/* A request loop over `workers` engine workers (each with its own CUDA
+ * stream, device arenas and 1/workers of the context's memory budget).  Jobs
+ * are admitted by an estimate of their device memory, queue, and are
+ * coalesced into batched launches (dk_count_batch) by whichever worker frees
+ * up first, so work of jobs that arrive while others run overlaps on the
+ * device.  No counterpart in the reference (one kmercounter per run). */
+typedef struct {
+  double queued_us;  /* submit -> start of its batch                      */
+  double run_us;     /* start of its batch -> table ready on the host     */
+  int batch_jobs;    /* jobs in the batch it ran in                       */
+  int worker;
+} dk_job_info;
+
+int dk_serve_start(dk_ctx* ctx, int workers, int max_batch_jobs);
+/* text is borrowed until the job completes (or is cancelled and polled) */
+int dk_submit(dk_ctx* ctx, const char* text, uint64_t nbytes, const dk_input_desc* desc,
+              uint64_t* ticket);
+/* DK_ERR_PENDING while queued or running; otherwise the job's status, with
+ * its table in *out (release with dk_table_free) */
+int dk_poll(dk_ctx* ctx, uint64_t ticket, dk_table* out, dk_job_info* info);
+int dk_wait(dk_ctx* ctx, uint64_t ticket, int timeout_ms, dk_table* out, dk_job_info* info);
+int dk_cancel(dk_ctx* ctx, uint64_t ticket);
+int dk_serve_stop(dk_ctx* ctx);  /* finishes queued jobs, joins the workers */
 
 /* --- counting without any allocation ------------------------------------
  * No counterpart in the reference: DAKC always allocates its buffers.

@@ -1,0 +1,66 @@
+"""dk_count_batch: many read sets in one pipeline, each table bit-exact."""
+import numpy as np
+import pytest
+
+import dakc_gb300 as dk
+from dakc_gb300 import synth
+from oracle import pyoracle
+
+pytestmark = pytest.mark.gpu
+
+
+def job_texts(n, seed=0, W=250, max_reads=3000):
+    specs = synth.batch_specs(n, seed=seed + 4, median=400, sigma=1.5, cap=max_reads)
+    assert sum(s.n_reads for s in specs) > 0
+    return [synth.batch_job_text(s, line_width=W, err_rate=0.005) for s in specs]
+
+
+@pytest.mark.parametrize("variant", [dk.VARIANT_SORT, dk.VARIANT_HASH])
+def test_batch_matches_oracle_and_plain(engine, variant):
+    texts = job_texts(40)
+    texts[3] = np.zeros(0, np.uint8)                      # empty job
+    texts[7] = texts[7][:-1]                              # last terminator missing
+    texts[9] = synth.random_lines(3, 20, 250, b"N")       # no k-mers at all
+    got = engine.count_batch(texts, 250, 31, variant)
+    assert len(got) == len(texts)
+    for j, t in enumerate(texts):
+        keys, counts, nk = pyoracle.count(t, 250, 31)
+        assert got[j].n_kmers == nk, j
+        assert np.array_equal(got[j].kmers, keys), j
+        assert np.array_equal(got[j].counts, counts), j
+    # and equal to counting each job alone
+    for j in (0, 5, 7, 20):
+        alone = engine.count(texts[j], 250, 31, variant)
+        assert np.array_equal(alone.kmers, got[j].kmers)
+        assert np.array_equal(alone.counts, got[j].counts)
+
+
+def test_batch_nul_led_line_ends_its_job(engine):
+    W = 10
+    a = b"ACGTACGTAC\nCCCCCCCCCC\n\0GGGGGGGGG\nTTTTTTTTTT\n"
+    b = b"\0AAAAAAAAA\nGGGGGGGGGG\n"   # NUL first in line 0: just a break there
+    got = engine.count_batch([a, b, a], W, 4)
+    for j, t in enumerate([a, b, a]):
+        keys, counts, nk = pyoracle.count(t, W, 4)
+        assert got[j].n_kmers == nk and np.array_equal(got[j].kmers, keys)
+        assert np.array_equal(got[j].counts, counts)
+
+
+def test_batch_waves_under_a_small_budget():
+    texts = job_texts(24, seed=3, max_reads=4000)
+    with dk.Engine(0, mem_budget=96 << 20) as small:   # 96 MB: forces several waves
+        got = small.count_batch(texts, 250, 31, dk.VARIANT_HASH)
+        st = small.stats()
+    assert st["n_waves"] >= 2
+    for j, t in enumerate(texts):
+        keys, counts, nk = pyoracle.count(t, 250, 31)
+        assert got[j].n_kmers == nk and np.array_equal(got[j].kmers, keys)
+        assert np.array_equal(got[j].counts, counts)
+
+
+def test_batch_many_small_jobs(engine):
+    texts = [synth.random_lines(100 + j, 1 + (j % 7), 100) for j in range(300)]
+    got = engine.count_batch(texts, 100, 21)
+    for j, t in enumerate(texts):
+        keys, counts, nk = pyoracle.count(t, 100, 21)
+        assert got[j].n_kmers == nk and np.array_equal(got[j].kmers, keys)

@@ -1,0 +1,72 @@
+"""Serving loop: continuous batching over engine workers (GPU).
+
+Each served job's table must equal its table when counted alone (and the
+oracle's): integer work, exact equality.
+"""
+import time
+
+import numpy as np
+import pytest
+
+import dakc_gb300 as dk
+from dakc_gb300 import synth
+from oracle import pyoracle
+
+pytestmark = pytest.mark.gpu
+
+
+def texts(n, seed):
+    specs = synth.batch_specs(n, seed=seed, median=300, sigma=1.2, cap=3000)
+    return [synth.batch_job_text(s, line_width=250) for s in specs]
+
+
+def test_served_jobs_equal_alone_and_oracle():
+    jobs = texts(60, 11)
+    with dk.Engine(0) as eng:
+        alone = [eng.count(t, 250, 31, dk.VARIANT_HASH) for t in jobs[:10]]
+        eng.serve_start(workers=2, max_batch_jobs=64)
+        tickets = []
+        for i, t in enumerate(jobs):           # bursts arrive while others run
+            tickets.append(eng.submit(t, 250, 31, dk.VARIANT_HASH))
+            if i % 15 == 14:
+                time.sleep(0.01)
+        results = [eng.wait(tk, 120_000) for tk in tickets]
+        eng.serve_stop()
+    batched = 0
+    for j, (res, info) in enumerate(results):
+        keys, counts, nk = pyoracle.count(jobs[j], 250, 31)
+        assert res.n_kmers == nk and np.array_equal(res.kmers, keys), j
+        assert np.array_equal(res.counts, counts), j
+        if j < 10:
+            assert np.array_equal(res.kmers, alone[j].kmers)
+            assert np.array_equal(res.counts, alone[j].counts)
+        batched += info["batch_jobs"] > 1
+        assert info["run_us"] > 0
+    assert batched > 0  # jobs were coalesced into batched launches
+
+
+def test_poll_cancel_and_timeout():
+    jobs = texts(8, 12)
+    with dk.Engine(0) as eng:
+        eng.serve_start(workers=1, max_batch_jobs=2)
+        tks = [eng.submit(t, 250, 31) for t in jobs]
+        c = eng.cancel(tks[-1])                      # likely still queued
+        assert c in (dk.DK_OK, dk.DK_ERR_INVALID_ARG)
+        for tk in tks[:-1]:
+            res, info = eng.wait(tk, 120_000)
+            assert res.n_kmers > 0
+        t = dk.Table()
+        rc = eng.lib.dk_poll(eng.h, tks[-1], None, None)
+        assert rc in (dk.DK_ERR_CANCELLED, dk.DK_OK)
+        assert eng.lib.dk_poll(eng.h, 987654321, None, None) == dk.DK_ERR_NOT_FOUND
+        eng.serve_stop()
+
+
+def test_admission_rejects_oversized_job():
+    big = synth.random_lines(1, 200_000, 250)   # ~50 MB of reads, ~44M k-mers
+    with dk.Engine(0, mem_budget=256 << 20) as eng:
+        eng.serve_start(workers=2, max_batch_jobs=8)
+        with pytest.raises(dk.DkError) as e:
+            eng.submit(big, 250, 31)
+        assert e.value.status == dk.DK_ERR_ADMISSION
+        eng.serve_stop()
