@@ -188,6 +188,99 @@ def run_cpu(rs, cap_reads: int, steps: int, warmup: int, threads: int):
             "seconds": t}
 
 
+def job_pool(n: int, seed: int = 4):
+    """Read sets with the batched workload's shapes: lognormal read counts
+    (median 20,000, sigma 1.5, cap 5M), lengths U[100, 250] padded to 250,
+    per-set 0.5-5 Mbp genomes, 0.5% substitutions (the first n of the
+    4,096-set sequence)."""
+    from concurrent.futures import ThreadPoolExecutor
+    from dakc_gb300 import synth
+    specs = synth.batch_specs(4096, seed=seed)[:n]
+    with ThreadPoolExecutor(max_workers=os.cpu_count() or 4) as ex:
+        texts = list(ex.map(lambda s: synth.batch_job_text(s, line_width=250), specs))
+    return texts
+
+
+def pct(xs, p):
+    return float(np.percentile(np.asarray(xs, dtype=np.float64), p)) if len(xs) else None
+
+
+def run_batched(eng, texts, variant):
+    """jobs/s of one dk_count_batch over all sets vs one dk_count per set,
+    both timed around the C calls (tables are released, not copied out);
+    per-set tables of the two forms are compared on a subset."""
+    import dakc_gb300 as dk
+    desc = dk.Engine.desc(250, 31, variant, dk.RESIDENT_HOST)
+    keep = [dk._buf_ptr(t) for t in texts]
+    eng.count_batch_nocopy(texts, 250, 31, variant)  # warm-up: pools reach steady state
+    t0 = time.perf_counter()
+    nk, nd = eng.count_batch_nocopy(texts, 250, 31, variant)
+    t_batch = time.perf_counter() - t0
+    st = eng.stats()
+
+    def one(ptr, n):
+        t = eng.count_raw(ptr, n, desc)
+        eng.free_table(t)
+
+    for ptr, n, _ in keep:
+        one(ptr, n)  # warm-up
+    lat = []
+    t0 = time.perf_counter()
+    for ptr, n, _ in keep:
+        a = time.perf_counter()
+        one(ptr, n)
+        lat.append(time.perf_counter() - a)
+    t_plain = time.perf_counter() - t0
+    sub = texts[:16]
+    got = eng.count_batch(sub, 250, 31, variant)
+    exact = all(np.array_equal(g.kmers, p.kmers) and np.array_equal(g.counts, p.counts)
+                for g, p in zip(got, (eng.count(t, 250, 31, variant) for t in sub)))
+    return {"jobs": len(texts), "k_mers": nk, "distinct": nd, "exact_vs_plain_subset": bool(exact),
+            "batched": {"jobs_per_s": len(texts) / t_batch, "kmers_per_s": nk / t_batch,
+                        "seconds": t_batch, "waves": st["n_waves"], "ms_device": st["ms_device"],
+                        "ms_h2d": st["ms_h2d"], "ms_d2h": st["ms_d2h"],
+                        "kernel_launches": st["kernel_launches"]},
+            "one_job_per_launch": {"jobs_per_s": len(texts) / t_plain, "kmers_per_s": nk / t_plain,
+                                   "seconds": t_plain, "p50_ms": 1e3 * pct(lat, 50),
+                                   "p99_ms": 1e3 * pct(lat, 99)},
+            "speedup_jobs_per_s": t_plain / t_batch}
+
+
+def run_served(texts, rate, n_jobs, variant, workers, max_batch, seed=5):
+    """Open-loop Poisson arrivals at `rate` jobs/s; sizes drawn from the pool."""
+    import dakc_gb300 as dk
+    from dakc_gb300 import synth
+    gaps = synth.exponential(seed, n_jobs, rate)
+    pick = np.random.Generator(np.random.PCG64(seed)).integers(0, len(texts), n_jobs)
+    with dk.Engine(0) as eng:
+        eng.serve_start(workers=workers, max_batch_jobs=max_batch)
+        for t in texts[:2]:  # warm-up of every worker's pools
+            for _ in range(workers):
+                eng.wait(eng.submit(t, 250, 31, variant), 600_000)
+        tickets = []
+        t0 = time.perf_counter()
+        due = t0
+        for i in range(n_jobs):
+            due += gaps[i]
+            now = time.perf_counter()
+            if due > now:
+                time.sleep(due - now)
+            tickets.append((eng.submit(texts[pick[i]], 250, 31, variant), pick[i]))
+        lat, nk, batches = [], 0, []
+        for tk, j in tickets:
+            res, info = eng.wait(tk, 600_000)
+            lat.append((info["queued_us"] + info["run_us"]) / 1e3)
+            nk += res.n_kmers
+            batches.append(info["batch_jobs"])
+        t_end = time.perf_counter()
+        eng.serve_stop()
+    span = t_end - t0
+    return {"rate": rate, "jobs": n_jobs, "jobs_per_s": n_jobs / span, "kmers_per_s": nk / span,
+            "p50_ms": pct(lat, 50), "p99_ms": pct(lat, 99), "p999_ms": pct(lat, 99.9),
+            "mean_batch_jobs": float(np.mean(batches)), "workers": workers,
+            "max_batch": max_batch}
+
+
 def alg_bytes(st: dict, nbytes: int) -> list[float]:
     nk, nd, npart = st["n_kmers"], st["n_distinct"], st["n_partitioned"]
     return [nbytes,                    # extract_count: read the text
@@ -207,13 +300,40 @@ def main():
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
     ap.add_argument("--workload", default="large_100m")
     ap.add_argument("--scale", type=float, default=1.0)
-    ap.add_argument("--variant", default="sort", choices=["auto", "sort", "hash"])
+    ap.add_argument("--variant", default="auto", choices=["auto", "sort", "hash"])
+    ap.add_argument("--l1-bits", type=int, default=0, help="level-1 partition bits (0 = auto)")
+    ap.add_argument("--bin-target", type=int, default=0, help="keys per bin (0 = auto)")
     ap.add_argument("--cpu-reads", type=int, default=4_000_000,
                     help="reads in the CPU baseline's bounded sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--mode", default="count", choices=["count", "batch", "serve"],
+                    help="count: the headline line; batch / serve: batched and served forms")
+    ap.add_argument("--jobs", type=int, default=256, help="read sets for batch / serve modes")
+    ap.add_argument("--rates", default="10,30,100,300,1000,2000")
+    ap.add_argument("--serve-jobs", type=int, default=200)
+    ap.add_argument("--no-forms", action="store_true",
+                    help="skip the batched / served summaries in the headline line")
     args = ap.parse_args()
     rank, world, local = dist_env()
+
+    if args.mode in ("batch", "serve") and args.impl == "engine":
+        import dakc_gb300 as dk
+        variant = {"auto": dk.VARIANT_AUTO, "sort": dk.VARIANT_SORT,
+                   "hash": dk.VARIANT_HASH}[args.variant]
+        texts = job_pool(args.jobs)
+        if args.mode == "batch":
+            with dk.Engine(local) as eng:
+                out = run_batched(eng, texts, variant)
+            out.update(mode="batch", workload="batch_jobs (first %d of 4,096 sets)" % len(texts))
+            print(json.dumps(out), flush=True)
+        else:
+            for r in [float(x) for x in args.rates.split(",")]:
+                cb = run_served(texts, r, args.serve_jobs, variant, workers=2, max_batch=1024)
+                one = run_served(texts, r, args.serve_jobs, variant, workers=1, max_batch=1)
+                print(json.dumps({"mode": "serve", "continuous_batching": cb,
+                                  "one_job_per_launch": one}), flush=True)
+        return 0
 
     if args.impl == "reference":
         if rank != 0:
@@ -251,7 +371,8 @@ def main():
     d_text = torch.empty(nbytes + 64, dtype=torch.uint8, device=f"cuda:{local}")
     d_text[:nbytes].copy_(torch.from_numpy(rs.text))
     torch.cuda.synchronize()
-    desc = dk.Engine.desc(rs.line_width, rs.k, variant, dk.RESIDENT_DEVICE)
+    desc = dk.Engine.desc(rs.line_width, rs.k, variant, dk.RESIDENT_DEVICE, args.l1_bits,
+                          args.bin_target)
 
     def step():
         t = eng.count_raw(d_text.data_ptr(), nbytes, desc, on_device=True)
@@ -321,6 +442,14 @@ def main():
                "ms_h2d": st["ms_h2d"], "ms_d2h": st["ms_d2h"]}
         pin.free()
 
+    forms = None
+    if rank == 0 and world == 1 and not args.no_forms:
+        texts = job_pool(64)
+        forms = {"batched": run_batched(eng, texts, variant),
+                 "served": {"continuous_batching": run_served(texts, 100.0, 64, variant, 2, 1024),
+                            "one_job_per_launch": run_served(texts, 100.0, 64, variant, 1, 1)},
+                 "note": "first 64 sets of the 4,096-set batched workload; served: Poisson 100 jobs/s"}
+
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -345,6 +474,7 @@ def main():
             "e2e": e2e,
             "cpu_baseline": ({k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")}
                              if cpu else None),
+            "forms": forms,
         }
         print(json.dumps(line), flush=True)
     eng.close()

@@ -63,7 +63,8 @@ class Config(ctypes.Structure):
 class InputDesc(ctypes.Structure):
     _fields_ = [("line_width", ctypes.c_int), ("k", ctypes.c_int), ("convention", ctypes.c_int),
                 ("variant", ctypes.c_int), ("residency", ctypes.c_int),
-                ("reserved", ctypes.c_int * 3)]
+                ("l1_bits", ctypes.c_int), ("bin_target", ctypes.c_int),
+                ("reserved", ctypes.c_int)]
 
 
 class Table(ctypes.Structure):
@@ -227,8 +228,8 @@ class Engine:
 
     @staticmethod
     def desc(line_width: int, k: int, variant: int = VARIANT_AUTO,
-             residency: int = RESIDENT_HOST) -> InputDesc:
-        return InputDesc(line_width, k, CONV_DAKC, variant, residency)
+             residency: int = RESIDENT_HOST, l1_bits: int = 0, bin_target: int = 0) -> InputDesc:
+        return InputDesc(line_width, k, CONV_DAKC, variant, residency, l1_bits, bin_target, 0)
 
     def count_raw(self, ptr: int, nbytes: int, d: InputDesc, on_device: bool = False) -> Table:
         t = Table()
@@ -255,6 +256,24 @@ class Engine:
         finally:
             self.free_table(t)
             del keep
+
+    def count_batch_nocopy(self, texts, line_width: int, k: int, variant: int = VARIANT_AUTO):
+        """dk_count_batch without copying the tables out; returns (n_kmers, n_distinct)."""
+        keep = [_buf_ptr(t) for t in texts]
+        jobs = (Job * max(1, len(texts)))()
+        for j, (ptr, n, _) in enumerate(keep):
+            jobs[j].text = ptr
+            jobs[j].nbytes = n
+        outs = (Table * max(1, len(texts)))()
+        d = self.desc(line_width, k, variant)
+        self._check(self.lib.dk_count_batch(self.h, jobs, len(texts), ctypes.byref(d), outs),
+                    "dk_count_batch")
+        nk = sum(int(outs[j].n_kmers) for j in range(len(texts)))
+        nd = sum(int(outs[j].n) for j in range(len(texts)))
+        for j in range(len(texts)):
+            if outs[j].handle:
+                self.free_table(outs[j])
+        return nk, nd
 
     def count_batch(self, texts, line_width: int, k: int, variant: int = VARIANT_AUTO
                     ) -> list[CountResult]:

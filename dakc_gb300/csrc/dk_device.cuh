@@ -179,6 +179,17 @@ __device__ inline void block_bitonic(unsigned long long* s, uint32_t m) {
 }
 
 // ------------------------------------------------ TMA bulk copy + mbarrier
+// Asynchronous L2 prefetch of the 16-byte-aligned interior of [p, p + bytes):
+// no shared memory, no completion to wait for.
+__device__ __forceinline__ void prefetch_l2_range(const void* p, uint64_t bytes) {
+  const uint64_t a = (reinterpret_cast<uint64_t>(p) + 15) & ~15ull;
+  const uint64_t e = (reinterpret_cast<uint64_t>(p) + bytes) & ~15ull;
+  for (uint64_t x = a; x < e; x += (1u << 20)) {  // pieces of at most 1 MB
+    const uint32_t n = (uint32_t)min(e - x, (uint64_t)(1u << 20));
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(x), "r"(n) : "memory");
+  }
+}
+
 // 1-D bulk copies (cp.async.bulk) global -> shared, completed on an mbarrier.
 // Addresses must be 16-byte aligned and sizes multiples of 16.
 

@@ -20,6 +20,7 @@
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 namespace dk {
@@ -248,6 +249,21 @@ int Engine::release_table(uint64_t id) {
   return DK_ERR_NOT_FOUND;
 }
 
+// Level-1 split bits for a count of at most n_upper k-mers: one scatter pass
+// when 2^12 buckets reach the bin target, else the fan-out split evenly
+// between level 1 and the first partition level.
+static int l1_bits_for(uint64_t n_upper, double target) {
+  if ((double)n_upper / 4096.0 <= target) return ceil_log2((uint64_t)((double)n_upper / target) + 1);
+  const int total = ceil_log2((uint64_t)((double)n_upper / target) + 1);
+  return (total + 1) / 2;
+}
+
+static int floor_log2_int(int v) {
+  int b = 0;
+  while ((2 << b) <= v) ++b;
+  return b;
+}
+
 // ------------------------------------------------------------ batch mode
 int JobSet::upload_bounds(Engine* e) {
   const size_t n = (size_t)njobs;
@@ -255,6 +271,10 @@ int JobSet::upload_bounds(Engine* e) {
   DK_CUDA(cudaMemcpyAsync(d_start, job_start.data(), (n + 1) * 8, cudaMemcpyHostToDevice, e->stream));
   DK_CUDA(cudaMemcpyAsync(d_end, job_end.data(), n * 8, cudaMemcpyHostToDevice, e->stream));
   DK_CUDA(cudaMemcpyAsync(d_nul, nul.data(), n * 8, cudaMemcpyHostToDevice, e->stream));
+  DK_CUDA(cudaMemcpyAsync(d_base, job_base.data(), (n + 1) * 4, cudaMemcpyHostToDevice, e->stream));
+  DK_CUDA(cudaMemcpyAsync(d_bits, job_bits.data(), n, cudaMemcpyHostToDevice, e->stream));
+  DK_CUDA(cudaMemcpyAsync(d_bshift, bucket_shift.data(), bucket_shift.size() * 2,
+                          cudaMemcpyHostToDevice, e->stream));
   DK_CUDA(cudaStreamSynchronize(e->stream));  // host vectors are pageable and short-lived
   return DK_OK;
 }
@@ -303,12 +323,13 @@ int Engine::count_batch(const dk_job* jobs, int njobs, const dk_input_desc* desc
   stats_batch = dk_stats();
   double ms_device = 0, ms_h2d = 0, ms_d2h = 0;
   uint64_t launches_total = 0;
+  const int max_wave_jobs = l1_max_buckets(W, true);  // every job needs one bucket at least
   int j0 = 0;
   while (j0 < njobs) {
     // greedy wave: consecutive jobs while they fit the budget and the bucket limit
     int j1 = j0;
     uint64_t bytes = 0;
-    while (j1 < njobs && j1 - j0 < (1 << kMaxL1Bits) && (j1 == j0 || bytes + est(j1) <= wave_cap)) {
+    while (j1 < njobs && j1 - j0 < max_wave_jobs && (j1 == j0 || bytes + est(j1) <= wave_cap)) {
       bytes += est(j1);
       ++j1;
     }
@@ -324,16 +345,50 @@ int Engine::count_batch(const dk_job* jobs, int njobs, const dk_input_desc* desc
     js.job_end.assign(js.job_start.begin() + 1, js.job_start.end());
     const uint64_t total_lines = js.job_start[nj];
     const uint64_t wave_bytes = total_lines * stride;
+    // level-1 buckets per job: the plain count's split, capped so the wave's
+    // buckets fit the scatter kernel (largest jobs give up bits first)
+    {
+      const int max_f1 = l1_max_buckets(W, true);
+      const double target = (double)((desc->bin_target > 0)
+                                         ? std::min(desc->bin_target, kBinCap / 2) : kBinCap / 2);
+      std::vector<int> want(nj);
+      for (int j = 0; j < nj; ++j) {
+        int b = desc->l1_bits > 0 ? desc->l1_bits : l1_bits_for(lines[j0 + j] * per_line, target);
+        want[j] = std::max(0, std::min({b, kMaxL1Bits, 2 * k}));
+      }
+      int cap = floor_log2_int(max_f1);
+      for (;; --cap) {
+        uint64_t tot = 0;
+        for (int j = 0; j < nj; ++j) tot += 1ull << std::min(want[j], cap);
+        if (tot <= (uint64_t)max_f1 || cap == 0) break;
+      }
+      js.job_bits.resize(nj);
+      js.job_base.assign(nj + 1, 0);
+      for (int j = 0; j < nj; ++j) {
+        js.job_bits[j] = (uint8_t)std::min(want[j], cap);
+        js.job_base[j + 1] = js.job_base[j] + (1u << js.job_bits[j]);
+      }
+      js.bucket_shift.resize(js.job_base[nj]);
+      for (int j = 0; j < nj; ++j)
+        for (uint32_t b = js.job_base[j]; b < js.job_base[j + 1]; ++b)
+          js.bucket_shift[b] = (int16_t)(2 * k - js.job_bits[j]);
+    }
+    const int F1 = js.F1();
     DK_TRY(Arena::ensure(this, text, wave_bytes + 64));
-    DK_TRY(Arena::ensure(this, jobmeta, (size_t)(3 * nj + 1) * 8));
+    DK_TRY(Arena::ensure(this, jobmeta, (size_t)(3 * nj + 1) * 8 + (size_t)(nj + 1) * 4 + nj +
+                                            (size_t)F1 * 2 + 64));
     js.d_start = (uint64_t*)jobmeta.p;
     js.d_end = js.d_start + nj + 1;
     js.d_nul = (unsigned long long*)(js.d_end + nj);
+    js.d_base = (uint32_t*)(js.d_nul + nj);
+    js.d_bshift = (int16_t*)(js.d_base + nj + 1);
+    js.d_bits = (uint8_t*)(js.d_bshift + F1);
     DK_CUDA(cudaEventRecord(ev_h2d0, stream));
+    std::vector<Seg> segs;
     for (int j = 0; j < nj; ++j)
       if (jobs[j0 + j].nbytes)
-        DK_TRY(upload(jobs[j0 + j].text, jobs[j0 + j].nbytes,
-                      (uint8_t*)text.p + js.job_start[j] * stride));
+        segs.push_back(Seg{jobs[j0 + j].text, jobs[j0 + j].nbytes, js.job_start[j] * stride});
+    DK_TRY(upload_segments(segs, (uint8_t*)text.p));
     TableBuf* dev_tb = nullptr;
     DK_TRY(acquire_table(total_lines * per_line, true, &dev_tb));
     out_k = (uint64_t*)dev_tb->k;
@@ -369,11 +424,18 @@ int Engine::count_batch(const dk_job* jobs, int njobs, const dk_input_desc* desc
     for (int j = 0; j < nj; ++j) {
       dk_table& t = outs[j0 + j];
       const bool has = !js.nodes.empty();
-      const uint64_t d = has ? js.nodes[j].d : 0, off = has ? js.nodes[j].out_off : 0;
+      uint64_t d = 0, n = 0, off = 0;
+      if (has) {  // a job's buckets are consecutive in key order: its table is one run
+        off = js.nodes[js.job_base[j]].out_off;
+        for (uint32_t b = js.job_base[j]; b < js.job_base[j + 1]; ++b) {
+          d += js.nodes[b].d;
+          n += js.nodes[b].n;
+        }
+      }
       t.kmers = (uint64_t*)h_tb->k + off;
       t.counts = (uint32_t*)h_tb->c + off;
       t.n = d;
-      t.n_kmers = has ? js.nodes[j].n : 0;
+      t.n_kmers = n;
       t.on_device = 0;
       t.variant_used = stats.variant_used;
       t.handle = h_tb->id;
@@ -394,36 +456,84 @@ int Engine::count_batch(const dk_job* jobs, int njobs, const dk_input_desc* desc
 // Copy host reads into device memory: one async copy when the buffer is
 // pinned, else through two pinned staging slots so host memcpy overlaps the
 // previous slot's DMA.
-int Engine::upload(const char* h, uint64_t nbytes, uint8_t* d) {
-  Engine* e = this;
+static bool is_pinned(const void* h) {
   cudaPointerAttributes at;
   bool pinned = false;
-  if (cudaPointerGetAttributes(&at, h) == cudaSuccess)
-    pinned = (at.type == cudaMemoryTypeHost);
+  if (cudaPointerGetAttributes(&at, h) == cudaSuccess) pinned = (at.type == cudaMemoryTypeHost);
   cudaGetLastError();
-  if (pinned) {
-    DK_CUDA(cudaMemcpyAsync(d, h, nbytes, cudaMemcpyHostToDevice, stream));
-    return DK_OK;
+  return pinned;
+}
+
+// Copy [dst_lo, dst_hi) of the concatenated destination layout out of the
+// segments that cover it (segments sorted by destination offset).
+static void gather_range(const std::vector<Engine::Seg>& segs, uint64_t dst_lo, uint64_t dst_hi,
+                         uint8_t* out, uint64_t out_base) {
+  size_t a = 0, b = segs.size();
+  while (b - a > 1) {  // last segment starting at or before dst_lo
+    const size_t m = (a + b) / 2;
+    if (segs[m].doff <= dst_lo) a = m; else b = m;
   }
+  for (size_t i = a; i < segs.size() && segs[i].doff < dst_hi; ++i) {
+    const uint64_t s0 = std::max(dst_lo, segs[i].doff);
+    const uint64_t s1 = std::min(dst_hi, segs[i].doff + segs[i].n);
+    if (s1 > s0) std::memcpy(out + (s0 - out_base), segs[i].h + (s0 - segs[i].doff), s1 - s0);
+  }
+}
+
+// Host -> device copy of segments laid out at segs[i].doff in d.  Pinned
+// segments go straight to the DMA engine; pageable ones are packed into two
+// 64 MB pinned slots by several host threads while the other slot's DMA runs.
+// A slot is refilled only after the copy that last read it has finished.
+int Engine::upload_segments(const std::vector<Seg>& all, uint8_t* d) {
+  Engine* e = this;
+  std::vector<Seg> segs;
+  for (const Seg& sg : all) {
+    if (!sg.n) continue;
+    if (is_pinned(sg.h)) {
+      DK_CUDA(cudaMemcpyAsync(d + sg.doff, sg.h, sg.n, cudaMemcpyHostToDevice, stream));
+    } else {
+      segs.push_back(sg);
+    }
+  }
+  if (segs.empty()) return DK_OK;
+  std::sort(segs.begin(), segs.end(), [](const Seg& x, const Seg& y) { return x.doff < y.doff; });
   const size_t slot = 64ull << 20;
   for (int i = 0; i < 2; ++i) {
     if (!stage_pinned[i]) DK_CUDA(cudaMallocHost(&stage_pinned[i], slot));
     if (!stage_ev[i]) DK_CUDA(cudaEventCreateWithFlags(&stage_ev[i], cudaEventDisableTiming));
   }
-  // a slot is refilled only after the copy that last read it has finished,
-  // also across calls (batches upload job after job)
-  uint64_t off = 0;
-  while (off < nbytes) {
+  const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+  const int nthreads = (int)std::min<unsigned>(8, std::max(1u, hw / 2));
+  uint64_t lo = segs.front().doff;
+  const uint64_t end = segs.back().doff + segs.back().n;
+  while (lo < end) {
     const int i = stage_next;
-    const size_t len = (size_t)std::min<uint64_t>(slot, nbytes - off);
+    const uint64_t hi = std::min<uint64_t>(end, lo + slot);
     DK_CUDA(cudaEventSynchronize(stage_ev[i]));
-    std::memcpy(stage_pinned[i], h + off, len);
-    DK_CUDA(cudaMemcpyAsync(d + off, stage_pinned[i], len, cudaMemcpyHostToDevice, stream));
+    uint8_t* buf = (uint8_t*)stage_pinned[i];
+    const uint64_t len = hi - lo;
+    if (len < (4u << 20) || nthreads == 1) {
+      gather_range(segs, lo, hi, buf, lo);
+    } else {
+      std::vector<std::thread> th;
+      const uint64_t chunk = (len + nthreads - 1) / nthreads;
+      for (int t = 0; t < nthreads; ++t) {
+        const uint64_t a = lo + (uint64_t)t * chunk, b = std::min(hi, a + chunk);
+        if (a >= b) break;
+        th.emplace_back([&segs, a, b, buf, lo] { gather_range(segs, a, b, buf, lo); });
+      }
+      for (auto& t : th) t.join();
+    }
+    DK_CUDA(cudaMemcpyAsync(d + lo, buf, len, cudaMemcpyHostToDevice, stream));
     DK_CUDA(cudaEventRecord(stage_ev[i], stream));
-    off += len;
+    lo = hi;
     stage_next ^= 1;
   }
   return DK_OK;
+}
+
+int Engine::upload(const char* h, uint64_t nbytes, uint8_t* d) {
+  return upload_segments({Seg{h, nbytes, 0}}, d);
 }
 
 // The device pipeline: reads at d_text (nbytes, padded by >= 64 bytes of
@@ -463,16 +573,14 @@ int Engine::count_device(const uint8_t* d_text, uint64_t nbytes, const dk_input_
   // level-1 fan-out: aim at ~kBinCap/2 keys per final bin after at most one
   // 8-bit partition level
   const uint64_t n_upper = L * per_line;
-  const double target = 0.5 * kBinCap;
-  int B1;
-  if ((double)n_upper / 4096.0 <= target)
-    B1 = ceil_log2((uint64_t)((double)n_upper / target) + 1);
-  else
-    B1 = ceil_log2((uint64_t)((double)n_upper / (target * kFanout)) + 1);
-  B1 = std::max(1, std::min(B1, kMaxL1Bits));
+  const int bin_target =
+      (desc.bin_target > 0) ? std::min(desc.bin_target, kBinCap / 2) : kBinCap / 2;
+  const double target = (double)bin_target;
+  int B1 = desc.l1_bits > 0 ? desc.l1_bits : l1_bits_for(n_upper, target);
+  B1 = std::max(1, std::min({B1, kMaxL1Bits, floor_log2_int(l1_max_buckets(W, false))}));
   B1 = std::min(B1, 2 * k);
-  // batch mode: one level-1 bucket per job, all 2k bits still free
-  const int F1 = js ? js->njobs : (1 << B1);
+  // batch mode: each job owns its own run of level-1 buckets (JobSet)
+  const int F1 = js ? js->F1() : (1 << B1);
   const int shift1 = js ? 2 * k : 2 * k - B1;
   const int G = 2 * sm_count;
 
@@ -488,6 +596,8 @@ int Engine::count_device(const uint8_t* d_text, uint64_t nbytes, const dk_input_
   a.job_start = js ? js->d_start : nullptr;
   a.job_end = js ? js->d_end : nullptr;
   a.job_nul = js ? js->d_nul : nullptr;
+  a.job_base = js ? js->d_base : nullptr;
+  a.job_bits = js ? js->d_bits : nullptr;
 
   DK_TRY(Arena::ensure(this, H, (size_t)G * F1 * 4));
   DK_TRY(Arena::ensure(this, O, (size_t)G * F1 * 8));
@@ -530,7 +640,8 @@ int Engine::count_device(const uint8_t* d_text, uint64_t nbytes, const dk_input_
   // level-1 nodes and offsets
   node_cap_needed = (size_t)F1;
   DK_TRY(Arena::ensure(this, nodes, node_cap_needed * sizeof(Node)));
-  TIMED(7, launch_l1_scan((uint32_t*)H.p, G, F1, (uint64_t*)O.p, (Node*)nodes.p, shift1, stream));
+  TIMED(7, launch_l1_scan((uint32_t*)H.p, G, F1, (uint64_t*)O.p, (Node*)nodes.p, shift1,
+                          js ? js->d_bshift : nullptr, stream));
   DK_TRY(Arena::ensure(this, keysA, n_kmers * 8));
   DK_TRY(Arena::ensure(this, keysB, n_kmers * 8));
   DK_TRY(Arena::ensure(this, cnt, n_kmers * 4));
@@ -544,9 +655,9 @@ int Engine::count_device(const uint8_t* d_text, uint64_t nbytes, const dk_input_
   for (int lvl = 0; lvl < 16; ++lvl) {
     levels.emplace_back(lo, hi);
     // the final list can grow by at most this level's node count
-    uint32_t hc[8];
-    DK_TRY(sync_read(lc, 32, hc));
-    const uint32_t n_final_so_far = hc[0];
+    LevelCounters lv;
+    DK_TRY(sync_read(lc, sizeof(LevelCounters), &lv));
+    const uint32_t n_final_so_far = lv.n_final;
     {
       // finals must hold n_final_so_far + (hi - lo)
       DevBuf& f = finals;
@@ -560,20 +671,18 @@ int Engine::count_device(const uint8_t* d_text, uint64_t nbytes, const dk_input_
         f = nb;
       }
     }
-    DK_CUDA(cudaMemsetAsync((char*)lc + 4, 0, 28, stream));  // keep n_final
-    TIMED(7, launch_classify((Node*)nodes.p, lo, hi, (uint32_t*)finals.p, lc, kBinCap, stream));
-    DK_TRY(sync_read(lc, 32, hc));
-    const uint32_t n_split = hc[1], n_tiles = hc[2];
-    if (hc[3]) {
+    DK_CUDA(cudaMemsetAsync((char*)lc + 4, 0, sizeof(LevelCounters) - 4, stream));  // keep n_final
+    TIMED(7, launch_classify((Node*)nodes.p, lo, hi, (uint32_t*)finals.p, lc, kBinCap,
+                             2 * bin_target, stream));
+    DK_TRY(sync_read(lc, sizeof(LevelCounters), &lv));
+    if (lv.too_big) {
       set_error("a partition node holds >= 2^32 keys");
       return DK_ERR_INVALID_ARG;
     }
-    if (n_split == 0) break;
-    uint64_t split_keys = 0;
-    std::memcpy(&split_keys, &hc[6], 8);
-    stats.n_partitioned += split_keys;
+    if (lv.n_split == 0) break;
+    stats.n_partitioned += lv.split_keys;
     // grow node storage for the children (copying existing nodes)
-    const size_t need_nodes = (size_t)hi + (size_t)n_split * kFanout;
+    const size_t need_nodes = (size_t)hi + (size_t)lv.n_children;
     if (nodes.cap < need_nodes * sizeof(Node)) {
       DevBuf nb;
       DK_TRY(Arena::ensure(this, nb, need_nodes * sizeof(Node)));
@@ -581,22 +690,23 @@ int Engine::count_device(const uint8_t* d_text, uint64_t nbytes, const dk_input_
       Arena::release(this, nodes);
       nodes = nb;
     }
+    const uint32_t n_tiles = lv.n_tiles;
     DK_TRY(Arena::ensure(this, tiles, (size_t)n_tiles * sizeof(Tile)));
-    DK_TRY(Arena::ensure(this, TH, (size_t)n_tiles * kFanout * 4));
+    DK_TRY(Arena::ensure(this, TH, (size_t)lv.th_entries * 4));
     TIMED(7, launch_assign((Node*)nodes.p, lo, hi, hi, (Tile*)tiles.p, lc, stream));
     TIMED(2, launch_tile_hist((Node*)nodes.p, (Tile*)tiles.p, n_tiles, (uint64_t*)keysA.p,
                               (uint64_t*)keysB.p, (uint32_t*)TH.p, stream));
     TIMED(7, launch_node_scan((Node*)nodes.p, lo, hi, (Tile*)tiles.p, (uint32_t*)TH.p, stream));
     TIMED(3, launch_tile_scatter((Node*)nodes.p, (Tile*)tiles.p, n_tiles, (uint64_t*)keysA.p,
-                                 (uint64_t*)keysB.p, (uint32_t*)TH.p, stream));
+                                 (uint64_t*)keysB.p, (uint32_t*)TH.p, (int)lv.max_width, stream));
     lo = hi;
-    hi = hi + n_split * kFanout;
+    hi = hi + lv.n_children;
   }
   stats.partition_levels = (int)levels.size();
   DK_CUDA(cudaEventRecord(ev_stage[3], stream));
-  uint32_t hc[8];
-  DK_TRY(sync_read(lc, 32, hc));
-  const uint32_t n_final = hc[0];
+  LevelCounters lvf;
+  DK_TRY(sync_read(lc, sizeof(LevelCounters), &lvf));
+  const uint32_t n_final = lvf.n_final;
   stats.n_bins = n_final;
   TIMED(4, launch_bin_count((Node*)nodes.p, (uint32_t*)finals.p, n_final, (uint64_t*)keysA.p,
                             (uint64_t*)keysB.p, (uint32_t*)cnt.p, use_hash ? 1 : 0, c64, sm_count,

@@ -56,6 +56,15 @@ struct JobSet {
   uint64_t* d_start = nullptr;      // device mirrors (inside the engine's job arena)
   uint64_t* d_end = nullptr;
   unsigned long long* d_nul = nullptr;
+  // level-1 buckets: job j owns [job_base[j], job_base[j+1]), 2^job_bits[j] of them,
+  // split by the top job_bits[j] bits of its k-mers
+  std::vector<uint32_t> job_base;   // njobs + 1
+  std::vector<uint8_t> job_bits;    // njobs
+  std::vector<int16_t> bucket_shift;  // F1: free key bits below each bucket's prefix
+  uint32_t* d_base = nullptr;
+  uint8_t* d_bits = nullptr;
+  int16_t* d_bshift = nullptr;
+  int F1() const { return job_base.empty() ? njobs : (int)job_base.back(); }
   std::vector<Node> nodes;          // level-1 nodes read back after the count
   int upload_bounds(Engine* e);     // job_end -> device, job_nul reset
   int apply_nul(Engine* e);         // shorten job_end to each job's first NUL-led line
@@ -101,7 +110,13 @@ struct Engine {
   ~Engine();
   void set_error(const std::string& m);
   int sync_read(const void* dsrc, size_t bytes, void* hdst);
+  struct Seg {
+    const char* h;
+    uint64_t n;
+    uint64_t doff;  // destination offset
+  };
   int upload(const char* h, uint64_t nbytes, uint8_t* d);
+  int upload_segments(const std::vector<Seg>& segs, uint8_t* d);
   int acquire_table(uint64_t n, bool on_device, TableBuf** out);
   int release_table(uint64_t id);
   int count_device(const uint8_t* d_text, uint64_t nbytes, const dk_input_desc& desc,

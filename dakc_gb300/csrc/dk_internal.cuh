@@ -16,41 +16,53 @@ struct Node {
   uint64_t n;
   uint64_t d;        // distinct keys in the subtree (filled bottom-up)
   uint64_t out_off;  // output offset of the subtree's first distinct key
-  uint32_t first_child;  // valid when split
+  uint32_t first_child;  // valid when split: 2^width children from here
   int16_t shift;     // remaining low bits not fixed by the path to this node
   uint8_t buf;
-  uint8_t state;     // NODE_FINAL or NODE_SPLIT
+  uint8_t state;     // NODE_FINAL / NODE_SPLIT / NODE_EMPTY
   uint32_t tile_base;  // first partition tile (split nodes)
   uint32_t ntiles;
+  uint64_t th_base;  // first tile-histogram entry (rows of 2^width per tile)
+  uint8_t width;     // digit bits this node is split on (split nodes)
+  uint8_t pad[7];
 };
+static_assert(sizeof(Node) == 64, "Node layout");
 enum : uint8_t { NODE_FINAL = 1, NODE_SPLIT = 2, NODE_EMPTY = 3 };
 
 struct Tile {  // a slice of a split node's keys, partitioned by one CTA
   uint64_t start;
   uint32_t n;
   uint32_t node;  // global node index
+  uint64_t th;    // first entry of this tile's histogram row
 };
 
 // counters written by the classify / assign kernels.  n_final accumulates over
-// all levels; the others are per level.
+// all levels; the others are per level (zeroed from byte 4 on).
 struct LevelCounters {
   uint32_t n_final;
   uint32_t n_split;
   uint32_t n_tiles;
-  uint32_t too_big;  // a split node holds >= 2^32 keys
-  uint32_t n_children;
-  uint32_t n_tiles_assigned;
+  uint32_t too_big;      // a split node holds >= 2^32 keys
+  uint32_t n_children;   // sum of 2^width over split nodes
+  uint32_t max_width;
   unsigned long long split_keys;  // keys held by this level's split nodes
+  unsigned long long th_entries;  // sum of ntiles * 2^width
+  uint32_t n_tiles_assigned;
+  uint32_t n_children_assigned;
+  unsigned long long th_assigned;
+  uint32_t pad[2];
 };
-static_assert(sizeof(LevelCounters) == 32, "LevelCounters is read back as 32 bytes");
+static_assert(sizeof(LevelCounters) == 64, "LevelCounters is read back as 64 bytes");
 
-constexpr int kDigitBits = 8;           // fan-out of partition levels 2+
+constexpr int kDigitBits = 8;           // typical partition fan-out (level-1 sizing)
 constexpr int kFanout = 1 << kDigitBits;
+constexpr int kMaxSplitBits = 12;       // widest per-node split (4096 children)
 constexpr int kTileKeys = 8192;         // keys per partition tile
 constexpr int kBinCap = 12000;          // keys a bin-count CTA sorts in shared memory
 constexpr int kDenseBits = 12;          // nodes with <= this many free bits are counted densely
 constexpr int kBinThreads = 512;
 constexpr int kMaxL1Bits = 12;          // level-1 fan-out <= 4096 buckets
+constexpr size_t kMaxSmemPerBlock = 232448;  // opt-in shared memory per block (sm_100 family)
 
 struct ExtractArgs {
   const uint8_t* text;  // device text, 16-byte aligned
@@ -70,18 +82,27 @@ struct ExtractArgs {
   const uint64_t* job_start;
   const uint64_t* job_end;
   unsigned long long* job_nul;
+  // job j owns level-1 buckets [job_base[j], job_base[j] + 2^job_bits[j]): a
+  // k-mer of job j goes to job_base[j] + (key >> (2k - job_bits[j]))
+  const uint32_t* job_base;
+  const uint8_t* job_bits;
 };
 
 // ---- launchers (dk_kernels.cu); every launcher returns the number of kernel
 // launches it issued (for the launch count reported in stats)
 int launch_l1_count(const ExtractArgs& a, int grid, uint32_t* H, unsigned long long* n_kmers,
                     cudaStream_t s);
+// bucket_shift (optional, F1 entries): per-bucket free bits in batch mode
 int launch_l1_scan(const uint32_t* H, int grid, int F1, uint64_t* O, Node* nodes, int shift1,
-                   cudaStream_t s);
+                   const int16_t* bucket_shift, cudaStream_t s);
+// largest level-1 fan-out (power of two <= 2^kMaxL1Bits) whose scatter kernel
+// fits the per-block shared-memory limit for line width W
+int l1_max_buckets(int W, bool jobs);
 int launch_l1_scatter(const ExtractArgs& a, int grid, const uint64_t* O, uint64_t* keys,
                       unsigned long long* counters, cudaStream_t s);
+// split nodes get a digit width that makes their children ~split_target/2 keys
 int launch_classify(Node* nodes, uint32_t node_lo, uint32_t node_hi, uint32_t* final_list,
-                    LevelCounters* ctr, int bin_cap, cudaStream_t s);
+                    LevelCounters* ctr, int bin_cap, int split_target, cudaStream_t s);
 int launch_assign(Node* nodes, uint32_t node_lo, uint32_t node_hi, uint32_t child_base,
                   Tile* tiles, LevelCounters* ctr, cudaStream_t s);
 int launch_tile_hist(const Node* nodes, const Tile* tiles, uint32_t n_tiles,
@@ -89,7 +110,7 @@ int launch_tile_hist(const Node* nodes, const Tile* tiles, uint32_t n_tiles,
 int launch_node_scan(Node* nodes, uint32_t node_lo, uint32_t node_hi, const Tile* tiles,
                      uint32_t* TH, cudaStream_t s);
 int launch_tile_scatter(const Node* nodes, const Tile* tiles, uint32_t n_tiles, uint64_t* A,
-                        uint64_t* B, const uint32_t* TH, cudaStream_t s);
+                        uint64_t* B, const uint32_t* TH, int max_width, cudaStream_t s);
 // ctr: [4] (low 32 bits) = bin ticket, [5] = count overflow flag, [6] = hash bins that fell
 // back to sorting (all zeroed by the caller); use_hash selects the hash-first bin count
 int launch_bin_count(Node* nodes, const uint32_t* final_list, uint32_t n_final, uint64_t* A,

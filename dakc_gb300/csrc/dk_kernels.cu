@@ -127,6 +127,22 @@ __host__ __device__ inline uint32_t tile_buf_bytes(uint32_t lt, uint64_t stride)
   return (uint32_t)(((uint64_t)lt * stride + 32 + 127) & ~127ull);
 }
 
+// level-1 bucket rule of one job in batch mode: bucket = base + (key >> shift),
+// shift = 64 (no split) when the job has a single bucket
+struct JobBucket {
+  uint32_t base = 0;
+  uint32_t shift = 64;
+  JobBucket() = default;
+  __device__ __forceinline__ JobBucket(const ExtractArgs& a, uint32_t job) {
+    const uint32_t bits = __ldg(a.job_bits + job);
+    base = __ldg(a.job_base + job);
+    shift = bits ? 2u * (uint32_t)a.k - bits : 64u;
+  }
+  __device__ __forceinline__ uint32_t operator()(uint64_t key) const {
+    return base + (shift < 64 ? (uint32_t)(key >> shift) : 0u);
+  }
+};
+
 // job that owns line l in batch mode (binary search over job_start)
 __device__ __forceinline__ uint32_t job_of_line(const ExtractArgs& a, uint64_t l) {
   uint32_t lo = 0, hi = (uint32_t)a.njobs;
@@ -188,8 +204,9 @@ __global__ void __launch_bounds__(512) k_l1_count(ExtractArgs a, uint32_t* __res
           atomicMin(&a.job_nul[job], (unsigned long long)l);
           atomicMax(&counters[1], 1ull);
         }
-        warp_line_kmers<C>(line, a.W, a.k, a.kmask, lut, [&](int, uint64_t, bool valid) {
-          if (valid) { atomicAdd(&hist[job], 1u); ++mine; }
+        const JobBucket jb(a, job);
+        warp_line_kmers<C>(line, a.W, a.k, a.kmask, lut, [&](int, uint64_t key, bool valid) {
+          if (valid) { atomicAdd(&hist[jb(key)], 1u); ++mine; }
         });
         continue;
       }
@@ -218,7 +235,7 @@ __global__ void k_l1_totals(const uint32_t* __restrict__ H, int G, int F1, Node*
 }
 
 // bucket starts (single block): exclusive scan of totals, node init
-__global__ void k_l1_starts(Node* nodes, int F1, int shift1) {
+__global__ void k_l1_starts(Node* nodes, int F1, int shift1, const int16_t* bucket_shift) {
   __shared__ unsigned long long tmp[32];
   const int per = (F1 + blockDim.x - 1) / blockDim.x;
   const int lo = min(F1, (int)threadIdx.x * per), hi = min(F1, lo + per);
@@ -232,11 +249,13 @@ __global__ void k_l1_starts(Node* nodes, int F1, int shift1) {
     nd.d = 0;
     nd.out_off = 0;
     nd.first_child = 0;
-    nd.shift = (int16_t)shift1;
+    nd.shift = bucket_shift ? bucket_shift[i] : (int16_t)shift1;
     nd.buf = 0;
     nd.state = 0;
     nd.tile_base = 0;
     nd.ntiles = 0;
+    nd.th_base = 0;
+    nd.width = 0;
   }
 }
 
@@ -271,6 +290,7 @@ __global__ void __launch_bounds__(512, 2) k_l1_scatter(ExtractArgs a, const uint
   uint32_t* tile_off = tile_hist + F1;                                    // F1
   uint32_t* tmp = tile_off + F1;                                          // 32
   uint8_t* lut = reinterpret_cast<uint8_t*>(tmp + 32);                    // 256
+  uint16_t* staged_b = reinterpret_cast<uint16_t*>(lut + 256);            // stage_cap (batch mode)
   TextTiles T;
   T.text = a.text;
   T.nbytes = a.nbytes;
@@ -305,7 +325,7 @@ __global__ void __launch_bounds__(512, 2) k_l1_scatter(ExtractArgs a, const uint
     T.range(ti, &t0, &t1);
     uint64_t kr[LPW][C];
     uint32_t sr[LPW][C];
-    uint32_t jr[LPW];
+    JobBucket jbr[LPW];  // batch mode: bucket rule of each line's job
 #pragma unroll
     for (int j = 0; j < LPW; ++j) {
       const uint64_t l = t0 + (uint64_t)j * nwarps + warp;
@@ -316,13 +336,15 @@ __global__ void __launch_bounds__(512, 2) k_l1_scatter(ExtractArgs a, const uint
         live = l < __ldg(a.job_end + job);
       }
       if (live) {
+        if (a.njobs) jbr[j] = JobBucket(a, job);
+        const JobBucket jb = jbr[j];
         warp_line_kmers<C>(base + (l - t0) * stride, a.W, a.k, a.kmask, lut,
                            [&](int t, uint64_t key, bool valid) {
                              kr[j][t] = key;
-                             const uint32_t bkt = a.njobs ? job : (uint32_t)(key >> a.shift1);
+                             const uint32_t bkt =
+                                 a.njobs ? jb(key) : (uint32_t)(key >> a.shift1);
                              sr[j][t] = valid ? atomicAdd(&tile_hist[bkt], 1u) : 0xFFFFFFFFu;
                            });
-        jr[j] = job;
       } else {
 #pragma unroll
         for (int t = 0; t < C; ++t) { kr[j][t] = 0; sr[j][t] = 0xFFFFFFFFu; }
@@ -337,20 +359,16 @@ __global__ void __launch_bounds__(512, 2) k_l1_scatter(ExtractArgs a, const uint
 #pragma unroll
       for (int t = 0; t < C; ++t)
         if (sr[j][t] != 0xFFFFFFFFu) {
-          const uint32_t bkt = a.njobs ? jr[j] : (uint32_t)(kr[j][t] >> a.shift1);
+          const uint32_t bkt = a.njobs ? jbr[j](kr[j][t]) : (uint32_t)(kr[j][t] >> a.shift1);
           staging[tile_off[bkt] + sr[j][t]] = kr[j][t];
+          if (a.njobs) staged_b[tile_off[bkt] + sr[j][t]] = (uint16_t)bkt;
         }
     __syncthreads();
     if (a.njobs) {
-      // batch mode: a staged key's bucket is the job whose run contains it
+      // batch mode: the bucket was staged with the key
       for (uint32_t i = threadIdx.x; i < Tn; i += blockDim.x) {
-        // the largest bucket whose run starts at or before i is the one that holds i
-        uint32_t lo = 0, hi = (uint32_t)F1;
-        while (hi - lo > 1) {
-          const uint32_t mid = (lo + hi) >> 1;
-          if (tile_off[mid] <= i) lo = mid; else hi = mid;
-        }
-        keys_out[cursor[lo] + (i - tile_off[lo])] = staging[i];
+        const uint32_t b = staged_b[i];
+        keys_out[cursor[b] + (i - tile_off[b])] = staging[i];
       }
     } else {
       for (uint32_t i = threadIdx.x; i < Tn; i += blockDim.x) {
@@ -369,9 +387,13 @@ __global__ void __launch_bounds__(512, 2) k_l1_scatter(ExtractArgs a, const uint
 }
 
 // ---------------------------------------------------- partition levels
-// Mark each node of the level final / split / empty; count splits and tiles.
+// A split node is split on its next `width` bits, width chosen so that the
+// children average about half a bin: wide for big nodes, narrow for small.
+
+// Mark each node of the level final / split / empty; count what the split
+// nodes need (children, tiles, histogram entries).
 __global__ void k_classify(Node* nodes, uint32_t lo, uint32_t hi, uint32_t* final_list,
-                           LevelCounters* ctr, int bin_cap) {
+                           LevelCounters* ctr, int bin_cap, int split_target) {
   const uint32_t i = lo + blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= hi) return;
   const Node nd = nodes[i];
@@ -385,107 +407,145 @@ __global__ void k_classify(Node* nodes, uint32_t lo, uint32_t hi, uint32_t* fina
     final_list[atomicAdd(&ctr->n_final, 1u)] = i;
     return;
   }
+  const uint64_t target = (uint64_t)max(1, split_target / 2);  // children ~ target keys
+  int w = ceil_log2_u64((nd.n + target - 1) / target);
+  w = max(1, min(w, kMaxSplitBits));
+  const uint32_t nt = (uint32_t)((nd.n + kTileKeys - 1) / kTileKeys);
   nodes[i].state = NODE_SPLIT;
+  nodes[i].width = (uint8_t)w;
   atomicAdd(&ctr->n_split, 1u);
   atomicAdd(&ctr->split_keys, (unsigned long long)nd.n);
-  atomicAdd(&ctr->n_tiles, (uint32_t)((nd.n + kTileKeys - 1) / kTileKeys));
+  atomicAdd(&ctr->n_tiles, nt);
+  atomicAdd(&ctr->n_children, 1u << w);
+  atomicAdd(&ctr->th_entries, (unsigned long long)nt << w);
+  atomicMax(&ctr->max_width, (uint32_t)w);
   if (nd.n >= (1ull << 32)) atomicOr(&ctr->too_big, 1u);
 }
 
-// Give each split node its children block and its partition tiles (buffers
-// sized by the host from k_classify's counts).
+// Give each split node its children block, its partition tiles and their
+// histogram rows (buffers sized by the host from k_classify's counts).
 __global__ void k_assign(Node* nodes, uint32_t lo, uint32_t hi, uint32_t child_base, Tile* tiles,
                          LevelCounters* ctr) {
   const uint32_t i = lo + blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= hi) return;
   const Node nd = nodes[i];
   if (nd.state != NODE_SPLIT) return;
+  const uint32_t R = 1u << nd.width;
   const uint32_t nt = (uint32_t)((nd.n + kTileKeys - 1) / kTileKeys);
   const uint32_t tb = atomicAdd(&ctr->n_tiles_assigned, nt);
-  const uint32_t fc = child_base + atomicAdd(&ctr->n_children, (uint32_t)kFanout);
+  const uint32_t fc = child_base + atomicAdd(&ctr->n_children_assigned, R);
+  const unsigned long long thb = atomicAdd(&ctr->th_assigned, (unsigned long long)nt * R);
   nodes[i].first_child = fc;
   nodes[i].tile_base = tb;
   nodes[i].ntiles = nt;
+  nodes[i].th_base = thb;
   for (uint32_t t = 0; t < nt; ++t) {
     Tile tl;
     tl.start = nd.start + (uint64_t)t * kTileKeys;
     tl.n = (uint32_t)min((uint64_t)kTileKeys, nd.n - (uint64_t)t * kTileKeys);
     tl.node = i;
+    tl.th = thb + (uint64_t)t * R;
     tiles[tb + t] = tl;
   }
 }
 
-__device__ __forceinline__ uint32_t digit_of(uint64_t key, int shift) {
-  return (uint32_t)(key >> (shift - kDigitBits)) & (kFanout - 1);
+__device__ __forceinline__ uint32_t digit_of(uint64_t key, int shift, int width) {
+  return (uint32_t)(key >> (shift - width)) & ((1u << width) - 1u);
 }
 
 __global__ void __launch_bounds__(256) k_tile_hist(const Node* nodes, const Tile* tiles,
                                                    const uint64_t* A, const uint64_t* B,
                                                    uint32_t* TH) {
-  __shared__ uint32_t hist[kFanout];
+  __shared__ uint32_t hist[1u << kMaxSplitBits];
   const Tile tl = tiles[blockIdx.x];
   const Node nd = nodes[tl.node];
+  const uint32_t R = 1u << nd.width;
   const uint64_t* src = (nd.buf ? B : A) + tl.start;
-  hist[threadIdx.x] = 0;
+  for (uint32_t j = threadIdx.x; j < R; j += blockDim.x) hist[j] = 0;
   __syncthreads();
-  for (uint32_t i = threadIdx.x; i < tl.n; i += blockDim.x)
-    atomicAdd(&hist[digit_of(__ldg(src + i), nd.shift)], 1u);
+  uint32_t i = threadIdx.x;
+  const uint32_t T = blockDim.x;
+  for (; i + 3 * T < tl.n; i += 4 * T) {
+    const uint64_t k0 = __ldg(src + i), k1 = __ldg(src + i + T), k2 = __ldg(src + i + 2 * T),
+                   k3 = __ldg(src + i + 3 * T);
+    atomicAdd(&hist[digit_of(k0, nd.shift, nd.width)], 1u);
+    atomicAdd(&hist[digit_of(k1, nd.shift, nd.width)], 1u);
+    atomicAdd(&hist[digit_of(k2, nd.shift, nd.width)], 1u);
+    atomicAdd(&hist[digit_of(k3, nd.shift, nd.width)], 1u);
+  }
+  for (; i < tl.n; i += T) atomicAdd(&hist[digit_of(__ldg(src + i), nd.shift, nd.width)], 1u);
   __syncthreads();
-  TH[(size_t)blockIdx.x * kFanout + threadIdx.x] = hist[threadIdx.x];
+  for (uint32_t j = threadIdx.x; j < R; j += blockDim.x) TH[tl.th + j] = hist[j];
 }
 
 // one CTA per node of the level; split nodes turn their tiles' counts into
-// offsets within each child and create the children
+// offsets within each child and create the 2^width children
 __global__ void __launch_bounds__(256) k_node_scan(Node* nodes, uint32_t lo, const Tile* tiles,
                                                    uint32_t* TH) {
+  __shared__ unsigned long long csize[1u << kMaxSplitBits];
   __shared__ unsigned long long tmp[32];
   const uint32_t i = lo + blockIdx.x;
   const Node nd = nodes[i];
   if (nd.state != NODE_SPLIT) return;
-  const int j = threadIdx.x;
-  uint32_t run = 0;
-  for (uint32_t t = 0; t < nd.ntiles; ++t) {
-    uint32_t* p = TH + (size_t)(nd.tile_base + t) * kFanout + j;
-    const uint32_t c = *p;
-    *p = run;
-    run += c;
+  const uint32_t R = 1u << nd.width;
+  for (uint32_t j = threadIdx.x; j < R; j += blockDim.x) {
+    uint32_t run = 0;
+    for (uint32_t t = 0; t < nd.ntiles; ++t) {
+      uint32_t* p = TH + nd.th_base + (uint64_t)t * R + j;
+      const uint32_t c = *p;
+      *p = run;
+      run += c;
+    }
+    csize[j] = run;
   }
-  unsigned long long excl = block_excl_scan<unsigned long long>(run, tmp, nullptr);
-  Node ch;
-  ch.start = nd.start + excl;
-  ch.n = run;
-  ch.d = 0;
-  ch.out_off = 0;
-  ch.first_child = 0;
-  ch.shift = (int16_t)(nd.shift - kDigitBits);
-  ch.buf = (uint8_t)(1 - nd.buf);
-  ch.state = 0;
-  ch.tile_base = 0;
-  ch.ntiles = 0;
-  nodes[nd.first_child + j] = ch;
+  __syncthreads();
+  // child starts: exclusive scan of the child sizes (kept separately: csize
+  // becomes the starts, sizes are re-derived from neighbouring starts)
+  const unsigned long long total = block_scan_array<unsigned long long>(csize, (int)R, tmp);
+  for (uint32_t j = threadIdx.x; j < R; j += blockDim.x) {
+    Node ch;
+    ch.start = nd.start + csize[j];
+    ch.n = (j + 1 < R ? csize[j + 1] : total) - csize[j];
+    ch.d = 0;
+    ch.out_off = 0;
+    ch.first_child = 0;
+    ch.shift = (int16_t)(nd.shift - nd.width);
+    ch.buf = (uint8_t)(1 - nd.buf);
+    ch.state = 0;
+    ch.tile_base = 0;
+    ch.ntiles = 0;
+    ch.th_base = 0;
+    ch.width = 0;
+    nodes[nd.first_child + j] = ch;
+  }
 }
 
-// Partition one tile by the next 8 bits.  Pass 1 ranks every key within its
-// digit (shared atomics); the tile is then laid out digit by digit in shared
-// memory (keys re-read from L2) so each digit's keys leave as one contiguous,
-// coalesced run at the tile's offset inside the child.
+// Partition one tile by the node's next `width` bits.  Pass 1 ranks every key
+// within its digit (shared atomics); the tile is then laid out digit by digit
+// in shared memory (keys re-read from L2) so each digit's keys leave as one
+// contiguous, coalesced run at the tile's offset inside the child.
 constexpr int kTileThreads = 512;
 constexpr int kTileKeysPerThread = kTileKeys / kTileThreads;
 
-__global__ void __launch_bounds__(kTileThreads, 3) k_tile_scatter(const Node* nodes,
+__global__ void __launch_bounds__(kTileThreads, 2) k_tile_scatter(const Node* nodes,
                                                                   const Tile* tiles, uint64_t* A,
                                                                   uint64_t* B,
-                                                                  const uint32_t* TH) {
-  extern __shared__ __align__(16) unsigned long long stage[];  // kTileKeys
-  __shared__ unsigned long long gbase[kFanout];
-  __shared__ uint32_t cnt[kFanout], loc[kFanout];
+                                                                  const uint32_t* TH,
+                                                                  int max_width) {
+  extern __shared__ __align__(16) unsigned long long dsm[];
+  unsigned long long* stage = dsm;                                  // kTileKeys
+  unsigned long long* gbase = stage + kTileKeys;                    // 2^max_width
+  uint32_t* cnt = reinterpret_cast<uint32_t*>(gbase + (1u << max_width));
+  uint32_t* loc = cnt + (1u << max_width);
   __shared__ uint32_t tmp[32];
   const Tile tl = tiles[blockIdx.x];
   const Node nd = nodes[tl.node];
+  const uint32_t R = 1u << nd.width;
+  const int sh = nd.shift, w = nd.width;
   const uint64_t* src = (nd.buf ? B : A) + tl.start;
   uint64_t* dst = nd.buf ? A : B;
-  for (uint32_t j = threadIdx.x; j < kFanout; j += blockDim.x) {
-    gbase[j] = nodes[nd.first_child + j].start + TH[(size_t)blockIdx.x * kFanout + j];
+  for (uint32_t j = threadIdx.x; j < R; j += blockDim.x) {
+    gbase[j] = nodes[nd.first_child + j].start + TH[tl.th + j];
     cnt[j] = 0;
   }
   __syncthreads();
@@ -493,29 +553,57 @@ __global__ void __launch_bounds__(kTileThreads, 3) k_tile_scatter(const Node* no
 #pragma unroll
   for (int u = 0; u < kTileKeysPerThread; ++u) {
     const uint32_t i = threadIdx.x + u * kTileThreads;
-    if (i < tl.n) rank[u] = (uint16_t)atomicAdd(&cnt[digit_of(__ldg(src + i), nd.shift)], 1u);
+    if (i < tl.n) rank[u] = (uint16_t)atomicAdd(&cnt[digit_of(__ldg(src + i), sh, w)], 1u);
   }
   __syncthreads();
-  for (uint32_t j = threadIdx.x; j < kFanout; j += blockDim.x) loc[j] = cnt[j];
+  for (uint32_t j = threadIdx.x; j < R; j += blockDim.x) loc[j] = cnt[j];
   __syncthreads();
-  block_scan_array<uint32_t>(loc, kFanout, tmp);
+  block_scan_array<uint32_t>(loc, (int)R, tmp);
 #pragma unroll
   for (int u = 0; u < kTileKeysPerThread; ++u) {
     const uint32_t i = threadIdx.x + u * kTileThreads;
     if (i < tl.n) {
       const uint64_t key = __ldg(src + i);
-      stage[loc[digit_of(key, nd.shift)] + rank[u]] = key;
+      stage[loc[digit_of(key, sh, w)] + rank[u]] = key;
     }
   }
   __syncthreads();
   for (uint32_t i = threadIdx.x; i < tl.n; i += blockDim.x) {
     const uint64_t key = stage[i];
-    const uint32_t d = digit_of(key, nd.shift);
+    const uint32_t d = digit_of(key, sh, w);
     dst[gbase[d] + (i - loc[d])] = key;
   }
 }
 
 // ------------------------------------------------------------ bin count
+
+// Warp-aggregated shared-memory atomics: lanes holding the same value add
+// once (by the lowest such lane).  Hot k-mers (many copies of one key in a
+// bin) otherwise serialise on one shared-memory word.
+__device__ __forceinline__ void agg_add_u32(uint32_t* ctr, uint32_t v, bool hot) {
+  if (!hot) { atomicAdd(&ctr[v], 1u); return; }
+  const uint32_t mask = __activemask();
+  const uint32_t peers = __match_any_sync(mask, v);
+  if ((int)lane_id() == __ffs(peers) - 1) atomicAdd(&ctr[v], (uint32_t)__popc(peers));
+}
+
+// returns this lane's slot: leader reserves popc(peers) slots, peers take ranks
+__device__ __forceinline__ uint32_t agg_reserve_u32(uint32_t* ctr, uint32_t v, bool hot) {
+  if (!hot) return atomicAdd(&ctr[v], 1u);
+  const uint32_t mask = __activemask();
+  const uint32_t peers = __match_any_sync(mask, v);
+  const int leader = __ffs(peers) - 1;
+  uint32_t base = 0;
+  if ((int)lane_id() == leader) base = atomicAdd(&ctr[v], (uint32_t)__popc(peers));
+  base = __shfl_sync(peers, base, leader);
+  return base + (uint32_t)__popc(peers & ((1u << lane_id()) - 1u));
+}
+
+__device__ __forceinline__ void agg_add_u64(unsigned long long* ctr, uint32_t v) {
+  const uint32_t mask = __activemask();
+  const uint32_t peers = __match_any_sync(mask, v);
+  if ((int)lane_id() == __ffs(peers) - 1) atomicAdd(&ctr[v], (unsigned long long)__popc(peers));
+}
 
 // Block-wide exclusive scan of (sum, max) pairs; returns both exclusive
 // values and the block totals.  `tmp` needs 64 u32 slots.
@@ -572,12 +660,12 @@ __device__ void bin_dense(Node* nodes, uint32_t ni, const Node& nd, uint64_t* ke
   for (; i + 3 * T < nd.n; i += 4 * T) {
     const uint64_t k0 = __ldg(keys + i), k1 = __ldg(keys + i + T), k2 = __ldg(keys + i + 2 * T),
                    k3 = __ldg(keys + i + 3 * T);
-    atomicAdd(&hist[k0 & mask], 1ull);
-    atomicAdd(&hist[k1 & mask], 1ull);
-    atomicAdd(&hist[k2 & mask], 1ull);
-    atomicAdd(&hist[k3 & mask], 1ull);
+    agg_add_u64(hist, (uint32_t)(k0 & mask));
+    agg_add_u64(hist, (uint32_t)(k1 & mask));
+    agg_add_u64(hist, (uint32_t)(k2 & mask));
+    agg_add_u64(hist, (uint32_t)(k3 & mask));
   }
-  for (; i < nd.n; i += T) atomicAdd(&hist[__ldg(keys + i) & mask], 1ull);
+  for (; i < nd.n; i += T) agg_add_u64(hist, (uint32_t)(__ldg(keys + i) & mask));
   __syncthreads();
   const uint32_t per = (R + blockDim.x - 1) / blockDim.x;
   const uint32_t lo = min(R, threadIdx.x * per), hi = min(R, lo + per);
@@ -768,7 +856,7 @@ constexpr uint32_t kDeferMax = 64;  // ranges per bin left to the block-wide sor
 // block scan and writes (key, count) over the bin's own key range.
 __device__ void bin_sorted(Node* nodes, uint32_t ni, const Node& nd, uint64_t* keys, uint32_t* cnt,
                            unsigned long long* skeys, uint32_t* hist, uint32_t* tmp,
-                           uint32_t* mark, uint16_t* defer, uint32_t* n_defer) {
+                           uint32_t* mark, uint16_t* defer, uint32_t* n_defer, bool hot) {
   const uint32_t n = (uint32_t)nd.n;
   DK_PHASE_BEGIN();
   int D = ceil_log2_u64(n);
@@ -784,12 +872,12 @@ __device__ void bin_sorted(Node* nodes, uint32_t ni, const Node& nd, uint64_t* k
   for (; i + 3 * T < n; i += 4 * T) {
     const uint64_t k0 = __ldg(keys + i), k1 = __ldg(keys + i + T), k2 = __ldg(keys + i + 2 * T),
                    k3 = __ldg(keys + i + 3 * T);
-    atomicAdd(&hist[(uint32_t)(k0 >> sh) & M], 1u);
-    atomicAdd(&hist[(uint32_t)(k1 >> sh) & M], 1u);
-    atomicAdd(&hist[(uint32_t)(k2 >> sh) & M], 1u);
-    atomicAdd(&hist[(uint32_t)(k3 >> sh) & M], 1u);
+    agg_add_u32(hist, (uint32_t)(k0 >> sh) & M, hot);
+    agg_add_u32(hist, (uint32_t)(k1 >> sh) & M, hot);
+    agg_add_u32(hist, (uint32_t)(k2 >> sh) & M, hot);
+    agg_add_u32(hist, (uint32_t)(k3 >> sh) & M, hot);
   }
-  for (; i < n; i += T) atomicAdd(&hist[(uint32_t)(__ldg(keys + i) >> sh) & M], 1u);
+  for (; i < n; i += T) agg_add_u32(hist, (uint32_t)(__ldg(keys + i) >> sh) & M, hot);
   __syncthreads();
   DK_PHASE(1);
   block_scan_array<uint32_t>(hist, (int)R, tmp);
@@ -798,17 +886,17 @@ __device__ void bin_sorted(Node* nodes, uint32_t ni, const Node& nd, uint64_t* k
   for (; i + 3 * T < n; i += 4 * T) {
     const uint64_t k0 = __ldg(keys + i), k1 = __ldg(keys + i + T), k2 = __ldg(keys + i + 2 * T),
                    k3 = __ldg(keys + i + 3 * T);
-    uint32_t p0 = atomicAdd(&hist[(uint32_t)(k0 >> sh) & M], 1u);
-    uint32_t p1 = atomicAdd(&hist[(uint32_t)(k1 >> sh) & M], 1u);
-    uint32_t p2 = atomicAdd(&hist[(uint32_t)(k2 >> sh) & M], 1u);
-    uint32_t p3 = atomicAdd(&hist[(uint32_t)(k3 >> sh) & M], 1u);
+    uint32_t p0 = agg_reserve_u32(hist, (uint32_t)(k0 >> sh) & M, hot);
+    uint32_t p1 = agg_reserve_u32(hist, (uint32_t)(k1 >> sh) & M, hot);
+    uint32_t p2 = agg_reserve_u32(hist, (uint32_t)(k2 >> sh) & M, hot);
+    uint32_t p3 = agg_reserve_u32(hist, (uint32_t)(k3 >> sh) & M, hot);
     if (DK_OK_IDX(p0 < n && p1 < n && p2 < n && p3 < n, 11, n)) {
       skeys[p0] = k0; skeys[p1] = k1; skeys[p2] = k2; skeys[p3] = k3;
     }
   }
   for (; i < n; i += T) {
     const uint64_t k0 = __ldg(keys + i);
-    const uint32_t p0 = atomicAdd(&hist[(uint32_t)(k0 >> sh) & M], 1u);
+    const uint32_t p0 = agg_reserve_u32(hist, (uint32_t)(k0 >> sh) & M, hot);
     if (DK_OK_IDX(p0 < n, 12, n)) skeys[p0] = k0;
   }
   __syncthreads();
@@ -961,7 +1049,7 @@ __device__ void warp_bitonic_pairs(unsigned long long* s, uint32_t* c, uint32_t 
 // when the bin holds more than kHashMaxDistinct distinct keys.
 __device__ bool bin_hashed(Node* nodes, uint32_t ni, const Node& nd, uint64_t* keys, uint32_t* cnt,
                            unsigned long long* region, uint32_t* hist, uint32_t* tmp,
-                           uint32_t* mark, uint32_t* flags) {
+                           uint32_t* mark, uint32_t* flags, bool hot) {
   unsigned long long* tk = region;                                  // kHashSlots keys
   uint32_t* tc = reinterpret_cast<uint32_t*>(tk + kHashSlots);       // kHashSlots counts
   unsigned long long* sk = reinterpret_cast<unsigned long long*>(tc + kHashSlots);  // sorted keys
@@ -971,17 +1059,38 @@ __device__ bool bin_hashed(Node* nodes, uint32_t ni, const Node& nd, uint64_t* k
   for (uint32_t j = threadIdx.x; j < kHashSlots; j += T) { tk[j] = kEmptyKey; tc[j] = 0; }
   if (threadIdx.x == 0) { flags[0] = 0; flags[1] = 0; }
   __syncthreads();
-  for (uint32_t i = threadIdx.x; i < n; i += T) {
-    const unsigned long long key = __ldg(keys + i);
-    uint32_t slot = (uint32_t)((key * 0x9E3779B97F4A7C15ull) >> 52);  // 12 bits = kHashSlots
-    for (uint32_t probe = 0; probe < kHashSlots; ++probe) {
-      const unsigned long long prev = atomicCAS(&tk[slot], kEmptyKey, key);
-      if (prev == kEmptyKey || prev == key) {
-        atomicAdd(&tc[slot], 1u);
-        if (prev == kEmptyKey && atomicAdd(&flags[0], 1u) + 1 > kHashMaxDistinct) flags[1] = 1;
-        break;
+  // keys are loaded kHashBatch at a time so their global loads overlap
+  constexpr int kHashBatch = 8;
+  for (uint32_t i0 = 0; i0 < n; i0 += kHashBatch * T) {
+    unsigned long long kk[kHashBatch];
+#pragma unroll
+    for (int u = 0; u < kHashBatch; ++u) {
+      const uint32_t i = i0 + (uint32_t)u * T + threadIdx.x;
+      kk[u] = i < n ? __ldg(keys + i) : kEmptyKey;
+    }
+#pragma unroll
+    for (int u = 0; u < kHashBatch; ++u) {
+      const unsigned long long key = kk[u];
+      if (i0 + (uint32_t)u * T >= n) break;  // uniform: no lane has a key from here on
+      bool live = key != kEmptyKey;
+      // in a hot bin, copies of one key in this warp insert once with their multiplicity
+      uint32_t mult = 1;
+      if (hot) {
+        const uint32_t peers = __match_any_sync(0xFFFFFFFFu, key);
+        live = live && (int)lane_id() == __ffs(peers) - 1;
+        mult = (uint32_t)__popc(peers);
       }
-      slot = (slot + 1) & (kHashSlots - 1);
+      if (!live) continue;
+      uint32_t slot = (uint32_t)((key * 0x9E3779B97F4A7C15ull) >> 52);  // 12 bits = kHashSlots
+      for (uint32_t probe = 0; probe < kHashSlots; ++probe) {
+        const unsigned long long prev = atomicCAS(&tk[slot], kEmptyKey, key);
+        if (prev == kEmptyKey || prev == key) {
+          atomicAdd(&tc[slot], mult);
+          if (prev == kEmptyKey && atomicAdd(&flags[0], 1u) + 1 > kHashMaxDistinct) flags[1] = 1;
+          break;
+        }
+        slot = (slot + 1) & (kHashSlots - 1);
+      }
     }
   }
   __syncthreads();
@@ -1056,26 +1165,47 @@ __global__ void __launch_bounds__(kBinThreads, 2) k_bin_count(Node* nodes,
   __shared__ uint16_t defer[kDeferMax];
   __shared__ uint32_t s_bin, n_defer;
   __shared__ uint32_t hflags[2];
+  __shared__ bool s_hot;
+  if (threadIdx.x == 0) s_bin = atomicAdd(reinterpret_cast<unsigned int*>(&ctr[4]), 1u);
+  __syncthreads();
   for (;;) {
-    if (threadIdx.x == 0) s_bin = atomicAdd(reinterpret_cast<unsigned int*>(&ctr[4]), 1u);
-    __syncthreads();
     const uint32_t b = s_bin;
     if (b >= n_final) break;
     const uint32_t ni = finals[b];
     const Node nd = nodes[ni];
     uint64_t* keys = (nd.buf ? B : A) + nd.start;
     uint32_t* cnt = C + nd.start;
+    __syncthreads();  // every thread has read s_bin
+    if (threadIdx.x == 32) {
+      // take the next bin now and start pulling its keys into L2 while this one runs
+      const uint32_t nb = atomicAdd(reinterpret_cast<unsigned int*>(&ctr[4]), 1u);
+      s_bin = nb;
+      if (nb < n_final) {
+        const Node& nx = nodes[finals[nb]];
+        prefetch_l2_range((nx.buf ? B : A) + nx.start, nx.n * 8);
+      }
+    }
+    // hot bin: a sample of 32 keys spread over the bin repeats one key >= 4
+    // times; its atomics are then aggregated per warp
+    if (threadIdx.x < 32) {
+      const uint64_t smp = nd.n ? __ldg(keys + (nd.n * threadIdx.x) / 32) : 0ull;
+      const uint32_t peers = __match_any_sync(0xFFFFFFFFu, smp);
+      const uint32_t dup = __reduce_max_sync(0xFFFFFFFFu, (uint32_t)__popc(peers));
+      if (threadIdx.x == 0) s_hot = dup >= 4;
+    }
+    __syncthreads();
+    const bool hot = s_hot;
     if (nd.shift <= kDenseBits) {
       bin_dense(nodes, ni, nd, keys, cnt, skeys, reinterpret_cast<unsigned long long*>(tmp),
                 &ctr[5]);
     } else {
       bool done = false;
       if (use_hash) {
-        done = bin_hashed(nodes, ni, nd, keys, cnt, skeys, hist, tmp, mark, hflags);
+        done = bin_hashed(nodes, ni, nd, keys, cnt, skeys, hist, tmp, mark, hflags, hot);
         if (!done && threadIdx.x == 0) atomicAdd(&ctr[6], 1ull);  // bins that fell back
         __syncthreads();
       }
-      if (!done) bin_sorted(nodes, ni, nd, keys, cnt, skeys, hist, tmp, mark, defer, &n_defer);
+      if (!done) bin_sorted(nodes, ni, nd, keys, cnt, skeys, hist, tmp, mark, defer, &n_defer, hot);
     }
     __syncthreads();
   }
@@ -1088,7 +1218,8 @@ __global__ void k_aggregate(Node* nodes, uint32_t lo, uint32_t hi) {
   const Node nd = nodes[i];
   if (nd.state != NODE_SPLIT) return;
   uint64_t d = 0;
-  for (int j = 0; j < kFanout; ++j) d += nodes[nd.first_child + j].d;
+  const uint32_t R = 1u << nd.width;
+  for (uint32_t j = 0; j < R; ++j) d += nodes[nd.first_child + j].d;
   nodes[i].d = d;
 }
 
@@ -1111,9 +1242,17 @@ __global__ void __launch_bounds__(256) k_child_offsets(Node* nodes, uint32_t lo)
   __shared__ unsigned long long tmp[32];
   const Node nd = nodes[lo + blockIdx.x];
   if (nd.state != NODE_SPLIT) return;
-  Node& ch = nodes[nd.first_child + threadIdx.x];
-  const unsigned long long e = block_excl_scan<unsigned long long>(ch.d, tmp, nullptr);
-  ch.out_off = nd.out_off + e;
+  const uint32_t R = 1u << nd.width;
+  const uint32_t per = (R + blockDim.x - 1) / blockDim.x;
+  const uint32_t j0 = min(R, threadIdx.x * per), j1 = min(R, j0 + per);
+  unsigned long long s = 0;
+  for (uint32_t j = j0; j < j1; ++j) s += nodes[nd.first_child + j].d;
+  unsigned long long base = nd.out_off + block_excl_scan<unsigned long long>(s, tmp, nullptr);
+  for (uint32_t j = j0; j < j1; ++j) {
+    Node& ch = nodes[nd.first_child + j];
+    ch.out_off = base;
+    base += ch.d;
+  }
 }
 
 // one warp per final node: staged pairs -> output table
@@ -1170,12 +1309,28 @@ int launch_l1_count(const ExtractArgs& a, int grid, uint32_t* H, unsigned long l
 }
 
 int launch_l1_scan(const uint32_t* H, int grid, int F1, uint64_t* O, Node* nodes, int shift1,
-                   cudaStream_t s) {
+                   const int16_t* bucket_shift, cudaStream_t s) {
   const int tb = 256, nb = (F1 + tb - 1) / tb;
   k_l1_totals<<<nb, tb, 0, s>>>(H, grid, F1, nodes);
-  k_l1_starts<<<1, 1024, 0, s>>>(nodes, F1, shift1);
+  k_l1_starts<<<1, 1024, 0, s>>>(nodes, F1, shift1, bucket_shift);
   k_l1_offsets_rows<<<nb, tb, 0, s>>>(H, grid, F1, nodes, O);
   return 3;
+}
+
+static int lpw_of(int c) { return c <= 2 ? 4 : (c <= 8 ? 2 : 1); }
+
+static size_t scatter_smem(int W, int F1, bool jobs) {
+  const int C = choose_c(W);
+  const uint32_t lt = 16u * (uint32_t)lpw_of(C);
+  const size_t stage_cap = (size_t)lt * 32 * C;
+  return 128 + 2 * (size_t)tile_buf_bytes(lt, (uint64_t)W + 1) + (size_t)F1 * 16 +
+         stage_cap * 8 + 32 * 4 + 256 + (jobs ? stage_cap * 2 : 0);
+}
+
+int l1_max_buckets(int W, bool jobs) {
+  int f = 1 << kMaxL1Bits;
+  while (f > 1 && scatter_smem(W, f, jobs) > kMaxSmemPerBlock) f >>= 1;
+  return f;
 }
 
 template <int C, int LPW>
@@ -1184,8 +1339,8 @@ static void scatter_launch(const ExtractArgs& a, int grid, const uint64_t* O, ui
   const int threads = 512;
   const uint32_t lt = (threads / 32) * LPW;
   const int stage_cap = (int)lt * 32 * C;  // >= k-mers of one tile
-  const size_t smem = 128 + 2 * (size_t)tile_buf_bytes(lt, (uint64_t)a.W + 1) +
-                      (size_t)a.F1 * 8 + (size_t)stage_cap * 8 + (size_t)a.F1 * 8 + 32 * 4 + 256;
+  static_assert(LPW == (C <= 2 ? 4 : (C <= 8 ? 2 : 1)), "scatter_smem mirrors this tiling");
+  const size_t smem = scatter_smem(a.W, a.F1, a.njobs != 0);
   cudaFuncSetAttribute(k_l1_scatter<C, LPW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   k_l1_scatter<C, LPW><<<grid, threads, smem, s>>>(a, O, keys, stage_cap, counters);
 }
@@ -1205,10 +1360,11 @@ int launch_l1_scatter(const ExtractArgs& a, int grid, const uint64_t* O, uint64_
 }
 
 int launch_classify(Node* nodes, uint32_t lo, uint32_t hi, uint32_t* final_list,
-                    LevelCounters* ctr, int bin_cap, cudaStream_t s) {
+                    LevelCounters* ctr, int bin_cap, int split_target, cudaStream_t s) {
   const uint32_t n = hi - lo;
   if (!n) return 0;
-  k_classify<<<(n + 255) / 256, 256, 0, s>>>(nodes, lo, hi, final_list, ctr, bin_cap);
+  k_classify<<<(n + 255) / 256, 256, 0, s>>>(nodes, lo, hi, final_list, ctr, bin_cap,
+                                            split_target);
   return 1;
 }
 
@@ -1235,10 +1391,11 @@ int launch_node_scan(Node* nodes, uint32_t lo, uint32_t hi, const Tile* tiles, u
 }
 
 int launch_tile_scatter(const Node* nodes, const Tile* tiles, uint32_t n_tiles, uint64_t* A,
-                        uint64_t* B, const uint32_t* TH, cudaStream_t s) {
+                        uint64_t* B, const uint32_t* TH, int max_width, cudaStream_t s) {
   if (!n_tiles) return 0;
-  cudaFuncSetAttribute(k_tile_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize, kTileKeys * 8);
-  k_tile_scatter<<<n_tiles, kTileThreads, kTileKeys * 8, s>>>(nodes, tiles, A, B, TH);
+  const size_t smem = (size_t)kTileKeys * 8 + ((size_t)1 << max_width) * 16;
+  cudaFuncSetAttribute(k_tile_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  k_tile_scatter<<<n_tiles, kTileThreads, smem, s>>>(nodes, tiles, A, B, TH, max_width);
   return 1;
 }
 

@@ -81,7 +81,9 @@ typedef struct {
   int convention;  /* DK_CONV_DAKC                                               */
   int variant;     /* DK_VARIANT_*                                               */
   int residency;   /* DK_RESIDENT_*                                              */
-  int reserved[3];
+  int l1_bits;     /* tuning: level-1 partition bits, 0 = automatic (<= 12)     */
+  int bin_target;  /* tuning: target keys per bin, 0 = automatic (<= 6000)      */
+  int reserved;
 } dk_input_desc;
 
 typedef struct {
