@@ -469,6 +469,7 @@ def main():
                                   "frac_nominal_8tbs": pipe / 8000.0},
             "kernels_ms_per_step": {KERNEL_NAMES[i]: float(kms[i]) for i in range(8)},
             "n_kmers": nk, "n_distinct": nd, "partition_levels": sts[0]["partition_levels"],
+            "n_bins": sts[0]["n_bins"], "n_bins_resorted": sts[0]["n_bins_resorted"],
             "wall_ms_per_step": (w1 - w0) * 1000.0 / args.steps,
             "clocks": clk,
             "e2e": e2e,

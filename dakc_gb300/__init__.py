@@ -93,7 +93,8 @@ class Stats(ctypes.Structure):
                 ("dev_bytes_peak", ctypes.c_uint64), ("variant_used", ctypes.c_int),
                 ("partition_levels", ctypes.c_int), ("n_bins", ctypes.c_uint64),
                 ("ms_kernel", ctypes.c_double * 8), ("launches_kernel", ctypes.c_uint64 * 8),
-                ("n_partitioned", ctypes.c_uint64), ("n_waves", ctypes.c_uint64)]
+                ("n_partitioned", ctypes.c_uint64), ("n_waves", ctypes.c_uint64),
+                ("n_bins_resorted", ctypes.c_uint64)]
 
     KERNEL_NAMES = ["extract_count", "extract_scatter", "partition_hist", "partition_scatter",
                     "bin_count", "compact", "hash_insert", "other"]

@@ -404,6 +404,19 @@ int Engine::count_batch(const dk_job* jobs, int njobs, const dk_input_desc* desc
     ms_h2d += t_h2d;
     ms_device += stats.ms_device;
     launches_total += stats.kernel_launches;
+    for (int q = 0; q < 8; ++q) {
+      stats_batch.ms_kernel[q] += stats.ms_kernel[q];
+      stats_batch.launches_kernel[q] += stats.launches_kernel[q];
+      stats_batch.ms_stage[q] += stats.ms_stage[q];
+    }
+    stats_batch.n_kmers += stats.n_kmers;
+    stats_batch.n_distinct += stats.n_distinct;
+    stats_batch.n_lines += stats.n_lines;
+    stats_batch.n_bins += stats.n_bins;
+    stats_batch.n_partitioned += stats.n_partitioned;
+    stats_batch.n_bins_resorted += stats.n_bins_resorted;
+    stats_batch.partition_levels = std::max(stats_batch.partition_levels, stats.partition_levels);
+    stats_batch.variant_used = stats.variant_used;
     TableBuf* h_tb = nullptr;
     rc = acquire_table(std::max<uint64_t>(dt.n, 1), false, &h_tb);
     if (rc != DK_OK) {
@@ -481,22 +494,31 @@ static void gather_range(const std::vector<Engine::Seg>& segs, uint64_t dst_lo, 
 }
 
 // Host -> device copy of segments laid out at segs[i].doff in d.  Pinned
-// segments go straight to the DMA engine; pageable ones are packed into two
-// 64 MB pinned slots by several host threads while the other slot's DMA runs.
-// A slot is refilled only after the copy that last read it has finished.
+// segments go straight to the DMA engine; runs of pageable segments (no pinned
+// segment between them) are packed into two 64 MB pinned slots by several host
+// threads while the other slot's DMA runs.  A slot copy covers only its run,
+// so it never overwrites a pinned segment's bytes; bytes inside a run that no
+// segment covers are missing final terminators, which are never examined.  A
+// slot is refilled only after the copy that last read it has finished.
 int Engine::upload_segments(const std::vector<Seg>& all, uint8_t* d) {
   Engine* e = this;
-  std::vector<Seg> segs;
-  for (const Seg& sg : all) {
-    if (!sg.n) continue;
-    if (is_pinned(sg.h)) {
-      DK_CUDA(cudaMemcpyAsync(d + sg.doff, sg.h, sg.n, cudaMemcpyHostToDevice, stream));
+  struct S {
+    Seg sg;
+    bool pinned;
+  };
+  std::vector<S> v;
+  for (const Seg& sg : all)
+    if (sg.n) v.push_back({sg, is_pinned(sg.h)});
+  std::sort(v.begin(), v.end(), [](const S& x, const S& y) { return x.sg.doff < y.sg.doff; });
+  bool any_pageable = false;
+  for (const S& x : v) {
+    if (x.pinned) {
+      DK_CUDA(cudaMemcpyAsync(d + x.sg.doff, x.sg.h, x.sg.n, cudaMemcpyHostToDevice, stream));
     } else {
-      segs.push_back(sg);
+      any_pageable = true;
     }
   }
-  if (segs.empty()) return DK_OK;
-  std::sort(segs.begin(), segs.end(), [](const Seg& x, const Seg& y) { return x.doff < y.doff; });
+  if (!any_pageable) return DK_OK;
   const size_t slot = 64ull << 20;
   for (int i = 0; i < 2; ++i) {
     if (!stage_pinned[i]) DK_CUDA(cudaMallocHost(&stage_pinned[i], slot));
@@ -504,30 +526,38 @@ int Engine::upload_segments(const std::vector<Seg>& all, uint8_t* d) {
   }
   const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
   const int nthreads = (int)std::min<unsigned>(8, std::max(1u, hw / 2));
-  uint64_t lo = segs.front().doff;
-  const uint64_t end = segs.back().doff + segs.back().n;
-  while (lo < end) {
-    const int i = stage_next;
-    const uint64_t hi = std::min<uint64_t>(end, lo + slot);
-    DK_CUDA(cudaEventSynchronize(stage_ev[i]));
-    uint8_t* buf = (uint8_t*)stage_pinned[i];
-    const uint64_t len = hi - lo;
-    if (len < (4u << 20) || nthreads == 1) {
-      gather_range(segs, lo, hi, buf, lo);
-    } else {
-      std::vector<std::thread> th;
-      const uint64_t chunk = (len + nthreads - 1) / nthreads;
-      for (int t = 0; t < nthreads; ++t) {
-        const uint64_t a = lo + (uint64_t)t * chunk, b = std::min(hi, a + chunk);
-        if (a >= b) break;
-        th.emplace_back([&segs, a, b, buf, lo] { gather_range(segs, a, b, buf, lo); });
+  size_t r0 = 0;
+  while (r0 < v.size()) {
+    if (v[r0].pinned) { ++r0; continue; }
+    size_t r1 = r0;
+    std::vector<Seg> run;
+    while (r1 < v.size() && !v[r1].pinned) run.push_back(v[r1++].sg);
+    uint64_t lo = run.front().doff;
+    const uint64_t end = run.back().doff + run.back().n;
+    while (lo < end) {
+      const int i = stage_next;
+      const uint64_t hi = std::min<uint64_t>(end, lo + slot);
+      DK_CUDA(cudaEventSynchronize(stage_ev[i]));
+      uint8_t* buf = (uint8_t*)stage_pinned[i];
+      const uint64_t len = hi - lo;
+      if (len < (4u << 20) || nthreads == 1) {
+        gather_range(run, lo, hi, buf, lo);
+      } else {
+        std::vector<std::thread> th;
+        const uint64_t chunk = (len + nthreads - 1) / nthreads;
+        for (int t = 0; t < nthreads; ++t) {
+          const uint64_t a = lo + (uint64_t)t * chunk, b = std::min(hi, a + chunk);
+          if (a >= b) break;
+          th.emplace_back([&run, a, b, buf, lo] { gather_range(run, a, b, buf, lo); });
+        }
+        for (auto& t : th) t.join();
       }
-      for (auto& t : th) t.join();
+      DK_CUDA(cudaMemcpyAsync(d + lo, buf, len, cudaMemcpyHostToDevice, stream));
+      DK_CUDA(cudaEventRecord(stage_ev[i], stream));
+      lo = hi;
+      stage_next ^= 1;
     }
-    DK_CUDA(cudaMemcpyAsync(d + lo, buf, len, cudaMemcpyHostToDevice, stream));
-    DK_CUDA(cudaEventRecord(stage_ev[i], stream));
-    lo = hi;
-    stage_next ^= 1;
+    r0 = r1;
   }
   return DK_OK;
 }
@@ -718,8 +748,9 @@ int Engine::count_device(const uint8_t* d_text, uint64_t nbytes, const dk_input_
   TIMED(7, launch_l1_offsets((Node*)nodes.p, (uint32_t)F1, c64 + 2, stream));
   for (size_t l = 0; l + 1 < levels.size(); ++l)
     TIMED(7, launch_child_offsets((Node*)nodes.p, levels[l].first, levels[l].second, stream));
-  uint64_t tail[4];
-  DK_TRY(sync_read(c64 + 2, 32, tail));
+  uint64_t tail[5];
+  DK_TRY(sync_read(c64 + 2, 40, tail));
+  stats.n_bins_resorted = tail[4];
   const uint64_t n_distinct = tail[0];
   if (tail[1]) {
     set_error("a bounded device wait (TMA copy) timed out");

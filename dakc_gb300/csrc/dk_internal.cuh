@@ -61,6 +61,8 @@ constexpr int kTileKeys = 8192;         // keys per partition tile
 constexpr int kBinCap = 12000;          // keys a bin-count CTA sorts in shared memory
 constexpr int kDenseBits = 12;          // nodes with <= this many free bits are counted densely
 constexpr int kBinThreads = 512;
+constexpr int kBinBlocksPerSM = 2;      // resident bin-count CTAs per SM
+constexpr int kBinDigitBits = 12;       // counting-sort digit of a bin: at most this many bits
 constexpr int kMaxL1Bits = 12;          // level-1 fan-out <= 4096 buckets
 constexpr size_t kMaxSmemPerBlock = 232448;  // opt-in shared memory per block (sm_100 family)
 

@@ -51,7 +51,7 @@ __device__ unsigned long long g_check[4];
 // Optional per-phase cycle counters for the bin kernel (build with
 // -DDK_PHASE_TIMING; read them with dk_debug_phases).  Compiled out otherwise.
 #ifdef DK_PHASE_TIMING
-__device__ unsigned long long g_phase[16];
+__device__ unsigned long long g_phase[32];
 #define DK_PHASE_BEGIN() unsigned long long _ph_t = clock64()
 #define DK_PHASE(k)                                                    \
   do {                                                                 \
@@ -526,6 +526,7 @@ __global__ void __launch_bounds__(256) k_node_scan(Node* nodes, uint32_t lo, con
 // contiguous, coalesced run at the tile's offset inside the child.
 constexpr int kTileThreads = 512;
 constexpr int kTileKeysPerThread = kTileKeys / kTileThreads;
+static_assert(kTileKeys <= 65536 && kTileKeysPerThread % 2 == 0, "ranks are packed as 16-bit pairs");
 
 __global__ void __launch_bounds__(kTileThreads, 2) k_tile_scatter(const Node* nodes,
                                                                   const Tile* tiles, uint64_t* A,
@@ -549,11 +550,21 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_tile_scatter(const Node* no
     cnt[j] = 0;
   }
   __syncthreads();
-  uint16_t rank[kTileKeysPerThread];
+  // all of this thread's keys are loaded first (their loads overlap) and kept
+  // in registers for the staging pass
+  uint64_t kr[kTileKeysPerThread];
 #pragma unroll
   for (int u = 0; u < kTileKeysPerThread; ++u) {
     const uint32_t i = threadIdx.x + u * kTileThreads;
-    if (i < tl.n) rank[u] = (uint16_t)atomicAdd(&cnt[digit_of(__ldg(src + i), sh, w)], 1u);
+    kr[u] = i < tl.n ? __ldg(src + i) : 0ull;
+  }
+  uint32_t rank[kTileKeysPerThread / 2];  // two 16-bit ranks per word
+#pragma unroll
+  for (int u = 0; u < kTileKeysPerThread; ++u) {
+    const uint32_t i = threadIdx.x + u * kTileThreads;
+    const uint32_t r = i < tl.n ? atomicAdd(&cnt[digit_of(kr[u], sh, w)], 1u) : 0u;
+    if (u & 1) rank[u >> 1] |= r << 16;
+    else rank[u >> 1] = r;
   }
   __syncthreads();
   for (uint32_t j = threadIdx.x; j < R; j += blockDim.x) loc[j] = cnt[j];
@@ -563,8 +574,8 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_tile_scatter(const Node* no
   for (int u = 0; u < kTileKeysPerThread; ++u) {
     const uint32_t i = threadIdx.x + u * kTileThreads;
     if (i < tl.n) {
-      const uint64_t key = __ldg(src + i);
-      stage[loc[digit_of(key, sh, w)] + rank[u]] = key;
+      const uint32_t r = (rank[u >> 1] >> ((u & 1) * 16)) & 0xFFFFu;
+      stage[loc[digit_of(kr[u], sh, w)] + r] = kr[u];
     }
   }
   __syncthreads();
@@ -576,6 +587,7 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_tile_scatter(const Node* no
 }
 
 // ------------------------------------------------------------ bin count
+constexpr uint32_t kThreadSortMax = 16;  // larger digit ranges are sorted by a warp
 
 // Warp-aggregated shared-memory atomics: lanes holding the same value add
 // once (by the lowest such lane).  Hot k-mers (many copies of one key in a
@@ -860,7 +872,7 @@ __device__ void bin_sorted(Node* nodes, uint32_t ni, const Node& nd, uint64_t* k
   const uint32_t n = (uint32_t)nd.n;
   DK_PHASE_BEGIN();
   int D = ceil_log2_u64(n);
-  D = max(4, min(D, kDenseBits));
+  D = max(4, min(D, kBinDigitBits));
   D = min(D, (int)nd.shift);
   const int sh = nd.shift - D;
   const uint32_t R = 1u << D, M = R - 1;
@@ -922,6 +934,27 @@ __device__ void bin_sorted(Node* nodes, uint32_t ni, const Node& nd, uint64_t* k
     }
     __syncthreads();
     DK_PHASE(4);
+    // small marked ranges: sorted by the thread that owns the digit
+    {
+      const uint32_t per = (R + T - 1) / T;
+      const uint32_t j0 = min(R, threadIdx.x * per), j1 = min(R, j0 + per);
+      for (uint32_t j = j0; j < j1; ++j) {
+        if (!(mark[j >> 5] & (1u << (j & 31)))) continue;
+        const uint32_t lo = j ? hist[j - 1] : 0, hi = hist[j];
+        if (!DK_OK_IDX(lo <= hi && hi <= n, 16, ((uint64_t)lo << 32) | hi)) continue;
+        if (hi - lo > kThreadSortMax) continue;
+        for (uint32_t x = lo + 1; x < hi; ++x) {
+          const unsigned long long v = skeys[x];
+          uint32_t y = x;
+          while (y > lo && skeys[y - 1] > v) {
+            skeys[y] = skeys[y - 1];
+            --y;
+          }
+          skeys[y] = v;
+        }
+      }
+    }
+    __syncthreads();
     const uint32_t warp = threadIdx.x >> 5, nwarps = T >> 5;
     for (uint32_t w = warp; w < (R + 31) / 32; w += nwarps) {
       uint32_t bits = mark[w];
@@ -931,6 +964,7 @@ __device__ void bin_sorted(Node* nodes, uint32_t ni, const Node& nd, uint64_t* k
         const uint32_t lo = j ? hist[j - 1] : 0, hi = hist[j];
         const uint32_t m = hi - lo;
         if (!DK_OK_IDX(lo <= hi && hi <= n && j < R, 13, ((uint64_t)lo << 32) | hi)) continue;
+        if (m <= kThreadSortMax) continue;  // done above
         if (m <= 32) {
           warp_rank_sort(skeys + lo, m);
           DK_WARP_ADD(11, 1);
@@ -993,11 +1027,17 @@ __device__ void bin_sorted(Node* nodes, uint32_t ni, const Node& nd, uint64_t* k
 }
 
 // ---- hash variant: aggregate the bin in a shared-memory hash table first
-constexpr uint32_t kHashSlots = 4096;                 // table slots per bin
-constexpr uint32_t kHashMaxDistinct = 3072;           // 75% load; more falls back to sorting
+constexpr int kHashSlotBits = kBinCap >= 8192 ? 12 : 11;
+constexpr uint32_t kHashSlots = 1u << kHashSlotBits;  // table slots per bin
+constexpr uint32_t kHashMaxProbe = 64;                // a longer probe sends the bin to sorting
+// sorted pairs that fit beside the table (a multiple of 64)
+constexpr uint32_t kHashMaxDistinct = ((kBinCap * 8 - kHashSlots * 12) / 12) & ~63u;
 constexpr unsigned long long kEmptyKey = ~0ull;       // never a k-mer when k <= 31
+static_assert(kHashSlots * 12 + kHashMaxDistinct * 12 <= kBinCap * 8,
+              "table and sorted pairs share the bin's shared-memory region");
+static_assert(kBinCap >= (1 << kDenseBits) * 8 / 8, "a dense bin's 2^kDenseBits u64 counters fit the region");
 
-// (key, count) pair versions of the small in-place sorts
+// (key, count) pair versions of the warp sorts
 __device__ void warp_rank_sort_pairs(unsigned long long* s, uint32_t* c, uint32_t m) {
   const uint32_t lane = lane_id();
   const unsigned long long v = lane < m ? s[lane] : 0ull;
@@ -1043,10 +1083,12 @@ __device__ void warp_bitonic_pairs(unsigned long long* s, uint32_t* c, uint32_t 
 }
 
 // Aggregate the bin's keys in a shared-memory open-addressing table (linear
-// probing, 64-bit atomicCAS on the key, atomicAdd on its count), then
-// counting-sort the distinct (key, count) pairs on their top free bits and
-// finish the few out-of-order digit ranges.  Returns false (nothing written)
-// when the bin holds more than kHashMaxDistinct distinct keys.
+// probing on a multiplicative hash, 64-bit atomicCAS on the key, atomicAdd on
+// its count), counting-sort the distinct (key, count) pairs on their top free
+// bits, sort the digit ranges holding several keys (a thread per small range,
+// a warp per large one) and write the pairs over the bin's own key range.
+// Returns false, having written nothing, when a probe runs past
+// kHashMaxProbe slots or the bin holds more than kHashMaxDistinct keys.
 __device__ bool bin_hashed(Node* nodes, uint32_t ni, const Node& nd, uint64_t* keys, uint32_t* cnt,
                            unsigned long long* region, uint32_t* hist, uint32_t* tmp,
                            uint32_t* mark, uint32_t* flags, bool hot) {
@@ -1056,37 +1098,39 @@ __device__ bool bin_hashed(Node* nodes, uint32_t ni, const Node& nd, uint64_t* k
   uint32_t* sc = reinterpret_cast<uint32_t*>(sk + kHashMaxDistinct);                // sorted counts
   const uint32_t n = (uint32_t)nd.n;
   const uint32_t T = blockDim.x;
+  DK_PHASE_BEGIN();
   for (uint32_t j = threadIdx.x; j < kHashSlots; j += T) { tk[j] = kEmptyKey; tc[j] = 0; }
-  if (threadIdx.x == 0) { flags[0] = 0; flags[1] = 0; }
+  if (threadIdx.x == 0) flags[1] = 0;
   __syncthreads();
-  // keys are loaded kHashBatch at a time so their global loads overlap
-  constexpr int kHashBatch = 8;
-  for (uint32_t i0 = 0; i0 < n; i0 += kHashBatch * T) {
-    unsigned long long kk[kHashBatch];
+  constexpr int kBatch = 8;  // keys in flight per thread
+  for (uint32_t i0 = 0; i0 < n; i0 += kBatch * T) {
+    unsigned long long kk[kBatch];
 #pragma unroll
-    for (int u = 0; u < kHashBatch; ++u) {
+    for (int u = 0; u < kBatch; ++u) {
       const uint32_t i = i0 + (uint32_t)u * T + threadIdx.x;
       kk[u] = i < n ? __ldg(keys + i) : kEmptyKey;
     }
 #pragma unroll
-    for (int u = 0; u < kHashBatch; ++u) {
-      const unsigned long long key = kk[u];
+    for (int u = 0; u < kBatch; ++u) {
       if (i0 + (uint32_t)u * T >= n) break;  // uniform: no lane has a key from here on
+      const unsigned long long key = kk[u];
       bool live = key != kEmptyKey;
-      // in a hot bin, copies of one key in this warp insert once with their multiplicity
       uint32_t mult = 1;
-      if (hot) {
+      if (hot) {  // copies of one key in this warp insert once with their multiplicity
         const uint32_t peers = __match_any_sync(0xFFFFFFFFu, key);
         live = live && (int)lane_id() == __ffs(peers) - 1;
         mult = (uint32_t)__popc(peers);
       }
       if (!live) continue;
-      uint32_t slot = (uint32_t)((key * 0x9E3779B97F4A7C15ull) >> 52);  // 12 bits = kHashSlots
-      for (uint32_t probe = 0; probe < kHashSlots; ++probe) {
+      uint32_t slot = (uint32_t)((key * 0x9E3779B97F4A7C15ull) >> (64 - kHashSlotBits));
+      for (uint32_t probe = 0;; ++probe) {
+        if (probe == kHashMaxProbe) {  // table too full (or adversarial keys): sort instead
+          flags[1] = 1;
+          break;
+        }
         const unsigned long long prev = atomicCAS(&tk[slot], kEmptyKey, key);
         if (prev == kEmptyKey || prev == key) {
           atomicAdd(&tc[slot], mult);
-          if (prev == kEmptyKey && atomicAdd(&flags[0], 1u) + 1 > kHashMaxDistinct) flags[1] = 1;
           break;
         }
         slot = (slot + 1) & (kHashSlots - 1);
@@ -1094,20 +1138,29 @@ __device__ bool bin_hashed(Node* nodes, uint32_t ni, const Node& nd, uint64_t* k
     }
   }
   __syncthreads();
+  DK_PHASE(17);
   if (flags[1]) return false;
-  const uint32_t d = flags[0];
+  // distinct keys = filled slots
+  uint32_t occ = 0;
+  for (uint32_t j = threadIdx.x; j < kHashSlots; j += T) occ += tk[j] != kEmptyKey;
+  uint32_t d;
+  block_excl_scan<uint32_t>(occ, tmp, &d);
+  if (d > kHashMaxDistinct) return false;  // uniform: d is the block total
   // counting sort of the distinct pairs on the top D free bits
   int D = ceil_log2_u64(d);
-  D = max(4, min(D, kDenseBits));
+  D = max(4, min(D, kBinDigitBits));
   D = min(D, (int)nd.shift);
   const int sh = nd.shift - D;
   const uint32_t R = 1u << D, M = R - 1;
   for (uint32_t j = threadIdx.x; j < R; j += T) hist[j] = 0;
+  for (uint32_t w = threadIdx.x; w < (R + 31) / 32; w += T) mark[w] = 0;
   __syncthreads();
   for (uint32_t j = threadIdx.x; j < kHashSlots; j += T)
     if (tk[j] != kEmptyKey) atomicAdd(&hist[(uint32_t)(tk[j] >> sh) & M], 1u);
   __syncthreads();
+  DK_PHASE(18);
   block_scan_array<uint32_t>(hist, (int)R, tmp);
+  DK_PHASE(19);
   for (uint32_t j = threadIdx.x; j < kHashSlots; j += T) {
     const unsigned long long key = tk[j];
     if (key != kEmptyKey) {
@@ -1116,18 +1169,38 @@ __device__ bool bin_hashed(Node* nodes, uint32_t ni, const Node& nd, uint64_t* k
     }
   }
   __syncthreads();
-  // ranges with a descent hold several distinct keys out of order
+  DK_PHASE(20);
+  // hist[j] is now the end of digit range j.  A range holding several
+  // distinct keys is in arbitrary order: each thread sorts the small ranges
+  // of its own digits in place (insertion sort); ranges of more than
+  // kThreadSortMax keys are marked and sorted by a warp.
   if (sh > 0) {
-    for (uint32_t w = threadIdx.x; w < (R + 31) / 32; w += T) mark[w] = 0;
-    __syncthreads();
-    for (uint32_t x = threadIdx.x + 1; x < d; x += T) {
-      const unsigned long long v = sk[x], p = sk[x - 1];
-      if ((v >> sh) == (p >> sh) && v < p) {
-        const uint32_t dg = (uint32_t)(v >> sh) & M;
-        atomicOr(&mark[dg >> 5], 1u << (dg & 31));
+    const uint32_t per = (R + T - 1) / T;
+    const uint32_t j0 = min(R, threadIdx.x * per), j1 = min(R, j0 + per);
+    for (uint32_t j = j0; j < j1; ++j) {
+      const uint32_t lo = j ? hist[j - 1] : 0, hi = hist[j];
+      if (!DK_OK_IDX(lo <= hi && hi <= d, 32, ((uint64_t)lo << 32) | hi)) continue;
+      const uint32_t m = hi - lo;
+      if (m < 2) continue;
+      if (m > kThreadSortMax) {
+        atomicOr(&mark[j >> 5], 1u << (j & 31));
+        continue;
+      }
+      for (uint32_t x = lo + 1; x < hi; ++x) {
+        const unsigned long long v = sk[x];
+        const uint32_t c = sc[x];
+        uint32_t y = x;
+        while (y > lo && sk[y - 1] > v) {
+          sk[y] = sk[y - 1];
+          sc[y] = sc[y - 1];
+          --y;
+        }
+        sk[y] = v;
+        sc[y] = c;
       }
     }
     __syncthreads();
+    DK_PHASE(21);
     const uint32_t warp = threadIdx.x >> 5, nwarps = T >> 5;
     for (uint32_t w = warp; w < (R + 31) / 32; w += nwarps) {
       uint32_t bits = mark[w];
@@ -1135,33 +1208,38 @@ __device__ bool bin_hashed(Node* nodes, uint32_t ni, const Node& nd, uint64_t* k
         const uint32_t j = w * 32 + (__ffs(bits) - 1);
         bits &= bits - 1;
         const uint32_t lo = j ? hist[j - 1] : 0, hi = hist[j];
-        if (!DK_OK_IDX(lo <= hi && hi <= d, 32, ((uint64_t)lo << 32) | hi)) continue;
+        if (!DK_OK_IDX(lo <= hi && hi <= d, 33, ((uint64_t)lo << 32) | hi)) continue;
         if (hi - lo <= 32) warp_rank_sort_pairs(sk + lo, sc + lo, hi - lo);
         else warp_bitonic_pairs(sk + lo, sc + lo, hi - lo);
       }
     }
     __syncthreads();
+    DK_PHASE(22);
   }
   for (uint32_t x = threadIdx.x; x < d; x += T) {
     keys[x] = sk[x];
     cnt[x] = sc[x];
   }
+  DK_PHASE(23);
+  DK_PHASE_ADD(24, 1);
+  DK_PHASE_ADD(25, n);
+  DK_PHASE_ADD(26, d);
   if (threadIdx.x == 0) nodes[ni].d = d;
   return true;
 }
 
 // Persistent bin counter: CTAs take final nodes from a ticket until none are
 // left.  Two CTAs fit per SM (96 KB keys + 16 KB histogram each).
-__global__ void __launch_bounds__(kBinThreads, 2) k_bin_count(Node* nodes,
+__global__ void __launch_bounds__(kBinThreads, kBinBlocksPerSM) k_bin_count(Node* nodes,
                                                               const uint32_t* __restrict__ finals,
                                                               uint32_t n_final, uint64_t* A,
                                                               uint64_t* B, uint32_t* C,
                                                               unsigned long long* ctr,
                                                               int use_hash) {
   extern __shared__ __align__(16) unsigned long long skeys[];  // kBinCap keys / 4096 u64 counts
-  __shared__ uint32_t hist[1u << kDenseBits];
+  __shared__ uint32_t hist[1u << kBinDigitBits];
   __shared__ uint32_t tmp[64];
-  __shared__ uint32_t mark[(1u << kDenseBits) / 32];
+  __shared__ uint32_t mark[(1u << kBinDigitBits) / 32];
   __shared__ uint16_t defer[kDeferMax];
   __shared__ uint32_t s_bin, n_defer;
   __shared__ uint32_t hflags[2];
@@ -1273,6 +1351,23 @@ __global__ void k_compact(const Node* nodes, const uint32_t* __restrict__ finals
 }  // namespace
 
 // ------------------------------------------------------------ launchers
+// Every launcher raises a kernel's dynamic shared-memory limit to the same
+// value, everything the block may use beside its static shared memory:
+// engines on other host threads launch the same kernels with other sizes, and
+// a per-launch value set by one thread could undercut another thread's launch
+// between its set and its launch.
+template <typename K>
+static void allow_max_smem(K* kernel) {
+  int dev = 0, optin = 0;
+  cudaFuncAttributes fa;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess ||
+      cudaFuncGetAttributes(&fa, kernel) != cudaSuccess)
+    return;  // the launch itself reports the failure
+  cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       optin - (int)fa.sharedSizeBytes);
+}
+
 static int choose_c(int W) {
   const int c = (W + 31) / 32;
   if (c <= 1) return 1;
@@ -1290,7 +1385,7 @@ static void count_launch(const ExtractArgs& a, int grid, uint32_t* H, unsigned l
   const uint64_t stride = (uint64_t)a.W + 1;
   const uint32_t lt = (uint32_t)std::max<uint64_t>(16, std::min<uint64_t>(128, 16384 / stride));
   const size_t smem = 128 + 2 * (size_t)tile_buf_bytes(lt, stride) + (size_t)a.F1 * 4 + 256;
-  cudaFuncSetAttribute(k_l1_count<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  allow_max_smem(k_l1_count<C>);
   k_l1_count<C><<<grid, 512, smem, s>>>(a, H, counters, lt);
 }
 
@@ -1341,7 +1436,7 @@ static void scatter_launch(const ExtractArgs& a, int grid, const uint64_t* O, ui
   const int stage_cap = (int)lt * 32 * C;  // >= k-mers of one tile
   static_assert(LPW == (C <= 2 ? 4 : (C <= 8 ? 2 : 1)), "scatter_smem mirrors this tiling");
   const size_t smem = scatter_smem(a.W, a.F1, a.njobs != 0);
-  cudaFuncSetAttribute(k_l1_scatter<C, LPW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  allow_max_smem(k_l1_scatter<C, LPW>);
   k_l1_scatter<C, LPW><<<grid, threads, smem, s>>>(a, O, keys, stage_cap, counters);
 }
 
@@ -1394,7 +1489,7 @@ int launch_tile_scatter(const Node* nodes, const Tile* tiles, uint32_t n_tiles, 
                         uint64_t* B, const uint32_t* TH, int max_width, cudaStream_t s) {
   if (!n_tiles) return 0;
   const size_t smem = (size_t)kTileKeys * 8 + ((size_t)1 << max_width) * 16;
-  cudaFuncSetAttribute(k_tile_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  allow_max_smem(k_tile_scatter);
   k_tile_scatter<<<n_tiles, kTileThreads, smem, s>>>(nodes, tiles, A, B, TH, max_width);
   return 1;
 }
@@ -1405,8 +1500,8 @@ int launch_bin_count(Node* nodes, const uint32_t* final_list, uint32_t n_final, 
                      uint64_t* B, uint32_t* C, int use_hash, unsigned long long* ctr, int sm_count,
                      cudaStream_t s) {
   if (!n_final) return 0;
-  cudaFuncSetAttribute(k_bin_count, cudaFuncAttributeMaxDynamicSharedMemorySize, kBinCap * 8);
-  const uint32_t grid = std::min<uint32_t>(n_final, 2u * (uint32_t)sm_count);
+  allow_max_smem(k_bin_count);
+  const uint32_t grid = std::min<uint32_t>(n_final, (uint32_t)(kBinBlocksPerSM * sm_count));
   k_bin_count<<<grid, kBinThreads, kBinCap * 8, s>>>(nodes, final_list, n_final, A, B, C, ctr,
                                                      use_hash);
   return 1;
@@ -1443,10 +1538,10 @@ int launch_compact(const Node* nodes, const uint32_t* final_list, uint32_t n_fin
 
 #ifdef DK_PHASE_TIMING
 extern "C" int dk_debug_phases(unsigned long long* out) {
-  return (int)cudaMemcpyFromSymbol(out, dk::g_phase, sizeof(unsigned long long) * 16);
+  return (int)cudaMemcpyFromSymbol(out, dk::g_phase, sizeof(unsigned long long) * 32);
 }
 extern "C" int dk_debug_reset() {
-  unsigned long long z[16] = {0};
+  unsigned long long z[32] = {0};
   return (int)cudaMemcpyToSymbol(dk::g_phase, z, sizeof(z));
 }
 #endif

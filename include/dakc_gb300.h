@@ -119,6 +119,8 @@ typedef struct {
   uint64_t launches_kernel[8];
   uint64_t n_partitioned;  /* keys moved by partition levels below level 1    */
   uint64_t n_waves;        /* dk_count_batch: memory-bounded waves run         */
+  uint64_t n_bins_resorted; /* hash variant: bins the hash pass handed to sorting
+                               (too many distinct keys or a long probe run)      */
 } dk_stats;
 
 /* One read set of a batch (dk_count_batch). */
