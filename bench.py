@@ -239,7 +239,9 @@ def run_batched(eng, texts, variant):
             "batched": {"jobs_per_s": len(texts) / t_batch, "kmers_per_s": nk / t_batch,
                         "seconds": t_batch, "waves": st["n_waves"], "ms_device": st["ms_device"],
                         "ms_h2d": st["ms_h2d"], "ms_d2h": st["ms_d2h"],
-                        "kernel_launches": st["kernel_launches"]},
+                        "kernel_launches": st["kernel_launches"],
+                        "kernels_ms": {KERNEL_NAMES[i]: round(float(st["ms_kernel"][i]), 3)
+                                       for i in range(8)}},
             "one_job_per_launch": {"jobs_per_s": len(texts) / t_plain, "kmers_per_s": nk / t_plain,
                                    "seconds": t_plain, "p50_ms": 1e3 * pct(lat, 50),
                                    "p99_ms": 1e3 * pct(lat, 99)},
@@ -306,6 +308,8 @@ def main():
     ap.add_argument("--cpu-reads", type=int, default=4_000_000,
                     help="reads in the CPU baseline's bounded sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="count with the automatic parameters instead of the autotuned ones")
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--mode", default="count", choices=["count", "batch", "serve"],
                     help="count: the headline line; batch / serve: batched and served forms")
@@ -373,6 +377,12 @@ def main():
     torch.cuda.synchronize()
     desc = dk.Engine.desc(rs.line_width, rs.k, variant, dk.RESIDENT_DEVICE, args.l1_bits,
                           args.bin_target)
+    # autotuner (before the warm-up, outside the timed region): counts with
+    # automatic parameters then use the fastest choice it found for this shape
+    tuned = None
+    if not args.no_autotune and variant == dk.VARIANT_AUTO and not args.l1_bits \
+            and not args.bin_target:
+        tuned = eng.autotune(rs.text, rs.line_width, rs.k)
 
     def step():
         t = eng.count_raw(d_text.data_ptr(), nbytes, desc, on_device=True)
@@ -456,8 +466,11 @@ def main():
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "u64",
             "data": "synthetic (seeded generator; ART-simulated datasets are not available)",
-            "config": dict(cfg, variant=args.variant, l2_flush="inputs (3.02 GB) larger than L2",
-                           parallelism=f"replicas x{world}"),
+            "config": dict(cfg, variant=args.variant,
+                           l2_flush=f"inputs ({nbytes / 1e9:.2f} GB) larger than L2",
+                           parallelism=f"replicas x{world}",
+                           autotuned=({k: tuned[k] for k in ("l1_bits", "bin_target", "variant",
+                                                             "candidates")} if tuned else None)),
             "gpu_launches": launches,
             "roofline": {"bound": "hbm", "kernel": KERNEL_NAMES[top], "achieved": achieved,
                          "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,

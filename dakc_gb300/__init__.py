@@ -46,6 +46,7 @@ ABI_SYMBOLS = [
     "dk_count", "dk_count_device", "dk_table_free", "dk_last_stats", "dk_num_lines",
     "dk_host_alloc", "dk_host_free", "dk_count_small_noalloc", "dk_count_batch",
     "dk_serve_start", "dk_submit", "dk_poll", "dk_wait", "dk_cancel", "dk_serve_stop",
+    "dk_autotune", "dk_autotune_reset",
 ]
 
 
@@ -107,6 +108,12 @@ class Stats(ctypes.Structure):
         return d
 
 
+class Tune(ctypes.Structure):
+    _fields_ = [("l1_bits", ctypes.c_int), ("bin_target", ctypes.c_int), ("variant", ctypes.c_int),
+                ("candidates", ctypes.c_int), ("ms_device", ctypes.c_double),
+                ("ms_auto", ctypes.c_double)]
+
+
 _lib = None
 
 
@@ -130,6 +137,8 @@ def load_library(path: str = LIB_PATH):
     lib.dk_count_device.argtypes = [vp, vp, u64, ctypes.POINTER(InputDesc), ctypes.POINTER(Table)]
     lib.dk_table_free.argtypes = [vp, ctypes.POINTER(Table)]
     lib.dk_last_stats.argtypes = [vp, ctypes.POINTER(Stats)]
+    lib.dk_autotune.argtypes = [vp, vp, u64, ctypes.POINTER(InputDesc), ctypes.POINTER(Tune)]
+    lib.dk_autotune_reset.argtypes = [vp]
     lib.dk_num_lines.argtypes = [vp, u64, i32]
     lib.dk_num_lines.restype = ctypes.c_int64
     lib.dk_count_batch.argtypes = [vp, ctypes.POINTER(Job), i32, ctypes.POINTER(InputDesc),
@@ -356,6 +365,21 @@ class Engine:
 
     def cancel(self, ticket: int) -> int:
         return int(self.lib.dk_cancel(self.h, ticket))
+
+    def autotune(self, text, line_width: int, k: int) -> dict:
+        """Time the count of `text` under a few partition / bin / variant
+        choices and keep the fastest for inputs of this shape (dk_autotune);
+        later counts with automatic parameters use it."""
+        ptr, n, keep = _buf_ptr(text)
+        t = Tune()
+        d = self.desc(line_width, k, VARIANT_AUTO)
+        self._check(self.lib.dk_autotune(self.h, ctypes.c_void_p(ptr), n, ctypes.byref(d),
+                                         ctypes.byref(t)), "dk_autotune")
+        del keep
+        return {f: getattr(t, f) for f, _ in t._fields_}
+
+    def autotune_reset(self) -> None:
+        self._check(self.lib.dk_autotune_reset(self.h), "dk_autotune_reset")
 
     def stats(self) -> dict:
         s = Stats()

@@ -568,23 +568,34 @@ int Engine::upload(const char* h, uint64_t nbytes, uint8_t* d) {
 
 // The device pipeline: reads at d_text (nbytes, padded by >= 64 bytes of
 // readable memory) -> sorted table in out (device).  Fills stats.
-int Engine::count_device(const uint8_t* d_text, uint64_t nbytes, const dk_input_desc& desc,
+int Engine::count_device(const uint8_t* d_text, uint64_t nbytes, const dk_input_desc& desc_in,
                          DeviceTable* out, JobSet* js) {
   Engine* e = this;
-  const int W = desc.line_width, k = desc.k;
+  const int W = desc_in.line_width, k = desc_in.k;
   out->n = 0;
   out->n_kmers = 0;
   out->k = nullptr;
   out->c = nullptr;
   stats = dk_stats();
-  // the hash-first bin count needs a free sentinel key, i.e. k <= 31
-  const bool use_hash = desc.variant != DK_VARIANT_SORT && desc.k <= 31;
-  stats.variant_used = use_hash ? DK_VARIANT_HASH : DK_VARIANT_SORT;
   int64_t L0 = js ? (int64_t)js->job_start.back() : frame_lines(nbytes, W);
   if (L0 < 0) {
     set_error("buffer size is not a whole number of lines");
     return DK_ERR_INVALID_ARG;
   }
+  // parameters left automatic take the tuned choice for this input shape
+  dk_input_desc desc = desc_in;
+  if (!js && desc.l1_bits == 0 && desc.bin_target == 0 && desc.variant == DK_VARIANT_AUTO) {
+    const uint64_t pl = (W >= k) ? (uint64_t)(W - k + 1) : 0;
+    const auto it = tunes.find(shape_key(W, k, (uint64_t)L0 * pl));
+    if (it != tunes.end()) {
+      desc.l1_bits = it->second.l1_bits;
+      desc.bin_target = it->second.bin_target;
+      desc.variant = it->second.variant;
+    }
+  }
+  // the hash-first bin count needs a free sentinel key, i.e. k <= 31
+  const bool use_hash = desc.variant != DK_VARIANT_SORT && desc.k <= 31;
+  stats.variant_used = use_hash ? DK_VARIANT_HASH : DK_VARIANT_SORT;
   uint64_t L = (uint64_t)L0;
   launches = 0;
   kev.clear();
@@ -794,6 +805,102 @@ int Engine::count_device(const uint8_t* d_text, uint64_t nbytes, const dk_input_
   return DK_OK;
 }
 
+uint64_t Engine::shape_key(int W, int k, uint64_t n_upper) {
+  return ((uint64_t)W << 16) | ((uint64_t)k << 8) | (uint64_t)ceil_log2(n_upper + 1);
+}
+
+// Time the count of `text` under a small set of parameter choices and keep
+// the fastest for inputs of this shape.  Stages: level-1 bits around the
+// automatic rule (hash variant, default bin size), then the bin size at the
+// best bits, then the other variant at the best pair.  Each choice is timed
+// twice (device time, reads already in device memory) and its best kept.
+int Engine::autotune(const char* text, uint64_t nbytes, const dk_input_desc* desc, dk_tune* out) {
+  Engine* e = this;
+  std::lock_guard<std::mutex> g(mu);
+  if (!desc || (!text && nbytes) || desc->k < 1 || desc->k > 32 || desc->line_width < 1 ||
+      desc->line_width > 1024 || desc->convention != DK_CONV_DAKC) {
+    set_error("invalid autotune arguments");
+    return DK_ERR_INVALID_ARG;
+  }
+  const int W = desc->line_width, k = desc->k;
+  const int64_t L = frame_lines(nbytes, W);
+  if (L < 0) {
+    set_error("buffer size is not a whole number of lines");
+    return DK_ERR_INVALID_ARG;
+  }
+  const uint64_t per_line = W >= k ? (uint64_t)(W - k + 1) : 0;
+  const uint64_t n_upper = (uint64_t)L * per_line;
+  DK_CUDA(cudaSetDevice(device));
+  DK_TRY(Arena::ensure(this, this->text, nbytes + 64));
+  if (nbytes) DK_TRY(upload(text, nbytes, (uint8_t*)this->text.p));
+  uint64_t upper = n_upper;
+  if (k <= 16) upper = std::min<uint64_t>(upper, 1ull << (2 * k));
+  TableBuf* dev_tb = nullptr;
+  DK_TRY(acquire_table(upper, true, &dev_tb));
+  out_k = (uint64_t*)dev_tb->k;
+  out_c = (uint32_t*)dev_tb->c;
+  int timed = 0;
+  auto run = [&](int l1, int tgt, int var, double* ms) -> int {
+    dk_input_desc d = *desc;
+    d.l1_bits = l1;
+    d.bin_target = tgt;
+    d.variant = var;
+    double best = 1e30;
+    for (int rep = 0; rep < 2; ++rep) {
+      DeviceTable dt;
+      const int rc = count_device((const uint8_t*)this->text.p, nbytes, d, &dt);
+      if (rc != DK_OK) return rc;
+      best = std::min(best, stats.ms_device);
+    }
+    ++timed;
+    *ms = best;
+    return DK_OK;
+  };
+  const int hash = k <= 31 ? DK_VARIANT_HASH : DK_VARIANT_SORT;
+  const int max_bits = std::min({kMaxL1Bits, 2 * k, floor_log2_int(l1_max_buckets(W, false))});
+  const int t0 = kBinCap / 2;
+  const int b_auto = std::max(1, std::min(l1_bits_for(n_upper, (double)t0), max_bits));
+  int rc = DK_OK;
+  double ms_auto = 0, best_ms = 0;
+  int best_b = b_auto, best_t = t0, best_v = hash;
+  rc = run(b_auto, t0, hash, &ms_auto);
+  best_ms = ms_auto;
+  for (int b = std::max(1, b_auto - 2); rc == DK_OK && b <= std::min(max_bits, b_auto + 2); ++b) {
+    if (b == b_auto) continue;
+    double ms;
+    rc = run(b, t0, hash, &ms);
+    if (rc == DK_OK && ms < best_ms) { best_ms = ms; best_b = b; }
+  }
+  for (const int tgt : {kBinCap / 4, (3 * kBinCap) / 8}) {
+    if (rc != DK_OK) break;
+    double ms;
+    rc = run(best_b, tgt, hash, &ms);
+    if (rc == DK_OK && ms < best_ms) { best_ms = ms; best_t = tgt; }
+  }
+  if (rc == DK_OK && hash == DK_VARIANT_HASH) {
+    double ms;
+    rc = run(best_b, best_t, DK_VARIANT_SORT, &ms);
+    if (rc == DK_OK && ms < best_ms) { best_ms = ms; best_v = DK_VARIANT_SORT; }
+  }
+  release_table(dev_tb->id);
+  if (rc != DK_OK) return rc;
+  Tune t;
+  t.l1_bits = best_b;
+  t.bin_target = best_t;
+  t.variant = best_v;
+  t.ms = best_ms;
+  tunes[shape_key(W, k, n_upper)] = t;
+  if (out) {
+    out->l1_bits = best_b;
+    out->bin_target = best_t;
+    out->variant = best_v;
+    out->candidates = timed;
+    out->ms_device = best_ms;
+    out->ms_auto = ms_auto;
+  }
+  return DK_OK;
+}
+
 int Engine::count(const char* text, uint64_t nbytes, bool text_on_device, const dk_input_desc* desc,
                   dk_table* out) {
   Engine* e = this;
@@ -982,6 +1089,19 @@ int dk_table_free(dk_ctx* ctx, dk_table* t) {
   const int rc = ctx->eng.release_table(t->handle);
   std::memset(t, 0, sizeof(*t));
   return rc;
+}
+
+int dk_autotune(dk_ctx* ctx, const char* text, uint64_t nbytes, const dk_input_desc* desc,
+                dk_tune* out) {
+  if (!ctx) return DK_ERR_INVALID_ARG;
+  return ctx->eng.autotune(text, nbytes, desc, out);
+}
+
+int dk_autotune_reset(dk_ctx* ctx) {
+  if (!ctx) return DK_ERR_INVALID_ARG;
+  std::lock_guard<std::mutex> g(ctx->eng.mu);
+  ctx->eng.tunes.clear();
+  return DK_OK;
 }
 
 int dk_last_stats(dk_ctx* ctx, dk_stats* out) {

@@ -2,6 +2,7 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <cstdint>
+#include <map>
 #include <mutex>
 #include <string>
 #include <deque>
@@ -105,6 +106,15 @@ struct Engine {
   void* stage_pinned[2] = {nullptr, nullptr};
   cudaEvent_t stage_ev[2] = {nullptr, nullptr};
   int stage_next = 0;
+
+  // tuned (l1_bits, bin_target, variant) per input shape, from dk_autotune
+  struct Tune {
+    int l1_bits = 0, bin_target = 0, variant = 0;
+    double ms = 0;
+  };
+  std::map<uint64_t, Tune> tunes;
+  static uint64_t shape_key(int W, int k, uint64_t n_upper);
+  int autotune(const char* text, uint64_t nbytes, const dk_input_desc* desc, dk_tune* out);
 
   int init(const dk_config* cfg);
   ~Engine();

@@ -65,6 +65,8 @@ constexpr int kBinBlocksPerSM = 2;      // resident bin-count CTAs per SM
 constexpr int kBinDigitBits = 12;       // counting-sort digit of a bin: at most this many bits
 constexpr int kMaxL1Bits = 12;          // level-1 fan-out <= 4096 buckets
 constexpr size_t kMaxSmemPerBlock = 232448;  // opt-in shared memory per block (sm_100 family)
+constexpr int kLineThreads = 256;        // thread-per-line level-1 kernels: lines per tile
+constexpr int kLineMaxW = 256;           // longer lines use the warp-per-line kernels
 
 struct ExtractArgs {
   const uint8_t* text;  // device text, 16-byte aligned

@@ -271,6 +271,187 @@ __global__ void k_l1_offsets_rows(const uint32_t* __restrict__ H, int G, int F1,
   }
 }
 
+// Thread-per-line level-1 passes (lines of at most kLineMaxW bytes).  A tile
+// of blockDim.x lines is staged in shared memory (TMA, double-buffered) and
+// each thread walks one line, rolling its 2-bit key one base at a time.
+// Both passes see the same lines per CTA (lines_of_block) and the same
+// buckets, so the scatter fills exactly the ranges the count reserved.
+
+// One line's rolling state.  step() consumes the byte code of position p and
+// says whether a k-mer ends there (DAKC's rules: 'M' ends the line, any other
+// non-base splits it, and k = 1 keeps a final run only if it starts before
+// W-1, kcounter_funcs.cpp:69-111).
+struct LineRoll {
+  uint64_t key;
+  int run;
+  uint32_t prev;
+  bool stopped;
+  __device__ __forceinline__ void reset() { key = 0; run = 0; prev = 0; stopped = false; }
+  __device__ __forceinline__ bool step(uint32_t c, int p, int W, int k, uint64_t kmask) {
+    if (stopped || c == 0xF0u) { stopped = true; return false; }
+    bool emit = false;
+    if (c >= 4u) {
+      run = 0;
+    } else {
+      key = ((key << 2) | c) & kmask;
+      ++run;
+      emit = run >= k && !(k == 1 && p == W - 1 && (W == 1 || prev == 0xFFu));
+    }
+    prev = c;
+    return emit;
+  }
+};
+
+// Per-line prologue of a tile: is line l parsed, and its bucket rule (batch
+// mode); records NUL-led lines.
+__device__ __forceinline__ bool line_prologue(const ExtractArgs& a, uint64_t l, uint64_t l1,
+                                              const uint8_t* line, JobBucket* jb,
+                                              unsigned long long* counters) {
+  if (l >= l1) return false;
+  if (a.njobs) {
+    const uint32_t job = job_of_line(a, l);
+    if (l >= __ldg(a.job_end + job)) return false;  // past the job's first NUL-led line
+    if (l > __ldg(a.job_start + job) && line[0] == 0) {
+      atomicMin(&a.job_nul[job], (unsigned long long)l);
+      atomicMax(&counters[1], 1ull);
+    }
+    *jb = JobBucket(a, job);
+  } else if (l > 0 && line[0] == 0) {
+    atomicMax(&counters[1], a.n_lines - l);
+  }
+  return true;
+}
+
+__device__ __forceinline__ void setup_tiles(TextTiles* T, const ExtractArgs& a, uint8_t* smraw,
+                                            uint32_t bb) {
+  T->text = a.text;
+  T->nbytes = a.nbytes;
+  T->stride = (uint64_t)a.W + 1;
+  lines_of_block(a.n_lines, &T->lo, &T->hi);
+  T->lt = blockDim.x;
+  T->bar = reinterpret_cast<uint64_t*>(smraw);
+  T->buf[0] = smraw + 128;
+  T->buf[1] = smraw + 128 + bb;
+  if (threadIdx.x == 0) {
+    mbar_init(&T->bar[0], 1);
+    mbar_init(&T->bar[1], 1);
+    fence_barrier_init();
+  }
+}
+
+// COUNT: per-CTA bucket histogram H[cta][bucket] and the k-mer total.
+__global__ void __launch_bounds__(kLineThreads) k_l1_lines_count(ExtractArgs a,
+                                                                 uint32_t* __restrict__ H,
+                                                                 unsigned long long* __restrict__ counters) {
+  extern __shared__ __align__(128) uint8_t smraw[];
+  const int W = a.W, k = a.k;
+  const uint64_t stride = (uint64_t)W + 1;
+  const uint32_t bb = tile_buf_bytes(blockDim.x, stride);
+  uint32_t* cnt = reinterpret_cast<uint32_t*>(smraw + 128 + 2 * bb);  // F1
+  uint8_t* lut = reinterpret_cast<uint8_t*>(cnt + a.F1);              // 256
+  TextTiles T;
+  setup_tiles(&T, a, smraw, bb);
+  for (int b = threadIdx.x; b < a.F1; b += blockDim.x) cnt[b] = 0;
+  init_lut(lut);
+  __syncthreads();
+  uint32_t mine = 0;
+  const uint32_t nt = T.ntiles();
+  if (threadIdx.x == 0 && nt) T.issue(0);
+  for (uint32_t ti = 0; ti < nt; ++ti) {
+    if (threadIdx.x == 0 && ti + 1 < nt) T.issue(ti + 1);
+    const uint8_t* tile = T.acquire(ti, &counters[3]);
+    if (!tile) {
+      T.drain(ti + 1);
+      return;
+    }
+    uint64_t l0, l1;
+    T.range(ti, &l0, &l1);
+    const uint64_t l = l0 + threadIdx.x;
+    const uint8_t* line = tile + (l - l0) * stride;
+    JobBucket jb;
+    if (line_prologue(a, l, l1, line, &jb, counters)) {
+      LineRoll r;
+      r.reset();
+      for (int p0 = 0; p0 < W && !r.stopped; p0 += 4) {
+        uint32_t c4[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) c4[u] = p0 + u < W ? lut[line[p0 + u]] : 0xF0u;
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+          if (r.step(c4[u], p0 + u, W, k, a.kmask)) {
+            atomicAdd(&cnt[a.njobs ? jb(r.key) : (uint32_t)(r.key >> a.shift1)], 1u);
+            ++mine;
+          }
+      }
+    }
+    __syncthreads();  // the buffer is refilled two tiles on
+  }
+#pragma unroll
+  for (int o = 16; o; o >>= 1) mine += __shfl_xor_sync(0xFFFFFFFFu, mine, o);
+  if (lane_id() == 0 && mine) atomicAdd(&counters[0], (unsigned long long)mine);
+  __syncthreads();
+  uint32_t* row = H + (size_t)blockIdx.x * a.F1;
+  for (int b = threadIdx.x; b < a.F1; b += blockDim.x) row[b] = cnt[b];
+}
+
+// Batch-mode scatter: each k-mer goes straight to its bucket at this CTA's
+// cursor, O[cta][bucket] + (its rank among this CTA's keys of the bucket).
+// A wave's jobs own up to 4,096 level-1 buckets, so a tile holds about one
+// key per bucket and staging would not lengthen the runs; writing directly
+// keeps shared memory small (text tiles and cursors only).  Consecutive keys
+// of a bucket land next to each other, so L2 merges the 8-byte stores.
+__global__ void __launch_bounds__(kLineThreads) k_l1_lines_direct(ExtractArgs a,
+                                                                  const uint64_t* __restrict__ O,
+                                                                  uint64_t* __restrict__ keys_out,
+                                                                  unsigned long long* __restrict__ counters) {
+  extern __shared__ __align__(128) uint8_t smraw[];
+  const int W = a.W, k = a.k;
+  const uint64_t stride = (uint64_t)W + 1;
+  const uint32_t bb = tile_buf_bytes(blockDim.x, stride);
+  unsigned long long* cursor = reinterpret_cast<unsigned long long*>(smraw + 128 + 2 * bb);  // F1
+  uint32_t* cnt = reinterpret_cast<uint32_t*>(cursor + a.F1);                                 // F1
+  uint8_t* lut = reinterpret_cast<uint8_t*>(cnt + a.F1);                                      // 256
+  TextTiles T;
+  setup_tiles(&T, a, smraw, bb);
+  for (int b = threadIdx.x; b < a.F1; b += blockDim.x) {
+    cursor[b] = O[(size_t)blockIdx.x * a.F1 + b];
+    cnt[b] = 0;
+  }
+  init_lut(lut);
+  __syncthreads();
+  const uint32_t nt = T.ntiles();
+  if (threadIdx.x == 0 && nt) T.issue(0);
+  for (uint32_t ti = 0; ti < nt; ++ti) {
+    if (threadIdx.x == 0 && ti + 1 < nt) T.issue(ti + 1);
+    const uint8_t* tile = T.acquire(ti, &counters[3]);
+    if (!tile) {
+      T.drain(ti + 1);
+      return;
+    }
+    uint64_t l0, l1;
+    T.range(ti, &l0, &l1);
+    const uint64_t l = l0 + threadIdx.x;
+    const uint8_t* line = tile + (l - l0) * stride;
+    JobBucket jb;
+    if (line_prologue(a, l, l1, line, &jb, counters)) {
+      LineRoll r;
+      r.reset();
+      for (int p0 = 0; p0 < W && !r.stopped; p0 += 4) {
+        uint32_t c4[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) c4[u] = p0 + u < W ? lut[line[p0 + u]] : 0xF0u;
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+          if (r.step(c4[u], p0 + u, W, k, a.kmask)) {
+            const uint32_t b = a.njobs ? jb(r.key) : (uint32_t)(r.key >> a.shift1);
+            keys_out[cursor[b] + atomicAdd(&cnt[b], 1u)] = r.key;
+          }
+      }
+    }
+    __syncthreads();  // the buffer is refilled two tiles on
+  }
+}
+
 template <int C, int LPW>
 __global__ void __launch_bounds__(512, 2) k_l1_scatter(ExtractArgs a, const uint64_t* __restrict__ O,
                                                     uint64_t* __restrict__ keys_out,
@@ -1389,8 +1570,22 @@ static void count_launch(const ExtractArgs& a, int grid, uint32_t* H, unsigned l
   k_l1_count<C><<<grid, 512, smem, s>>>(a, H, counters, lt);
 }
 
+static size_t lines_smem(const ExtractArgs& a, bool scatter) {
+  return 128 + 2 * (size_t)tile_buf_bytes(kLineThreads, (uint64_t)a.W + 1) +
+         (size_t)a.F1 * (scatter ? 12 : 4) + 256;
+}
+
+// batch waves (jobs) with lines the thread-per-line kernels take scatter
+// directly; plain counts stage their tiles (k_l1_scatter)
+static bool direct_scatter(int W, bool jobs) { return jobs && W <= kLineMaxW; }
+
 int launch_l1_count(const ExtractArgs& a, int grid, uint32_t* H, unsigned long long* counters,
                     cudaStream_t s) {
+  if (a.W <= kLineMaxW) {
+    allow_max_smem(k_l1_lines_count);
+    k_l1_lines_count<<<grid, kLineThreads, lines_smem(a, false), s>>>(a, H, counters);
+    return 1;
+  }
   switch (choose_c(a.W)) {
     case 1: count_launch<1>(a, grid, H, counters, s); break;
     case 2: count_launch<2>(a, grid, H, counters, s); break;
@@ -1424,6 +1619,13 @@ static size_t scatter_smem(int W, int F1, bool jobs) {
 
 int l1_max_buckets(int W, bool jobs) {
   int f = 1 << kMaxL1Bits;
+  if (direct_scatter(W, jobs)) {
+    ExtractArgs a{};
+    a.W = W;
+    a.F1 = f;
+    while (f > 1 && lines_smem(a, true) > kMaxSmemPerBlock) a.F1 = (f >>= 1);
+    return f;
+  }
   while (f > 1 && scatter_smem(W, f, jobs) > kMaxSmemPerBlock) f >>= 1;
   return f;
 }
@@ -1442,6 +1644,11 @@ static void scatter_launch(const ExtractArgs& a, int grid, const uint64_t* O, ui
 
 int launch_l1_scatter(const ExtractArgs& a, int grid, const uint64_t* O, uint64_t* keys,
                       unsigned long long* counters, cudaStream_t s) {
+  if (direct_scatter(a.W, a.njobs != 0)) {
+    allow_max_smem(k_l1_lines_direct);
+    k_l1_lines_direct<<<grid, kLineThreads, lines_smem(a, true), s>>>(a, O, keys, counters);
+    return 1;
+  }
   switch (choose_c(a.W)) {
     case 1: scatter_launch<1, 4>(a, grid, O, keys, counters, s); break;
     case 2: scatter_launch<2, 4>(a, grid, O, keys, counters, s); break;

@@ -172,6 +172,32 @@ int64_t dk_num_lines(const char* text, uint64_t nbytes, int line_width);
 int dk_host_alloc(uint64_t nbytes, void** out);
 int dk_host_free(void* p);
 
+/* --- autotuning --------------------------------------------------------- */
+/* The partition's level-1 fan-out, the keys per bin and the per-bin count
+ * variant decide how fast a count runs; their best values depend on the
+ * input's size and k-mer spectrum.  dk_autotune counts `text` (host buffer,
+ * as for dk_count) under a small set of choices -- level-1 bits around the
+ * automatic rule, three bin sizes, both variants -- and keeps the fastest in
+ * the context for inputs of the same shape (line width, k, and size class
+ * ceil(log2(lines * (line_width - k + 1)))).  Later dk_count /
+ * dk_count_device calls whose desc leaves l1_bits = 0, bin_target = 0 and
+ * variant = DK_VARIANT_AUTO use it.  Every choice gives the same table; only
+ * the time differs.  No counterpart in the reference (its bucket sizes are
+ * compile-time constants, common.hpp:36-44). */
+typedef struct {
+  int l1_bits;       /* chosen level-1 partition bits                          */
+  int bin_target;    /* chosen target keys per bin                             */
+  int variant;       /* chosen DK_VARIANT_SORT or DK_VARIANT_HASH              */
+  int candidates;    /* parameter sets timed                                   */
+  double ms_device;  /* device time of the chosen set                          */
+  double ms_auto;    /* device time of the automatic choice                    */
+} dk_tune;
+
+int dk_autotune(dk_ctx* ctx, const char* text, uint64_t nbytes, const dk_input_desc* desc,
+                dk_tune* out);
+/* forget every tuned choice of the context */
+int dk_autotune_reset(dk_ctx* ctx);
+
 /* --- serving ----------------------------------------------------------- */
 /* A request loop over `workers` engine workers (each with its own CUDA
  * stream, device arenas and 1/workers of the context's memory budget).  Jobs

@@ -83,3 +83,11 @@ def test_noalloc_argument_checks_without_gpu():
     assert f(p, 100, 150, 31, p, p, 200, p, None) == dk.DK_ERR_INVALID_ARG      # partial line
     assert f(p, 151 * 200, 150, 31, p, p, 10 ** 6, p, None) == dk.DK_ERR_ADMISSION  # > 12,288
     assert f(p, 151 * 10, 150, 31, p, p, 5, p, None) == dk.DK_ERR_INVALID_ARG   # capacity
+
+
+def test_autotune_rejects_bad_arguments_without_a_device():
+    lib = dk.load_library()
+    d = dk.Engine.desc(150, 31)
+    tune = dk.Tune()
+    assert lib.dk_autotune(None, None, 0, ctypes.byref(d), ctypes.byref(tune)) == dk.DK_ERR_INVALID_ARG
+    assert lib.dk_autotune_reset(None) == dk.DK_ERR_INVALID_ARG
