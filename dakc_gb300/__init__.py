@@ -363,6 +363,21 @@ class Engine:
             raise DkError(rc, "dk_wait timed out")
         return self._take(ticket, rc, t, info)
 
+    def wait_nocopy(self, ticket: int, timeout_ms: int = 60_000):
+        """Like wait(), but the table is released without being copied out:
+        returns (distinct k-mers, k-mer occurrences, job info)."""
+        t, info = Table(), JobInfo()
+        rc = self.lib.dk_wait(self.h, ticket, timeout_ms, ctypes.byref(t), ctypes.byref(info))
+        if rc == DK_ERR_TIMEOUT:
+            raise DkError(rc, "dk_wait timed out")
+        if rc == DK_ERR_PENDING:
+            return None
+        self._inflight.pop(ticket, None)
+        self._check(rc, "served job")
+        n, nk = int(t.n), int(t.n_kmers)
+        self.lib.dk_table_free(self.h, ctypes.byref(t))
+        return n, nk, {f: getattr(info, f) for f, _ in info._fields_}
+
     def cancel(self, ticket: int) -> int:
         return int(self.lib.dk_cancel(self.h, ticket))
 

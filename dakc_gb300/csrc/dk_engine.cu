@@ -87,7 +87,10 @@ void Arena::release(Engine* e, DevBuf& b) {
     if (_rc != DK_OK) return _rc; \
   } while (0)
 
-void Engine::set_error(const std::string& m) { last_error = m; }
+void Engine::set_error(const std::string& m) {
+  std::lock_guard<std::mutex> g(err_mu);
+  last_error = m;
+}
 
 // per-kernel CUDA-event timing on the engine stream; resolved after the final sync
 int Engine::kbegin() {
@@ -146,17 +149,25 @@ int Engine::init(const dk_config* cfg) {
   DK_CUDA(cudaMemGetInfo(&fr, &tot));
   budget = (cfg && cfg->mem_budget) ? cfg->mem_budget : (uint64_t)(0.8 * (double)fr);
   DK_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+  DK_CUDA(cudaStreamCreateWithFlags(&s_in, cudaStreamNonBlocking));
+  DK_CUDA(cudaStreamCreateWithFlags(&s_out, cudaStreamNonBlocking));
+  for (auto* evs : {ev_in0, ev_in1, ev_out0, ev_out1})
+    for (int i = 0; i < 2; ++i) DK_CUDA(cudaEventCreate(&evs[i]));
   for (auto& ev : ev_stage) DK_CUDA(cudaEventCreate(&ev));
   for (auto& ev : kev_pool) DK_CUDA(cudaEventCreate(&ev));
   DK_CUDA(cudaEventCreate(&ev_h2d0));
   DK_CUDA(cudaEventCreate(&ev_d2h1));
-  DK_CUDA(cudaMallocHost(&h_scratch, 256));
+  DK_CUDA(cudaMallocHost(&h_scratch, kMailboxBytes));
+  DK_CUDA(cudaMallocHost(&h_up, kMailboxBytes));
+  DK_CUDA(cudaHostGetDevicePointer(&d_scratch, h_scratch, 0));
+  DK_CUDA(cudaHostGetDevicePointer(&d_up, h_up, 0));
   return DK_OK;
 }
 
 Engine::~Engine() {
-  if (stream) cudaStreamSynchronize(stream);
-  for (DevBuf* b : {&text, &keysA, &keysB, &cnt, &H, &O, &nodes, &tiles, &TH, &finals, &ctrs})
+  for (cudaStream_t st : {stream, s_in, s_out})
+    if (st) cudaStreamSynchronize(st);
+  for (DevBuf* b : {&text, &text2, &keysA, &keysB, &cnt, &H, &O, &nodes, &tiles, &TH, &finals, &ctrs})
     Arena::release(this, *b);
   for (auto& t : tables) {
     if (t.on_device) {
@@ -174,16 +185,41 @@ Engine::~Engine() {
   if (ev_h2d0) cudaEventDestroy(ev_h2d0);
   if (ev_d2h1) cudaEventDestroy(ev_d2h1);
   if (h_scratch) cudaFreeHost(h_scratch);
+  if (h_up) cudaFreeHost(h_up);
   for (auto& s : stage_pinned)
     if (s) cudaFreeHost(s);
-  if (stream) cudaStreamDestroy(stream);
+  for (auto* evs : {ev_in0, ev_in1, ev_out0, ev_out1})
+    for (int i = 0; i < 2; ++i)
+      if (evs[i]) cudaEventDestroy(evs[i]);
+  for (cudaStream_t st : {stream, s_in, s_out})
+    if (st) cudaStreamDestroy(st);
 }
 
+// Read device bytes after the stream's prior work (synchronous): a kernel
+// writes them into the page-locked mailbox.
 int Engine::sync_read(const void* dsrc, size_t bytes, void* hdst) {
   Engine* e = this;
-  DK_CUDA(cudaMemcpyAsync(h_scratch, dsrc, bytes, cudaMemcpyDeviceToHost, stream));
-  DK_CUDA(cudaStreamSynchronize(stream));
-  std::memcpy(hdst, h_scratch, bytes);
+  for (size_t off = 0; off < bytes; off += kMailboxBytes) {
+    const size_t n = std::min(kMailboxBytes, bytes - off);
+    launch_copy_small((const uint8_t*)dsrc + off, d_scratch, n, stream);
+    DK_CUDA(cudaGetLastError());
+    DK_CUDA(cudaStreamSynchronize(stream));
+    std::memcpy((uint8_t*)hdst + off, h_scratch, n);
+  }
+  return DK_OK;
+}
+
+// Write host bytes to device memory, ordered on the stream and complete on
+// return: a kernel reads them from the page-locked mailbox.
+int Engine::write_small(void* ddst, const void* hsrc, size_t bytes) {
+  Engine* e = this;
+  for (size_t off = 0; off < bytes; off += kMailboxBytes) {
+    const size_t n = std::min(kMailboxBytes, bytes - off);
+    std::memcpy(h_up, (const uint8_t*)hsrc + off, n);
+    launch_copy_small(d_up, (uint8_t*)ddst + off, n, stream);
+    DK_CUDA(cudaGetLastError());
+    DK_CUDA(cudaStreamSynchronize(stream));  // the mailbox is refilled next
+  }
   return DK_OK;
 }
 
@@ -265,30 +301,36 @@ static int floor_log2_int(int v) {
 }
 
 // ------------------------------------------------------------ batch mode
+// The job arrays live back to back in the engine's job arena (d_start ...
+// d_bits), so one mailbox copy uploads them all.
 int JobSet::upload_bounds(Engine* e) {
   const size_t n = (size_t)njobs;
-  std::vector<uint64_t> nul(job_start.begin() + 1, job_start.end());
-  DK_CUDA(cudaMemcpyAsync(d_start, job_start.data(), (n + 1) * 8, cudaMemcpyHostToDevice, e->stream));
-  DK_CUDA(cudaMemcpyAsync(d_end, job_end.data(), n * 8, cudaMemcpyHostToDevice, e->stream));
-  DK_CUDA(cudaMemcpyAsync(d_nul, nul.data(), n * 8, cudaMemcpyHostToDevice, e->stream));
-  DK_CUDA(cudaMemcpyAsync(d_base, job_base.data(), (n + 1) * 4, cudaMemcpyHostToDevice, e->stream));
-  DK_CUDA(cudaMemcpyAsync(d_bits, job_bits.data(), n, cudaMemcpyHostToDevice, e->stream));
-  DK_CUDA(cudaMemcpyAsync(d_bshift, bucket_shift.data(), bucket_shift.size() * 2,
-                          cudaMemcpyHostToDevice, e->stream));
-  DK_CUDA(cudaStreamSynchronize(e->stream));  // host vectors are pageable and short-lived
-  return DK_OK;
+  std::vector<uint8_t> blob((uint8_t*)(d_bits + n) - (uint8_t*)d_start);
+  auto put = [&](const void* dptr, const void* src, size_t bytes) {
+    std::memcpy(blob.data() + ((const uint8_t*)dptr - (const uint8_t*)d_start), src, bytes);
+  };
+  put(d_start, job_start.data(), (n + 1) * 8);
+  put(d_end, job_end.data(), n * 8);
+  put(d_nul, job_start.data() + 1, n * 8);  // no NUL-led line found yet
+  put(d_base, job_base.data(), (n + 1) * 4);
+  put(d_bshift, bucket_shift.data(), bucket_shift.size() * 2);
+  put(d_bits, job_bits.data(), n);
+  return e->write_small(d_start, blob.data(), blob.size());
 }
 
 int JobSet::apply_nul(Engine* e) {
   std::vector<uint64_t> nul((size_t)njobs);
-  DK_CUDA(cudaMemcpyAsync(nul.data(), d_nul, (size_t)njobs * 8, cudaMemcpyDeviceToHost, e->stream));
-  DK_CUDA(cudaStreamSynchronize(e->stream));
+  DK_TRY(e->sync_read(d_nul, (size_t)njobs * 8, nul.data()));
   for (int j = 0; j < njobs; ++j) job_end[j] = std::min(job_end[j], nul[j]);
   return DK_OK;
 }
 
 // Count many read sets in memory-bounded waves; each wave is one pass of the
-// device pipeline in which every job is its own level-1 bucket.
+// device pipeline in which every job owns its own level-1 buckets.  Waves are
+// pipelined over three streams: while wave w is counted (`stream`), a helper
+// thread stages and uploads wave w+1 into the other text buffer (`s_in`), and
+// wave w-1's table is copied back to the host (`s_out`).  Large batches are
+// cut into at least four waves so that the three stages overlap.
 int Engine::count_batch(const dk_job* jobs, int njobs, const dk_input_desc* desc, dk_table* outs) {
   Engine* e = this;
   std::lock_guard<std::mutex> g(mu);
@@ -317,144 +359,214 @@ int Engine::count_batch(const dk_job* jobs, int njobs, const dk_input_desc* desc
     lines[j] = (uint64_t)L;
   }
   DK_CUDA(cudaSetDevice(device));
-  // device bytes per job: text + two key buffers + staged counts + table
-  auto est = [&](int j) { return lines[j] * stride + 32 * lines[j] * per_line + 4096; };
-  const uint64_t wave_cap = budget ? (uint64_t)(0.7 * (double)budget) : ~0ull;
-  stats_batch = dk_stats();
-  double ms_device = 0, ms_h2d = 0, ms_d2h = 0;
-  uint64_t launches_total = 0;
+  // device bytes per job while its wave runs: text in two buffers, two key
+  // buffers, staged counts, a device table and one in flight to the host
+  auto est = [&](int j) { return 2 * lines[j] * stride + 44 * lines[j] * per_line + 4096; };
+  uint64_t total = 0;
+  for (int j = 0; j < njobs; ++j) total += est(j);
+  const uint64_t mem_cap = budget ? (uint64_t)(0.7 * (double)budget) : ~0ull;
+  const uint64_t wave_cap = std::min(mem_cap, std::max<uint64_t>(total / 4, 256ull << 20));
   const int max_wave_jobs = l1_max_buckets(W, true);  // every job needs one bucket at least
-  int j0 = 0;
-  while (j0 < njobs) {
-    // greedy wave: consecutive jobs while they fit the budget and the bucket limit
+  const double target = (double)((desc->bin_target > 0) ? std::min(desc->bin_target, kBinCap / 2)
+                                                        : kBinCap / 2);
+  struct Wave {
+    int j0 = 0, j1 = 0;
+    JobSet js;
+    std::vector<Seg> segs;
+    uint64_t bytes = 0;
+  };
+  std::vector<Wave> waves;
+  uint64_t max_bytes = 0;
+  for (int j0 = 0; j0 < njobs;) {
     int j1 = j0;
     uint64_t bytes = 0;
     while (j1 < njobs && j1 - j0 < max_wave_jobs && (j1 == j0 || bytes + est(j1) <= wave_cap)) {
       bytes += est(j1);
       ++j1;
     }
-    if (bytes > wave_cap) {
+    if (bytes > mem_cap) {
       set_error("job " + std::to_string(j0) + " alone exceeds the memory budget");
       return DK_ERR_ADMISSION;
     }
+    Wave wv;
+    wv.j0 = j0;
+    wv.j1 = j1;
     const int nj = j1 - j0;
-    JobSet js;
+    JobSet& js = wv.js;
     js.njobs = nj;
     js.job_start.assign(nj + 1, 0);
     for (int j = 0; j < nj; ++j) js.job_start[j + 1] = js.job_start[j] + lines[j0 + j];
     js.job_end.assign(js.job_start.begin() + 1, js.job_start.end());
-    const uint64_t total_lines = js.job_start[nj];
-    const uint64_t wave_bytes = total_lines * stride;
     // level-1 buckets per job: the plain count's split, capped so the wave's
     // buckets fit the scatter kernel (largest jobs give up bits first)
-    {
-      const int max_f1 = l1_max_buckets(W, true);
-      const double target = (double)((desc->bin_target > 0)
-                                         ? std::min(desc->bin_target, kBinCap / 2) : kBinCap / 2);
-      std::vector<int> want(nj);
-      for (int j = 0; j < nj; ++j) {
-        int b = desc->l1_bits > 0 ? desc->l1_bits : l1_bits_for(lines[j0 + j] * per_line, target);
-        want[j] = std::max(0, std::min({b, kMaxL1Bits, 2 * k}));
-      }
-      int cap = floor_log2_int(max_f1);
-      for (;; --cap) {
-        uint64_t tot = 0;
-        for (int j = 0; j < nj; ++j) tot += 1ull << std::min(want[j], cap);
-        if (tot <= (uint64_t)max_f1 || cap == 0) break;
-      }
-      js.job_bits.resize(nj);
-      js.job_base.assign(nj + 1, 0);
-      for (int j = 0; j < nj; ++j) {
-        js.job_bits[j] = (uint8_t)std::min(want[j], cap);
-        js.job_base[j + 1] = js.job_base[j] + (1u << js.job_bits[j]);
-      }
-      js.bucket_shift.resize(js.job_base[nj]);
-      for (int j = 0; j < nj; ++j)
-        for (uint32_t b = js.job_base[j]; b < js.job_base[j + 1]; ++b)
-          js.bucket_shift[b] = (int16_t)(2 * k - js.job_bits[j]);
+    std::vector<int> want(nj);
+    for (int j = 0; j < nj; ++j) {
+      const int b = desc->l1_bits > 0 ? desc->l1_bits : l1_bits_for(lines[j0 + j] * per_line, target);
+      want[j] = std::max(0, std::min({b, kMaxL1Bits, 2 * k}));
     }
-    const int F1 = js.F1();
-    DK_TRY(Arena::ensure(this, text, wave_bytes + 64));
-    DK_TRY(Arena::ensure(this, jobmeta, (size_t)(3 * nj + 1) * 8 + (size_t)(nj + 1) * 4 + nj +
-                                            (size_t)F1 * 2 + 64));
-    js.d_start = (uint64_t*)jobmeta.p;
-    js.d_end = js.d_start + nj + 1;
-    js.d_nul = (unsigned long long*)(js.d_end + nj);
-    js.d_base = (uint32_t*)(js.d_nul + nj);
-    js.d_bshift = (int16_t*)(js.d_base + nj + 1);
-    js.d_bits = (uint8_t*)(js.d_bshift + F1);
-    DK_CUDA(cudaEventRecord(ev_h2d0, stream));
-    std::vector<Seg> segs;
+    int cap = floor_log2_int(max_wave_jobs);
+    for (;; --cap) {
+      uint64_t tot = 0;
+      for (int j = 0; j < nj; ++j) tot += 1ull << std::min(want[j], cap);
+      if (tot <= (uint64_t)max_wave_jobs || cap == 0) break;
+    }
+    js.job_bits.resize(nj);
+    js.job_base.assign(nj + 1, 0);
+    for (int j = 0; j < nj; ++j) {
+      js.job_bits[j] = (uint8_t)std::min(want[j], cap);
+      js.job_base[j + 1] = js.job_base[j] + (1u << js.job_bits[j]);
+    }
+    js.bucket_shift.resize(js.job_base[nj]);
+    for (int j = 0; j < nj; ++j)
+      for (uint32_t b = js.job_base[j]; b < js.job_base[j + 1]; ++b)
+        js.bucket_shift[b] = (int16_t)(2 * k - js.job_bits[j]);
     for (int j = 0; j < nj; ++j)
       if (jobs[j0 + j].nbytes)
-        segs.push_back(Seg{jobs[j0 + j].text, jobs[j0 + j].nbytes, js.job_start[j] * stride});
-    DK_TRY(upload_segments(segs, (uint8_t*)text.p));
-    TableBuf* dev_tb = nullptr;
-    DK_TRY(acquire_table(total_lines * per_line, true, &dev_tb));
-    out_k = (uint64_t*)dev_tb->k;
-    out_c = (uint32_t*)dev_tb->c;
-    DeviceTable dt;
-    int rc = count_device((const uint8_t*)text.p, wave_bytes, *desc, &dt, &js);
-    if (rc != DK_OK) {
-      release_table(dev_tb->id);
-      return rc;
-    }
-    float t_h2d = 0;
-    cudaEventElapsedTime(&t_h2d, ev_h2d0, ev_stage[0]);
-    ms_h2d += t_h2d;
-    ms_device += stats.ms_device;
-    launches_total += stats.kernel_launches;
-    for (int q = 0; q < 8; ++q) {
-      stats_batch.ms_kernel[q] += stats.ms_kernel[q];
-      stats_batch.launches_kernel[q] += stats.launches_kernel[q];
-      stats_batch.ms_stage[q] += stats.ms_stage[q];
-    }
-    stats_batch.n_kmers += stats.n_kmers;
-    stats_batch.n_distinct += stats.n_distinct;
-    stats_batch.n_lines += stats.n_lines;
-    stats_batch.n_bins += stats.n_bins;
-    stats_batch.n_partitioned += stats.n_partitioned;
-    stats_batch.n_bins_resorted += stats.n_bins_resorted;
-    stats_batch.partition_levels = std::max(stats_batch.partition_levels, stats.partition_levels);
-    stats_batch.variant_used = stats.variant_used;
-    TableBuf* h_tb = nullptr;
-    rc = acquire_table(std::max<uint64_t>(dt.n, 1), false, &h_tb);
-    if (rc != DK_OK) {
-      release_table(dev_tb->id);
-      return rc;
-    }
-    if (dt.n) {
-      DK_CUDA(cudaMemcpyAsync(h_tb->k, dev_tb->k, dt.n * 8, cudaMemcpyDeviceToHost, stream));
-      DK_CUDA(cudaMemcpyAsync(h_tb->c, dev_tb->c, dt.n * 4, cudaMemcpyDeviceToHost, stream));
-    }
-    DK_CUDA(cudaEventRecord(ev_d2h1, stream));
-    DK_CUDA(cudaEventSynchronize(ev_d2h1));
-    float t_d2h = 0;
-    cudaEventElapsedTime(&t_d2h, ev_stage[5], ev_d2h1);
-    if (dt.n) ms_d2h += t_d2h;
-    release_table(dev_tb->id);
-    h_tb->refs = (uint32_t)nj;
-    for (int j = 0; j < nj; ++j) {
-      dk_table& t = outs[j0 + j];
-      const bool has = !js.nodes.empty();
-      uint64_t d = 0, n = 0, off = 0;
-      if (has) {  // a job's buckets are consecutive in key order: its table is one run
-        off = js.nodes[js.job_base[j]].out_off;
-        for (uint32_t b = js.job_base[j]; b < js.job_base[j + 1]; ++b) {
-          d += js.nodes[b].d;
-          n += js.nodes[b].n;
-        }
-      }
-      t.kmers = (uint64_t*)h_tb->k + off;
-      t.counts = (uint32_t*)h_tb->c + off;
-      t.n = d;
-      t.n_kmers = n;
-      t.on_device = 0;
-      t.variant_used = stats.variant_used;
-      t.handle = h_tb->id;
-    }
+        wv.segs.push_back(Seg{jobs[j0 + j].text, jobs[j0 + j].nbytes, js.job_start[j] * stride});
+    wv.bytes = js.job_start[nj] * stride;
+    max_bytes = std::max(max_bytes, wv.bytes);
+    waves.push_back(std::move(wv));
     j0 = j1;
-    ++stats_batch.n_waves;
+  }
+  stats_batch = dk_stats();
+  if (waves.empty()) {
+    stats = stats_batch;
+    return DK_OK;
+  }
+  // both text buffers are sized here, on this thread: the helper only copies
+  DevBuf* tbuf[2] = {&text, &text2};
+  DK_TRY(Arena::ensure(this, text, max_bytes + 64));
+  if (waves.size() > 1) DK_TRY(Arena::ensure(this, text2, max_bytes + 64));
+  auto stage = [this, &waves, &tbuf](size_t w) -> int {
+    Engine* e = this;
+    DK_CUDA(cudaSetDevice(device));
+    const int b = (int)(w & 1);
+    DK_CUDA(cudaEventRecord(ev_in0[b], s_in));
+    DK_TRY(upload_segments(waves[w].segs, (uint8_t*)tbuf[b]->p, s_in));
+    DK_CUDA(cudaEventRecord(ev_in1[b], s_in));
+    return DK_OK;
+  };
+  double ms_device = 0, ms_h2d = 0, ms_d2h = 0;
+  uint64_t launches_total = 0;
+  TableBuf* dev_tb[2] = {nullptr, nullptr};  // device tables whose download may be in flight
+  bool out_pending[2] = {false, false};
+  int rc = stage(0);
+  std::thread helper;
+  int helper_rc = DK_OK;
+  auto finish_download = [&](int b) -> int {
+    if (!out_pending[b]) return DK_OK;
+    DK_CUDA(cudaEventSynchronize(ev_out1[b]));
+    float t = 0;
+    cudaEventElapsedTime(&t, ev_out0[b], ev_out1[b]);
+    ms_d2h += t;
+    release_table(dev_tb[b]->id);
+    dev_tb[b] = nullptr;
+    out_pending[b] = false;
+    return DK_OK;
+  };
+  for (size_t w = 0; rc == DK_OK && w < waves.size(); ++w) {
+    const int b = (int)(w & 1);
+    Wave& wv = waves[w];
+    JobSet& js = wv.js;
+    const int nj = wv.j1 - wv.j0;
+    // wave w+1 streams in while wave w runs (its buffer's last reader, wave
+    // w-1, has finished: count_device returns after its kernels complete)
+    if (w + 1 < waves.size()) {
+      helper = std::thread([&stage, &helper_rc, w] { helper_rc = stage(w + 1); });
+    }
+    rc = finish_download(b);  // the table buffer of wave w-2
+    if (rc == DK_OK) rc = [&]() -> int {
+      DK_CUDA(cudaStreamWaitEvent(stream, ev_in1[b], 0));
+      DK_TRY(Arena::ensure(this, jobmeta, (size_t)(3 * nj + 1) * 8 + (size_t)(nj + 1) * 4 + nj +
+                                              (size_t)js.F1() * 2 + 64));
+      js.d_start = (uint64_t*)jobmeta.p;
+      js.d_end = js.d_start + nj + 1;
+      js.d_nul = (unsigned long long*)(js.d_end + nj);
+      js.d_base = (uint32_t*)(js.d_nul + nj);
+      js.d_bshift = (int16_t*)(js.d_base + nj + 1);
+      js.d_bits = (uint8_t*)(js.d_bshift + js.F1());
+      DK_TRY(acquire_table(js.job_start[nj] * per_line, true, &dev_tb[b]));
+      out_k = (uint64_t*)dev_tb[b]->k;
+      out_c = (uint32_t*)dev_tb[b]->c;
+      DeviceTable dt;
+      int r = count_device((const uint8_t*)tbuf[b]->p, wv.bytes, *desc, &dt, &js);
+      if (r != DK_OK) {
+        release_table(dev_tb[b]->id);
+        dev_tb[b] = nullptr;
+        return r;
+      }
+      float t_in = 0;
+      cudaEventElapsedTime(&t_in, ev_in0[b], ev_in1[b]);
+      ms_h2d += t_in;
+      ms_device += stats.ms_device;
+      launches_total += stats.kernel_launches;
+      for (int q = 0; q < 8; ++q) {
+        stats_batch.ms_kernel[q] += stats.ms_kernel[q];
+        stats_batch.launches_kernel[q] += stats.launches_kernel[q];
+        stats_batch.ms_stage[q] += stats.ms_stage[q];
+      }
+      stats_batch.n_kmers += stats.n_kmers;
+      stats_batch.n_distinct += stats.n_distinct;
+      stats_batch.n_lines += stats.n_lines;
+      stats_batch.n_bins += stats.n_bins;
+      stats_batch.n_partitioned += stats.n_partitioned;
+      stats_batch.n_bins_resorted += stats.n_bins_resorted;
+      stats_batch.partition_levels = std::max(stats_batch.partition_levels, stats.partition_levels);
+      stats_batch.variant_used = stats.variant_used;
+      // the wave's table goes back on s_out while the next wave runs
+      TableBuf* h_tb = nullptr;
+      r = acquire_table(std::max<uint64_t>(dt.n, 1), false, &h_tb);
+      if (r != DK_OK) {
+        release_table(dev_tb[b]->id);
+        dev_tb[b] = nullptr;
+        return r;
+      }
+      DK_CUDA(cudaEventRecord(ev_stage[7], stream));
+      DK_CUDA(cudaStreamWaitEvent(s_out, ev_stage[7], 0));
+      DK_CUDA(cudaEventRecord(ev_out0[b], s_out));
+      if (dt.n) {
+        DK_CUDA(cudaMemcpyAsync(h_tb->k, dev_tb[b]->k, dt.n * 8, cudaMemcpyDeviceToHost, s_out));
+        DK_CUDA(cudaMemcpyAsync(h_tb->c, dev_tb[b]->c, dt.n * 4, cudaMemcpyDeviceToHost, s_out));
+      }
+      DK_CUDA(cudaEventRecord(ev_out1[b], s_out));
+      out_pending[b] = true;
+      h_tb->refs = (uint32_t)nj;
+      for (int j = 0; j < nj; ++j) {
+        dk_table& t = outs[wv.j0 + j];
+        const bool has = !js.nodes.empty();
+        uint64_t d = 0, n = 0, off = 0;
+        if (has) {  // a job's buckets are consecutive in key order: its table is one run
+          off = js.nodes[js.job_base[j]].out_off;
+          for (uint32_t q = js.job_base[j]; q < js.job_base[j + 1]; ++q) {
+            d += js.nodes[q].d;
+            n += js.nodes[q].n;
+          }
+        }
+        t.kmers = (uint64_t*)h_tb->k + off;
+        t.counts = (uint32_t*)h_tb->c + off;
+        t.n = d;
+        t.n_kmers = n;
+        t.on_device = 0;
+        t.variant_used = stats.variant_used;
+        t.handle = h_tb->id;
+      }
+      ++stats_batch.n_waves;
+      return DK_OK;
+    }();
+    if (helper.joinable()) helper.join();
+    if (rc == DK_OK) rc = helper_rc;
+  }
+  if (helper.joinable()) helper.join();
+  // every download completes before the tables are handed out
+  for (int b = 0; b < 2; ++b) {
+    const int r = finish_download(b);
+    if (rc == DK_OK) rc = r;
+  }
+  if (rc != DK_OK) {
+    for (int j = 0; j < njobs; ++j)
+      if (outs[j].handle) release_table(outs[j].handle);
+    for (int j = 0; j < njobs; ++j) std::memset(&outs[j], 0, sizeof(dk_table));
+    return rc;
   }
   stats_batch.ms_device = ms_device;
   stats_batch.ms_h2d = ms_h2d;
@@ -500,7 +612,7 @@ static void gather_range(const std::vector<Engine::Seg>& segs, uint64_t dst_lo, 
 // so it never overwrites a pinned segment's bytes; bytes inside a run that no
 // segment covers are missing final terminators, which are never examined.  A
 // slot is refilled only after the copy that last read it has finished.
-int Engine::upload_segments(const std::vector<Seg>& all, uint8_t* d) {
+int Engine::upload_segments(const std::vector<Seg>& all, uint8_t* d, cudaStream_t st) {
   Engine* e = this;
   struct S {
     Seg sg;
@@ -513,7 +625,7 @@ int Engine::upload_segments(const std::vector<Seg>& all, uint8_t* d) {
   bool any_pageable = false;
   for (const S& x : v) {
     if (x.pinned) {
-      DK_CUDA(cudaMemcpyAsync(d + x.sg.doff, x.sg.h, x.sg.n, cudaMemcpyHostToDevice, stream));
+      DK_CUDA(cudaMemcpyAsync(d + x.sg.doff, x.sg.h, x.sg.n, cudaMemcpyHostToDevice, st));
     } else {
       any_pageable = true;
     }
@@ -525,7 +637,7 @@ int Engine::upload_segments(const std::vector<Seg>& all, uint8_t* d) {
     if (!stage_ev[i]) DK_CUDA(cudaEventCreateWithFlags(&stage_ev[i], cudaEventDisableTiming));
   }
   const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
-  const int nthreads = (int)std::min<unsigned>(8, std::max(1u, hw / 2));
+  const int nthreads = (int)std::min<unsigned>(16, std::max(1u, hw - 1));
   size_t r0 = 0;
   while (r0 < v.size()) {
     if (v[r0].pinned) { ++r0; continue; }
@@ -552,8 +664,8 @@ int Engine::upload_segments(const std::vector<Seg>& all, uint8_t* d) {
         }
         for (auto& t : th) t.join();
       }
-      DK_CUDA(cudaMemcpyAsync(d + lo, buf, len, cudaMemcpyHostToDevice, stream));
-      DK_CUDA(cudaEventRecord(stage_ev[i], stream));
+      DK_CUDA(cudaMemcpyAsync(d + lo, buf, len, cudaMemcpyHostToDevice, st));
+      DK_CUDA(cudaEventRecord(stage_ev[i], st));
       lo = hi;
       stage_next ^= 1;
     }
@@ -563,7 +675,7 @@ int Engine::upload_segments(const std::vector<Seg>& all, uint8_t* d) {
 }
 
 int Engine::upload(const char* h, uint64_t nbytes, uint8_t* d) {
-  return upload_segments({Seg{h, nbytes, 0}}, d);
+  return upload_segments({Seg{h, nbytes, 0}}, d, stream);
 }
 
 // The device pipeline: reads at d_text (nbytes, padded by >= 64 bytes of
@@ -784,8 +896,7 @@ int Engine::count_device(const uint8_t* d_text, uint64_t nbytes, const dk_input_
   DK_CUDA(cudaGetLastError());
   if (js) {
     js->nodes.resize(F1);
-    DK_CUDA(cudaMemcpyAsync(js->nodes.data(), nodes.p, (size_t)F1 * sizeof(Node),
-                            cudaMemcpyDeviceToHost, stream));
+    DK_TRY(sync_read(nodes.p, (size_t)F1 * sizeof(Node), js->nodes.data()));
   }
   DK_CUDA(cudaEventRecord(ev_stage[5], stream));
   DK_CUDA(cudaEventSynchronize(ev_stage[5]));

@@ -77,15 +77,17 @@ struct Engine {
   int sm_count = 0;
   uint64_t budget = 0;
   uint64_t dev_bytes = 0, dev_peak = 0;
-  cudaStream_t stream = nullptr;
+  cudaStream_t stream = nullptr;            // kernels
+  cudaStream_t s_in = nullptr, s_out = nullptr;  // batch uploads / table downloads
   std::mutex mu;
+  std::mutex err_mu;                         // last_error (batch uploads run on a helper thread)
   std::string last_error;
   dk_stats stats{};
   dk_stats stats_batch{};
   uint64_t launches = 0;
 
   // device arenas
-  DevBuf text, keysA, keysB, cnt, H, O, nodes, tiles, TH, finals, ctrs;
+  DevBuf text, text2, keysA, keysB, cnt, H, O, nodes, tiles, TH, finals, ctrs;
   size_t node_cap_needed = 0;
   uint64_t* out_k = nullptr;
   uint32_t* out_c = nullptr;
@@ -102,9 +104,18 @@ struct Engine {
   void kend(int slot, int i0, int n);
   void kresolve();
   cudaEvent_t ev_h2d0 = nullptr, ev_d2h1 = nullptr;
-  void* h_scratch = nullptr;
+  // page-locked mailboxes for the engine's small control copies, moved by a
+  // kernel (launch_copy_small) instead of a copy engine
+  static constexpr size_t kMailboxBytes = 1 << 20;
+  void* h_scratch = nullptr;  // device -> host
+  void* h_up = nullptr;       // host -> device
+  void* d_scratch = nullptr;  // device views of the two
+  void* d_up = nullptr;
+  int write_small(void* ddst, const void* hsrc, size_t bytes);  // synchronous
   void* stage_pinned[2] = {nullptr, nullptr};
   cudaEvent_t stage_ev[2] = {nullptr, nullptr};
+  // batch pipeline: per text/table buffer, upload start/end and download start/end
+  cudaEvent_t ev_in0[2] = {}, ev_in1[2] = {}, ev_out0[2] = {}, ev_out1[2] = {};
   int stage_next = 0;
 
   // tuned (l1_bits, bin_target, variant) per input shape, from dk_autotune
@@ -126,7 +137,7 @@ struct Engine {
     uint64_t doff;  // destination offset
   };
   int upload(const char* h, uint64_t nbytes, uint8_t* d);
-  int upload_segments(const std::vector<Seg>& segs, uint8_t* d);
+  int upload_segments(const std::vector<Seg>& segs, uint8_t* d, cudaStream_t st);
   int acquire_table(uint64_t n, bool on_device, TableBuf** out);
   int release_table(uint64_t id);
   int count_device(const uint8_t* d_text, uint64_t nbytes, const dk_input_desc& desc,

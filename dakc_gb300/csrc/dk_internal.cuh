@@ -99,6 +99,9 @@ int launch_l1_count(const ExtractArgs& a, int grid, uint32_t* H, unsigned long l
 // bucket_shift (optional, F1 entries): per-bucket free bits in batch mode
 int launch_l1_scan(const uint32_t* H, int grid, int F1, uint64_t* O, Node* nodes, int shift1,
                    const int16_t* bucket_shift, cudaStream_t s);
+// copy `bytes` between device memory and page-locked host memory with a kernel
+int launch_copy_small(const void* src, void* dst, uint64_t bytes, cudaStream_t s);
+
 // largest level-1 fan-out (power of two <= 2^kMaxL1Bits) whose scatter kernel
 // fits the per-block shared-memory limit for line width W
 int l1_max_buckets(int W, bool jobs);

@@ -671,10 +671,23 @@ __global__ void __launch_bounds__(256) k_node_scan(Node* nodes, uint32_t lo, con
   const uint32_t R = 1u << nd.width;
   for (uint32_t j = threadIdx.x; j < R; j += blockDim.x) {
     uint32_t run = 0;
-    for (uint32_t t = 0; t < nd.ntiles; ++t) {
-      uint32_t* p = TH + nd.th_base + (uint64_t)t * R + j;
-      const uint32_t c = *p;
-      *p = run;
+    uint32_t* col = TH + nd.th_base + j;
+    // eight tiles at a time: their loads are independent, only the running
+    // sum is serial
+    uint32_t t = 0;
+    for (; t + 8 <= nd.ntiles; t += 8) {
+      uint32_t c[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) c[u] = col[(uint64_t)(t + u) * R];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        col[(uint64_t)(t + u) * R] = run;
+        run += c[u];
+      }
+    }
+    for (; t < nd.ntiles; ++t) {
+      const uint32_t c = col[(uint64_t)t * R];
+      col[(uint64_t)t * R] = run;
       run += c;
     }
     csize[j] = run;
@@ -1218,21 +1231,7 @@ static_assert(kHashSlots * 12 + kHashMaxDistinct * 12 <= kBinCap * 8,
               "table and sorted pairs share the bin's shared-memory region");
 static_assert(kBinCap >= (1 << kDenseBits) * 8 / 8, "a dense bin's 2^kDenseBits u64 counters fit the region");
 
-// (key, count) pair versions of the warp sorts
-__device__ void warp_rank_sort_pairs(unsigned long long* s, uint32_t* c, uint32_t m) {
-  const uint32_t lane = lane_id();
-  const unsigned long long v = lane < m ? s[lane] : 0ull;
-  const uint32_t vc = lane < m ? c[lane] : 0u;
-  uint32_t rank = 0;
-  for (uint32_t j = 0; j < m; ++j) {
-    const unsigned long long o = __shfl_sync(0xFFFFFFFFu, v, j);
-    rank += (o < v) || (o == v && j < lane);
-  }
-  __syncwarp();
-  if (lane < m) { s[rank] = v; c[rank] = vc; }
-  __syncwarp();
-}
-
+// (key, count) pair version of the warp bitonic sort
 __device__ void warp_bitonic_pairs(unsigned long long* s, uint32_t* c, uint32_t m) {
   int lg = 0;
   while ((1u << lg) < m) ++lg;
@@ -1265,9 +1264,10 @@ __device__ void warp_bitonic_pairs(unsigned long long* s, uint32_t* c, uint32_t 
 
 // Aggregate the bin's keys in a shared-memory open-addressing table (linear
 // probing on a multiplicative hash, 64-bit atomicCAS on the key, atomicAdd on
-// its count), counting-sort the distinct (key, count) pairs on their top free
-// bits, sort the digit ranges holding several keys (a thread per small range,
-// a warp per large one) and write the pairs over the bin's own key range.
+// its count; a new key also counts its digit, the top D free bits), place the
+// distinct (key, count) pairs by digit (counting sort), and write each pair
+// at its rank inside its digit range, found by comparing it with the range's
+// other keys (ranges of more than 32 keys are sorted by a warp instead).
 // Returns false, having written nothing, when a probe runs past
 // kHashMaxProbe slots or the bin holds more than kHashMaxDistinct keys.
 __device__ bool bin_hashed(Node* nodes, uint32_t ni, const Node& nd, uint64_t* keys, uint32_t* cnt,
@@ -1275,12 +1275,20 @@ __device__ bool bin_hashed(Node* nodes, uint32_t ni, const Node& nd, uint64_t* k
                            uint32_t* mark, uint32_t* flags, bool hot) {
   unsigned long long* tk = region;                                  // kHashSlots keys
   uint32_t* tc = reinterpret_cast<uint32_t*>(tk + kHashSlots);       // kHashSlots counts
-  unsigned long long* sk = reinterpret_cast<unsigned long long*>(tc + kHashSlots);  // sorted keys
-  uint32_t* sc = reinterpret_cast<uint32_t*>(sk + kHashMaxDistinct);                // sorted counts
+  unsigned long long* sk = reinterpret_cast<unsigned long long*>(tc + kHashSlots);  // by digit
+  uint32_t* sc = reinterpret_cast<uint32_t*>(sk + kHashMaxDistinct);
   const uint32_t n = (uint32_t)nd.n;
   const uint32_t T = blockDim.x;
   DK_PHASE_BEGIN();
+  // digits: the top D free bits, D from the bin size (a bound on its distinct keys)
+  int D = ceil_log2_u64(n);
+  D = max(4, min(D, kBinDigitBits));
+  D = min(D, (int)nd.shift);
+  const int sh = nd.shift - D;
+  const uint32_t R = 1u << D, M = R - 1;
   for (uint32_t j = threadIdx.x; j < kHashSlots; j += T) { tk[j] = kEmptyKey; tc[j] = 0; }
+  for (uint32_t j = threadIdx.x; j < R; j += T) hist[j] = 0;
+  for (uint32_t w = threadIdx.x; w < (R + 31) / 32; w += T) mark[w] = 0;
   if (threadIdx.x == 0) flags[1] = 0;
   __syncthreads();
   constexpr int kBatch = 8;  // keys in flight per thread
@@ -1312,6 +1320,7 @@ __device__ bool bin_hashed(Node* nodes, uint32_t ni, const Node& nd, uint64_t* k
         const unsigned long long prev = atomicCAS(&tk[slot], kEmptyKey, key);
         if (prev == kEmptyKey || prev == key) {
           atomicAdd(&tc[slot], mult);
+          if (prev == kEmptyKey) atomicAdd(&hist[(uint32_t)(key >> sh) & M], 1u);
           break;
         }
         slot = (slot + 1) & (kHashSlots - 1);
@@ -1321,27 +1330,9 @@ __device__ bool bin_hashed(Node* nodes, uint32_t ni, const Node& nd, uint64_t* k
   __syncthreads();
   DK_PHASE(17);
   if (flags[1]) return false;
-  // distinct keys = filled slots
-  uint32_t occ = 0;
-  for (uint32_t j = threadIdx.x; j < kHashSlots; j += T) occ += tk[j] != kEmptyKey;
-  uint32_t d;
-  block_excl_scan<uint32_t>(occ, tmp, &d);
+  const uint32_t d = block_scan_array<uint32_t>(hist, (int)R, tmp);  // distinct keys
   if (d > kHashMaxDistinct) return false;  // uniform: d is the block total
-  // counting sort of the distinct pairs on the top D free bits
-  int D = ceil_log2_u64(d);
-  D = max(4, min(D, kBinDigitBits));
-  D = min(D, (int)nd.shift);
-  const int sh = nd.shift - D;
-  const uint32_t R = 1u << D, M = R - 1;
-  for (uint32_t j = threadIdx.x; j < R; j += T) hist[j] = 0;
-  for (uint32_t w = threadIdx.x; w < (R + 31) / 32; w += T) mark[w] = 0;
-  __syncthreads();
-  for (uint32_t j = threadIdx.x; j < kHashSlots; j += T)
-    if (tk[j] != kEmptyKey) atomicAdd(&hist[(uint32_t)(tk[j] >> sh) & M], 1u);
-  __syncthreads();
   DK_PHASE(18);
-  block_scan_array<uint32_t>(hist, (int)R, tmp);
-  DK_PHASE(19);
   for (uint32_t j = threadIdx.x; j < kHashSlots; j += T) {
     const unsigned long long key = tk[j];
     if (key != kEmptyKey) {
@@ -1351,57 +1342,42 @@ __device__ bool bin_hashed(Node* nodes, uint32_t ni, const Node& nd, uint64_t* k
   }
   __syncthreads();
   DK_PHASE(20);
-  // hist[j] is now the end of digit range j.  A range holding several
-  // distinct keys is in arbitrary order: each thread sorts the small ranges
-  // of its own digits in place (insertion sort); ranges of more than
-  // kThreadSortMax keys are marked and sorted by a warp.
-  if (sh > 0) {
-    const uint32_t per = (R + T - 1) / T;
-    const uint32_t j0 = min(R, threadIdx.x * per), j1 = min(R, j0 + per);
-    for (uint32_t j = j0; j < j1; ++j) {
-      const uint32_t lo = j ? hist[j - 1] : 0, hi = hist[j];
-      if (!DK_OK_IDX(lo <= hi && hi <= d, 32, ((uint64_t)lo << 32) | hi)) continue;
-      const uint32_t m = hi - lo;
-      if (m < 2) continue;
-      if (m > kThreadSortMax) {
-        atomicOr(&mark[j >> 5], 1u << (j & 31));
-        continue;
-      }
-      for (uint32_t x = lo + 1; x < hi; ++x) {
-        const unsigned long long v = sk[x];
-        const uint32_t c = sc[x];
-        uint32_t y = x;
-        while (y > lo && sk[y - 1] > v) {
-          sk[y] = sk[y - 1];
-          sc[y] = sc[y - 1];
-          --y;
-        }
-        sk[y] = v;
-        sc[y] = c;
-      }
-    }
-    __syncthreads();
-    DK_PHASE(21);
-    const uint32_t warp = threadIdx.x >> 5, nwarps = T >> 5;
-    for (uint32_t w = warp; w < (R + 31) / 32; w += nwarps) {
-      uint32_t bits = mark[w];
-      while (bits) {
-        const uint32_t j = w * 32 + (__ffs(bits) - 1);
-        bits &= bits - 1;
-        const uint32_t lo = j ? hist[j - 1] : 0, hi = hist[j];
-        if (!DK_OK_IDX(lo <= hi && hi <= d, 33, ((uint64_t)lo << 32) | hi)) continue;
-        if (hi - lo <= 32) warp_rank_sort_pairs(sk + lo, sc + lo, hi - lo);
-        else warp_bitonic_pairs(sk + lo, sc + lo, hi - lo);
-      }
-    }
-    __syncthreads();
-    DK_PHASE(22);
-  }
+  // hist[j] is now the end of digit range j; keys within a range are in
+  // arbitrary order.  Each pair finds its rank among the range's keys (all
+  // distinct) and goes straight to the output; longer ranges are marked.
   for (uint32_t x = threadIdx.x; x < d; x += T) {
-    keys[x] = sk[x];
-    cnt[x] = sc[x];
+    const unsigned long long v = sk[x];
+    const uint32_t j = (uint32_t)(v >> sh) & M;
+    const uint32_t lo = j ? hist[j - 1] : 0, hi = hist[j];
+    if (hi - lo > 32) {
+      atomicOr(&mark[j >> 5], 1u << (j & 31));
+      continue;
+    }
+    uint32_t r = lo;
+    for (uint32_t y = lo; y < hi; ++y) r += sk[y] < v;
+    if (DK_OK_IDX(r < d, 32, r)) {
+      keys[r] = v;
+      cnt[r] = sc[x];
+    }
   }
-  DK_PHASE(23);
+  __syncthreads();
+  DK_PHASE(21);
+  const uint32_t warp = threadIdx.x >> 5, nwarps = T >> 5;
+  for (uint32_t w = warp; w < (R + 31) / 32; w += nwarps) {
+    uint32_t bits = mark[w];
+    while (bits) {
+      const uint32_t j = w * 32 + (__ffs(bits) - 1);
+      bits &= bits - 1;
+      const uint32_t lo = j ? hist[j - 1] : 0, hi = hist[j];
+      if (!DK_OK_IDX(lo <= hi && hi <= d, 33, ((uint64_t)lo << 32) | hi)) continue;
+      warp_bitonic_pairs(sk + lo, sc + lo, hi - lo);
+      for (uint32_t x = lo + lane_id(); x < hi; x += 32) {
+        keys[x] = sk[x];
+        cnt[x] = sc[x];
+      }
+    }
+  }
+  DK_PHASE(22);
   DK_PHASE_ADD(24, 1);
   DK_PHASE_ADD(25, n);
   DK_PHASE_ADD(26, d);
@@ -1529,7 +1505,32 @@ __global__ void k_compact(const Node* nodes, const uint32_t* __restrict__ finals
   }
 }
 
+// Small copies between device and page-locked host memory done by a kernel
+// (the GPU reads or writes the host side over the chip-to-chip link), so that
+// an engine's control traffic never queues behind a bulk copy that occupies a
+// copy engine.
+__global__ void k_copy_small(const uint8_t* __restrict__ src, uint8_t* __restrict__ dst,
+                             uint64_t bytes) {
+  const uint64_t i0 = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const uint64_t step = (uint64_t)gridDim.x * blockDim.x;
+  if (((reinterpret_cast<uintptr_t>(src) | reinterpret_cast<uintptr_t>(dst) | bytes) & 7) == 0) {
+    const uint64_t* s = reinterpret_cast<const uint64_t*>(src);
+    uint64_t* d = reinterpret_cast<uint64_t*>(dst);
+    for (uint64_t i = i0; i < bytes / 8; i += step) d[i] = s[i];
+  } else {
+    for (uint64_t i = i0; i < bytes; i += step) dst[i] = src[i];
+  }
+}
+
 }  // namespace
+
+int launch_copy_small(const void* src, void* dst, uint64_t bytes, cudaStream_t s) {
+  if (!bytes) return 0;
+  const uint64_t units = (bytes + 7) / 8;
+  const uint32_t blocks = (uint32_t)std::min<uint64_t>(64, (units + 255) / 256);
+  k_copy_small<<<blocks, 256, 0, s>>>((const uint8_t*)src, (uint8_t*)dst, bytes);
+  return 1;
+}
 
 // ------------------------------------------------------------ launchers
 // Every launcher raises a kernel's dynamic shared-memory limit to the same
