@@ -233,16 +233,29 @@ int64_t frame_lines(uint64_t nbytes, int W) {
   return (int64_t)((nbytes + 1) / stride);
 }
 
+// Smallest (8 + m) * 2^e, m < 8, that is >= n.
+static uint64_t size_class(uint64_t n) {
+  if (n <= 16) return n;
+  int e = 0;
+  while ((16ull << e) <= n) ++e;  // 2^(e+3) <= n < 2^(e+4)
+  const uint64_t step = 1ull << e;
+  return (n + step - 1) / step * step;
+}
+
 // Table storage: a pool of allocations reused across calls (pinned host or device).
 int Engine::acquire_table(uint64_t n, bool on_device, TableBuf** out) {
   Engine* e = this;
+  std::lock_guard<std::mutex> g(pool_mu);
   TableBuf* best = nullptr;
   for (auto& t : tables)
     if (!t.in_use && t.on_device == on_device && t.cap >= n && (!best || t.cap < best->cap)) best = &t;
   if (!best) {
     TableBuf t;
     t.on_device = on_device;
-    t.cap = std::max<uint64_t>(n, 1);
+    // capacities in size classes (eight per power of two, at most 12.5%
+    // over), so that tables of varying sizes -- batches of different jobs --
+    // reuse pooled buffers instead of pinning or allocating new ones
+    t.cap = size_class(std::max<uint64_t>(n, 1));
     if (on_device) {
       if (budget && dev_bytes + t.cap * 12 > budget) return DK_ERR_ADMISSION;
       if (cudaMalloc(&t.k, t.cap * 8) != cudaSuccess || cudaMalloc(&t.c, t.cap * 4) != cudaSuccess) {
@@ -272,6 +285,7 @@ int Engine::acquire_table(uint64_t n, bool on_device, TableBuf** out) {
 }
 
 int Engine::release_table(uint64_t id) {
+  std::lock_guard<std::mutex> g(pool_mu);
   for (auto& t : tables)
     if (t.id == id && t.in_use) {
       if (t.refs > 1) {
@@ -530,7 +544,10 @@ int Engine::count_batch(const dk_job* jobs, int njobs, const dk_input_desc* desc
       }
       DK_CUDA(cudaEventRecord(ev_out1[b], s_out));
       out_pending[b] = true;
-      h_tb->refs = (uint32_t)nj;
+      {
+        std::lock_guard<std::mutex> pg(pool_mu);
+        h_tb->refs = (uint32_t)nj;
+      }
       for (int j = 0; j < nj; ++j) {
         dk_table& t = outs[wv.j0 + j];
         const bool has = !js.nodes.empty();
@@ -1196,8 +1213,7 @@ int dk_table_free(dk_ctx* ctx, dk_table* t) {
     std::memset(t, 0, sizeof(*t));
     return rc;
   }
-  std::lock_guard<std::mutex> g(ctx->eng.mu);
-  const int rc = ctx->eng.release_table(t->handle);
+  const int rc = ctx->eng.release_table(t->handle);  // the pool has its own lock
   std::memset(t, 0, sizeof(*t));
   return rc;
 }

@@ -91,11 +91,12 @@ struct Engine {
   size_t node_cap_needed = 0;
   uint64_t* out_k = nullptr;
   uint32_t* out_c = nullptr;
-  std::deque<TableBuf> tables;  // deque: stable addresses
+  std::deque<TableBuf> tables;  // deque: stable addresses; guarded by pool_mu
+  std::mutex pool_mu;           // tables may be released while a count runs
   uint64_t table_ids = 0;
 
   cudaEvent_t ev_stage[8] = {};
-  static constexpr int kKEvents = 128;
+  static constexpr int kKEvents = 512;
   struct KEv { int slot, e0, e1, n; };
   cudaEvent_t kev_pool[kKEvents] = {};
   std::vector<KEv> kev;

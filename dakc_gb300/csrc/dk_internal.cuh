@@ -24,7 +24,8 @@ struct Node {
   uint32_t ntiles;
   uint64_t th_base;  // first tile-histogram entry (rows of 2^width per tile)
   uint8_t width;     // digit bits this node is split on (split nodes)
-  uint8_t pad[7];
+  uint8_t skewed;    // kept more than half of its parent's keys (a hot k-mer)
+  uint8_t pad[6];
 };
 static_assert(sizeof(Node) == 64, "Node layout");
 enum : uint8_t { NODE_FINAL = 1, NODE_SPLIT = 2, NODE_EMPTY = 3 };
@@ -34,7 +35,10 @@ struct Tile {  // a slice of a split node's keys, partitioned by one CTA
   uint32_t n;
   uint32_t node;  // global node index
   uint64_t th;    // first entry of this tile's histogram row
+  uint32_t hot;   // one digit holds more than a quarter of the tile (set by the node scan)
+  uint32_t pad;
 };
+static_assert(sizeof(Tile) == 32, "Tile layout");
 
 // counters written by the classify / assign kernels.  n_final accumulates over
 // all levels; the others are per level (zeroed from byte 4 on).
@@ -67,6 +71,8 @@ constexpr int kMaxL1Bits = 12;          // level-1 fan-out <= 4096 buckets
 constexpr size_t kMaxSmemPerBlock = 232448;  // opt-in shared memory per block (sm_100 family)
 constexpr int kLineThreads = 256;        // thread-per-line level-1 kernels: lines per tile
 constexpr int kLineMaxW = 256;           // longer lines use the warp-per-line kernels
+constexpr int kLineChunk = 16;           // positions per line in one chunked-scatter chunk
+constexpr bool kPlainChunkedScatter = true;  // plain counts: chunked thread-per-line scatter
 
 struct ExtractArgs {
   const uint8_t* text;  // device text, 16-byte aligned
@@ -114,7 +120,7 @@ int launch_assign(Node* nodes, uint32_t node_lo, uint32_t node_hi, uint32_t chil
                   Tile* tiles, LevelCounters* ctr, cudaStream_t s);
 int launch_tile_hist(const Node* nodes, const Tile* tiles, uint32_t n_tiles,
                      const uint64_t* A, const uint64_t* B, uint32_t* TH, cudaStream_t s);
-int launch_node_scan(Node* nodes, uint32_t node_lo, uint32_t node_hi, const Tile* tiles,
+int launch_node_scan(Node* nodes, uint32_t node_lo, uint32_t node_hi, Tile* tiles,
                      uint32_t* TH, cudaStream_t s);
 int launch_tile_scatter(const Node* nodes, const Tile* tiles, uint32_t n_tiles, uint64_t* A,
                         uint64_t* B, const uint32_t* TH, int max_width, cudaStream_t s);

@@ -143,14 +143,27 @@ struct JobBucket {
   }
 };
 
-// job that owns line l in batch mode (binary search over job_start)
-__device__ __forceinline__ uint32_t job_of_line(const ExtractArgs& a, uint64_t l) {
-  uint32_t lo = 0, hi = (uint32_t)a.njobs;
+// job that owns line l in batch mode: binary search over job_start within
+// jobs [lo, hi) (the whole set by default)
+__device__ __forceinline__ uint32_t job_of_line(const ExtractArgs& a, uint64_t l, uint32_t lo = 0,
+                                                uint32_t hi = 0xFFFFFFFFu) {
+  hi = min(hi, (uint32_t)a.njobs);
   while (hi - lo > 1) {
     const uint32_t mid = (lo + hi) >> 1;
     if (__ldg(a.job_start + mid) <= l) lo = mid; else hi = mid;
   }
   return lo;
+}
+
+// jobs owning the first and last line of a tile [l0, l1) (batch mode): the
+// tile's lines search only between them.  Call with the whole block.
+__device__ __forceinline__ void tile_jobs(const ExtractArgs& a, uint64_t l0, uint64_t l1,
+                                          uint32_t* s_jobs) {
+  if (a.njobs) {
+    if (threadIdx.x == 0) s_jobs[0] = job_of_line(a, l0);
+    if (threadIdx.x == 32) s_jobs[1] = job_of_line(a, l1 - 1) + 1;
+  }
+  __syncthreads();
 }
 
 // counters[0] = k-mers, [1] = n_lines - (first NUL-led line), [3] = device error
@@ -256,6 +269,7 @@ __global__ void k_l1_starts(Node* nodes, int F1, int shift1, const int16_t* buck
     nd.ntiles = 0;
     nd.th_base = 0;
     nd.width = 0;
+    nd.skewed = 0;
   }
 }
 
@@ -306,10 +320,11 @@ struct LineRoll {
 // mode); records NUL-led lines.
 __device__ __forceinline__ bool line_prologue(const ExtractArgs& a, uint64_t l, uint64_t l1,
                                               const uint8_t* line, JobBucket* jb,
-                                              unsigned long long* counters) {
+                                              unsigned long long* counters,
+                                              const uint32_t* s_jobs) {
   if (l >= l1) return false;
   if (a.njobs) {
-    const uint32_t job = job_of_line(a, l);
+    const uint32_t job = job_of_line(a, l, s_jobs[0], s_jobs[1]);
     if (l >= __ldg(a.job_end + job)) return false;  // past the job's first NUL-led line
     if (l > __ldg(a.job_start + job) && line[0] == 0) {
       atomicMin(&a.job_nul[job], (unsigned long long)l);
@@ -349,6 +364,7 @@ __global__ void __launch_bounds__(kLineThreads) k_l1_lines_count(ExtractArgs a,
   const uint32_t bb = tile_buf_bytes(blockDim.x, stride);
   uint32_t* cnt = reinterpret_cast<uint32_t*>(smraw + 128 + 2 * bb);  // F1
   uint8_t* lut = reinterpret_cast<uint8_t*>(cnt + a.F1);              // 256
+  __shared__ uint32_t s_jobs[2];
   TextTiles T;
   setup_tiles(&T, a, smraw, bb);
   for (int b = threadIdx.x; b < a.F1; b += blockDim.x) cnt[b] = 0;
@@ -366,10 +382,11 @@ __global__ void __launch_bounds__(kLineThreads) k_l1_lines_count(ExtractArgs a,
     }
     uint64_t l0, l1;
     T.range(ti, &l0, &l1);
+    tile_jobs(a, l0, l1, s_jobs);
     const uint64_t l = l0 + threadIdx.x;
     const uint8_t* line = tile + (l - l0) * stride;
     JobBucket jb;
-    if (line_prologue(a, l, l1, line, &jb, counters)) {
+    if (line_prologue(a, l, l1, line, &jb, counters, s_jobs)) {
       LineRoll r;
       r.reset();
       for (int p0 = 0; p0 < W && !r.stopped; p0 += 4) {
@@ -394,6 +411,96 @@ __global__ void __launch_bounds__(kLineThreads) k_l1_lines_count(ExtractArgs a,
   for (int b = threadIdx.x; b < a.F1; b += blockDim.x) row[b] = cnt[b];
 }
 
+// Plain-count scatter, thread per line: a tile's k-mers leave in chunks of
+// kLineChunk positions per line.  For each chunk every thread rolls its
+// line's positions once to count the chunk's keys per bucket, the block scans
+// those counts, and the thread rolls the same positions again (from the saved
+// state) to place each key in shared memory grouped by bucket; each bucket's
+// keys then leave as one contiguous run at this CTA's cursor of the bucket.
+// One text buffer (the next tile is fetched after the current one is done)
+// keeps shared memory at two CTAs per SM.
+__global__ void __launch_bounds__(kLineThreads, 2) k_l1_lines_chunked(ExtractArgs a,
+                                                                     const uint64_t* __restrict__ O,
+                                                                     uint64_t* __restrict__ keys_out,
+                                                                     unsigned long long* __restrict__ counters) {
+  extern __shared__ __align__(128) uint8_t smraw[];
+  const int W = a.W, k = a.k, F1 = a.F1;
+  const uint64_t stride = (uint64_t)W + 1;
+  const uint32_t bb = tile_buf_bytes(blockDim.x, stride);
+  unsigned long long* stage = reinterpret_cast<unsigned long long*>(smraw + 128 + bb);  // chunk keys
+  unsigned long long* cursor = stage + (size_t)blockDim.x * kLineChunk;                  // F1
+  uint32_t* ccount = reinterpret_cast<uint32_t*>(cursor + F1);                            // F1
+  uint32_t* coff = ccount + F1;                                                           // F1
+  uint32_t* tmp = coff + F1;                                                              // 32
+  uint8_t* lut = reinterpret_cast<uint8_t*>(tmp + 32);                                    // 256
+  TextTiles T;
+  setup_tiles(&T, a, smraw, bb);
+  T.buf[1] = T.buf[0];  // one buffer: tile t+1 is fetched once tile t is done
+  for (int b = threadIdx.x; b < F1; b += blockDim.x) {
+    cursor[b] = O[(size_t)blockIdx.x * F1 + b];
+    ccount[b] = 0;
+  }
+  init_lut(lut);
+  __syncthreads();
+  const uint32_t nt = T.ntiles();
+  if (threadIdx.x == 0 && nt) T.issue(0);
+  for (uint32_t ti = 0; ti < nt; ++ti) {
+    const uint8_t* tile = T.acquire(ti, &counters[3]);
+    if (!tile) return;  // nothing else is in flight into this CTA's shared memory
+    uint64_t l0, l1;
+    T.range(ti, &l0, &l1);
+    const uint64_t l = l0 + threadIdx.x;
+    const uint8_t* line = tile + (l - l0) * stride;
+    JobBucket jb;
+    const uint32_t no_jobs[2] = {0, 0};
+    const bool live = line_prologue(a, l, l1, line, &jb, counters, no_jobs);
+    LineRoll r;
+    r.reset();
+    if (!live) r.stopped = true;
+    // warm-up: positions before the first possible k-mer end emit nothing
+    const int warm = min(k - 1, W);
+    for (int p = 0; p < warm; ++p) r.step(r.stopped ? 0xF0u : lut[line[p]], p, W, k, a.kmask);
+    for (int p0 = warm; p0 < W; p0 += kLineChunk) {  // uniform over the block
+      const int p1 = min(W, p0 + kLineChunk);
+      const LineRoll r0 = r;
+      for (int p = p0; p < p1 && !r.stopped; ++p)
+        if (r.step(lut[line[p]], p, W, k, a.kmask))
+          atomicAdd(&ccount[(uint32_t)(r.key >> a.shift1)], 1u);
+      __syncthreads();
+      for (int b = threadIdx.x; b < F1; b += blockDim.x) {
+        coff[b] = ccount[b];
+        ccount[b] = 0;
+      }
+      __syncthreads();
+      const uint32_t Tn = block_scan_array<uint32_t>(coff, F1, tmp);
+      r = r0;
+      for (int p = p0; p < p1 && !r.stopped; ++p)
+        if (r.step(lut[line[p]], p, W, k, a.kmask)) {
+          const uint32_t b = (uint32_t)(r.key >> a.shift1);
+          const uint32_t pos = coff[b] + atomicAdd(&ccount[b], 1u);
+          if (DK_OK_IDX(pos < (uint32_t)blockDim.x * kLineChunk, 41, pos)) stage[pos] = r.key;
+        }
+      __syncthreads();
+      for (uint32_t i = threadIdx.x; i < Tn; i += blockDim.x) {
+        const uint64_t key = stage[i];
+        const uint32_t b = (uint32_t)(key >> a.shift1);
+        keys_out[cursor[b] + (i - coff[b])] = key;
+      }
+      __syncthreads();
+      for (int b = threadIdx.x; b < F1; b += blockDim.x) {
+        cursor[b] += ccount[b];
+        ccount[b] = 0;
+      }
+      __syncthreads();
+    }
+    // every thread's generic accesses of the buffer are ordered before the
+    // bulk copy that refills it
+    fence_barrier_init();
+    __syncthreads();
+    if (threadIdx.x == 0 && ti + 1 < nt) T.issue(ti + 1);
+  }
+}
+
 // Batch-mode scatter: each k-mer goes straight to its bucket at this CTA's
 // cursor, O[cta][bucket] + (its rank among this CTA's keys of the bucket).
 // A wave's jobs own up to 4,096 level-1 buckets, so a tile holds about one
@@ -411,6 +518,7 @@ __global__ void __launch_bounds__(kLineThreads) k_l1_lines_direct(ExtractArgs a,
   unsigned long long* cursor = reinterpret_cast<unsigned long long*>(smraw + 128 + 2 * bb);  // F1
   uint32_t* cnt = reinterpret_cast<uint32_t*>(cursor + a.F1);                                 // F1
   uint8_t* lut = reinterpret_cast<uint8_t*>(cnt + a.F1);                                      // 256
+  __shared__ uint32_t s_jobs[2];
   TextTiles T;
   setup_tiles(&T, a, smraw, bb);
   for (int b = threadIdx.x; b < a.F1; b += blockDim.x) {
@@ -430,10 +538,11 @@ __global__ void __launch_bounds__(kLineThreads) k_l1_lines_direct(ExtractArgs a,
     }
     uint64_t l0, l1;
     T.range(ti, &l0, &l1);
+    tile_jobs(a, l0, l1, s_jobs);
     const uint64_t l = l0 + threadIdx.x;
     const uint8_t* line = tile + (l - l0) * stride;
     JobBucket jb;
-    if (line_prologue(a, l, l1, line, &jb, counters)) {
+    if (line_prologue(a, l, l1, line, &jb, counters, s_jobs)) {
       LineRoll r;
       r.reset();
       for (int p0 = 0; p0 < W && !r.stopped; p0 += 4) {
@@ -567,6 +676,48 @@ __global__ void __launch_bounds__(512, 2) k_l1_scatter(ExtractArgs a, const uint
   }
 }
 
+// Warp-aggregated shared-memory atomics: lanes holding the same value add
+// once (by the lowest such lane).  Hot k-mers (many copies of one key in a
+// bin) otherwise serialise on one shared-memory word.
+__device__ __forceinline__ void agg_add_u32(uint32_t* ctr, uint32_t v, bool hot) {
+  if (!hot) { atomicAdd(&ctr[v], 1u); return; }
+  const uint32_t mask = __activemask();
+  const uint32_t peers = __match_any_sync(mask, v);
+  if ((int)lane_id() == __ffs(peers) - 1) atomicAdd(&ctr[v], (uint32_t)__popc(peers));
+}
+
+// returns this lane's slot: leader reserves popc(peers) slots, peers take ranks
+__device__ __forceinline__ uint32_t agg_reserve_u32(uint32_t* ctr, uint32_t v, bool hot) {
+  if (!hot) return atomicAdd(&ctr[v], 1u);
+  const uint32_t mask = __activemask();
+  const uint32_t peers = __match_any_sync(mask, v);
+  const int leader = __ffs(peers) - 1;
+  uint32_t base = 0;
+  if ((int)lane_id() == leader) base = atomicAdd(&ctr[v], (uint32_t)__popc(peers));
+  base = __shfl_sync(peers, base, leader);
+  return base + (uint32_t)__popc(peers & ((1u << lane_id()) - 1u));
+}
+
+__device__ __forceinline__ void agg_add_u64(unsigned long long* ctr, uint32_t v) {
+  const uint32_t mask = __activemask();
+  const uint32_t peers = __match_any_sync(mask, v);
+  if ((int)lane_id() == __ffs(peers) - 1) atomicAdd(&ctr[v], (unsigned long long)__popc(peers));
+}
+
+// Rank of this lane's key within its digit v (an atomic on ctr[v]); in a hot
+// tile, lanes of the warp with the same digit reserve together.  Every lane
+// of the warp calls it; `valid` lanes get a rank.
+__device__ __forceinline__ uint32_t rank_in_digit(uint32_t* ctr, uint32_t v, bool valid, bool hot) {
+  if (!hot) return valid ? atomicAdd(&ctr[v], 1u) : 0u;
+  const uint32_t peers = __match_any_sync(0xFFFFFFFFu, valid ? v : 0xFFFFFFFFu);
+  if (!valid) return 0u;
+  const int leader = __ffs(peers) - 1;
+  uint32_t base = 0;
+  if ((int)lane_id() == leader) base = atomicAdd(&ctr[v], (uint32_t)__popc(peers));
+  base = __shfl_sync(peers, base, leader);
+  return base + (uint32_t)__popc(peers & ((1u << lane_id()) - 1u));
+}
+
 // ---------------------------------------------------- partition levels
 // A split node is split on its next `width` bits, width chosen so that the
 // children average about half a bin: wide for big nodes, narrow for small.
@@ -626,6 +777,8 @@ __global__ void k_assign(Node* nodes, uint32_t lo, uint32_t hi, uint32_t child_b
     tl.n = (uint32_t)min((uint64_t)kTileKeys, nd.n - (uint64_t)t * kTileKeys);
     tl.node = i;
     tl.th = thb + (uint64_t)t * R;
+    tl.hot = 0;
+    tl.pad = 0;
     tiles[tb + t] = tl;
   }
 }
@@ -644,24 +797,25 @@ __global__ void __launch_bounds__(256) k_tile_hist(const Node* nodes, const Tile
   const uint64_t* src = (nd.buf ? B : A) + tl.start;
   for (uint32_t j = threadIdx.x; j < R; j += blockDim.x) hist[j] = 0;
   __syncthreads();
+  const bool hot = nd.skewed;  // the node kept most of its parent's keys: a hot k-mer
   uint32_t i = threadIdx.x;
   const uint32_t T = blockDim.x;
   for (; i + 3 * T < tl.n; i += 4 * T) {
     const uint64_t k0 = __ldg(src + i), k1 = __ldg(src + i + T), k2 = __ldg(src + i + 2 * T),
                    k3 = __ldg(src + i + 3 * T);
-    atomicAdd(&hist[digit_of(k0, nd.shift, nd.width)], 1u);
-    atomicAdd(&hist[digit_of(k1, nd.shift, nd.width)], 1u);
-    atomicAdd(&hist[digit_of(k2, nd.shift, nd.width)], 1u);
-    atomicAdd(&hist[digit_of(k3, nd.shift, nd.width)], 1u);
+    agg_add_u32(hist, digit_of(k0, nd.shift, nd.width), hot);
+    agg_add_u32(hist, digit_of(k1, nd.shift, nd.width), hot);
+    agg_add_u32(hist, digit_of(k2, nd.shift, nd.width), hot);
+    agg_add_u32(hist, digit_of(k3, nd.shift, nd.width), hot);
   }
-  for (; i < tl.n; i += T) atomicAdd(&hist[digit_of(__ldg(src + i), nd.shift, nd.width)], 1u);
+  for (; i < tl.n; i += T) agg_add_u32(hist, digit_of(__ldg(src + i), nd.shift, nd.width), hot);
   __syncthreads();
   for (uint32_t j = threadIdx.x; j < R; j += blockDim.x) TH[tl.th + j] = hist[j];
 }
 
 // one CTA per node of the level; split nodes turn their tiles' counts into
 // offsets within each child and create the 2^width children
-__global__ void __launch_bounds__(256) k_node_scan(Node* nodes, uint32_t lo, const Tile* tiles,
+__global__ void __launch_bounds__(256) k_node_scan(Node* nodes, uint32_t lo, Tile* tiles,
                                                    uint32_t* TH) {
   __shared__ unsigned long long csize[1u << kMaxSplitBits];
   __shared__ unsigned long long tmp[32];
@@ -675,6 +829,8 @@ __global__ void __launch_bounds__(256) k_node_scan(Node* nodes, uint32_t lo, con
     // eight tiles at a time: their loads are independent, only the running
     // sum is serial
     uint32_t t = 0;
+    // a digit with more than a quarter of a full tile marks that tile hot
+    constexpr uint32_t kHotCount = kTileKeys / 4;
     for (; t + 8 <= nd.ntiles; t += 8) {
       uint32_t c[8];
 #pragma unroll
@@ -683,12 +839,14 @@ __global__ void __launch_bounds__(256) k_node_scan(Node* nodes, uint32_t lo, con
       for (int u = 0; u < 8; ++u) {
         col[(uint64_t)(t + u) * R] = run;
         run += c[u];
+        if (c[u] > kHotCount) tiles[nd.tile_base + t + u].hot = 1;
       }
     }
     for (; t < nd.ntiles; ++t) {
       const uint32_t c = col[(uint64_t)t * R];
       col[(uint64_t)t * R] = run;
       run += c;
+      if (c > kHotCount) tiles[nd.tile_base + t].hot = 1;
     }
     csize[j] = run;
   }
@@ -710,6 +868,7 @@ __global__ void __launch_bounds__(256) k_node_scan(Node* nodes, uint32_t lo, con
     ch.ntiles = 0;
     ch.th_base = 0;
     ch.width = 0;
+    ch.skewed = ch.n * 2 > nd.n;
     nodes[nd.first_child + j] = ch;
   }
 }
@@ -744,6 +903,7 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_tile_scatter(const Node* no
     cnt[j] = 0;
   }
   __syncthreads();
+  const bool hot = tl.hot != 0;  // a skewed tile: ranks are reserved per warp
   // all of this thread's keys are loaded first (their loads overlap) and kept
   // in registers for the staging pass
   uint64_t kr[kTileKeysPerThread];
@@ -756,7 +916,8 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_tile_scatter(const Node* no
 #pragma unroll
   for (int u = 0; u < kTileKeysPerThread; ++u) {
     const uint32_t i = threadIdx.x + u * kTileThreads;
-    const uint32_t r = i < tl.n ? atomicAdd(&cnt[digit_of(kr[u], sh, w)], 1u) : 0u;
+    // every lane reaches the reserve (in a hot tile its match is warp-wide)
+    const uint32_t r = rank_in_digit(cnt, digit_of(kr[u], sh, w), i < tl.n, hot);
     if (u & 1) rank[u >> 1] |= r << 16;
     else rank[u >> 1] = r;
   }
@@ -782,34 +943,6 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_tile_scatter(const Node* no
 
 // ------------------------------------------------------------ bin count
 constexpr uint32_t kThreadSortMax = 16;  // larger digit ranges are sorted by a warp
-
-// Warp-aggregated shared-memory atomics: lanes holding the same value add
-// once (by the lowest such lane).  Hot k-mers (many copies of one key in a
-// bin) otherwise serialise on one shared-memory word.
-__device__ __forceinline__ void agg_add_u32(uint32_t* ctr, uint32_t v, bool hot) {
-  if (!hot) { atomicAdd(&ctr[v], 1u); return; }
-  const uint32_t mask = __activemask();
-  const uint32_t peers = __match_any_sync(mask, v);
-  if ((int)lane_id() == __ffs(peers) - 1) atomicAdd(&ctr[v], (uint32_t)__popc(peers));
-}
-
-// returns this lane's slot: leader reserves popc(peers) slots, peers take ranks
-__device__ __forceinline__ uint32_t agg_reserve_u32(uint32_t* ctr, uint32_t v, bool hot) {
-  if (!hot) return atomicAdd(&ctr[v], 1u);
-  const uint32_t mask = __activemask();
-  const uint32_t peers = __match_any_sync(mask, v);
-  const int leader = __ffs(peers) - 1;
-  uint32_t base = 0;
-  if ((int)lane_id() == leader) base = atomicAdd(&ctr[v], (uint32_t)__popc(peers));
-  base = __shfl_sync(peers, base, leader);
-  return base + (uint32_t)__popc(peers & ((1u << lane_id()) - 1u));
-}
-
-__device__ __forceinline__ void agg_add_u64(unsigned long long* ctr, uint32_t v) {
-  const uint32_t mask = __activemask();
-  const uint32_t peers = __match_any_sync(mask, v);
-  if ((int)lane_id() == __ffs(peers) - 1) atomicAdd(&ctr[v], (unsigned long long)__popc(peers));
-}
 
 // Block-wide exclusive scan of (sum, max) pairs; returns both exclusive
 // values and the block totals.  `tmp` needs 64 u32 slots.
@@ -1262,12 +1395,14 @@ __device__ void warp_bitonic_pairs(unsigned long long* s, uint32_t* c, uint32_t 
   }
 }
 
+constexpr uint32_t kRankMax = 256;  // longer digit ranges are sorted by a warp
+
 // Aggregate the bin's keys in a shared-memory open-addressing table (linear
 // probing on a multiplicative hash, 64-bit atomicCAS on the key, atomicAdd on
 // its count; a new key also counts its digit, the top D free bits), place the
 // distinct (key, count) pairs by digit (counting sort), and write each pair
 // at its rank inside its digit range, found by comparing it with the range's
-// other keys (ranges of more than 32 keys are sorted by a warp instead).
+// other keys (ranges of more than kRankMax keys are sorted by a warp instead).
 // Returns false, having written nothing, when a probe runs past
 // kHashMaxProbe slots or the bin holds more than kHashMaxDistinct keys.
 __device__ bool bin_hashed(Node* nodes, uint32_t ni, const Node& nd, uint64_t* keys, uint32_t* cnt,
@@ -1344,12 +1479,14 @@ __device__ bool bin_hashed(Node* nodes, uint32_t ni, const Node& nd, uint64_t* k
   DK_PHASE(20);
   // hist[j] is now the end of digit range j; keys within a range are in
   // arbitrary order.  Each pair finds its rank among the range's keys (all
-  // distinct) and goes straight to the output; longer ranges are marked.
+  // distinct) and goes straight to the output.  A range's pairs sit on
+  // consecutive threads, so the comparisons read shared memory as
+  // broadcasts; ranges of more than kRankMax keys are marked instead.
   for (uint32_t x = threadIdx.x; x < d; x += T) {
     const unsigned long long v = sk[x];
     const uint32_t j = (uint32_t)(v >> sh) & M;
     const uint32_t lo = j ? hist[j - 1] : 0, hi = hist[j];
-    if (hi - lo > 32) {
+    if (hi - lo > kRankMax) {
       atomicOr(&mark[j >> 5], 1u << (j & 31));
       continue;
     }
@@ -1580,6 +1717,16 @@ static size_t lines_smem(const ExtractArgs& a, bool scatter) {
 // directly; plain counts stage their tiles (k_l1_scatter)
 static bool direct_scatter(int W, bool jobs) { return jobs && W <= kLineMaxW; }
 
+static size_t chunked_smem(const ExtractArgs& a) {
+  return 128 + (size_t)tile_buf_bytes(kLineThreads, (uint64_t)a.W + 1) +
+         (size_t)kLineThreads * kLineChunk * 8 + (size_t)a.F1 * 16 + 32 * 4 + 256;
+}
+// plain counts whose chunked thread-per-line scatter fits two CTAs per SM
+static bool chunked_scatter(const ExtractArgs& a) {
+  return kPlainChunkedScatter && !a.njobs && a.W <= kLineMaxW &&
+         chunked_smem(a) <= kMaxSmemPerBlock / 2 - 1024;
+}
+
 int launch_l1_count(const ExtractArgs& a, int grid, uint32_t* H, unsigned long long* counters,
                     cudaStream_t s) {
   if (a.W <= kLineMaxW) {
@@ -1645,6 +1792,11 @@ static void scatter_launch(const ExtractArgs& a, int grid, const uint64_t* O, ui
 
 int launch_l1_scatter(const ExtractArgs& a, int grid, const uint64_t* O, uint64_t* keys,
                       unsigned long long* counters, cudaStream_t s) {
+  if (chunked_scatter(a)) {
+    allow_max_smem(k_l1_lines_chunked);
+    k_l1_lines_chunked<<<grid, kLineThreads, chunked_smem(a), s>>>(a, O, keys, counters);
+    return 1;
+  }
   if (direct_scatter(a.W, a.njobs != 0)) {
     allow_max_smem(k_l1_lines_direct);
     k_l1_lines_direct<<<grid, kLineThreads, lines_smem(a, true), s>>>(a, O, keys, counters);
@@ -1686,7 +1838,7 @@ int launch_tile_hist(const Node* nodes, const Tile* tiles, uint32_t n_tiles, con
   return 1;
 }
 
-int launch_node_scan(Node* nodes, uint32_t lo, uint32_t hi, const Tile* tiles, uint32_t* TH,
+int launch_node_scan(Node* nodes, uint32_t lo, uint32_t hi, Tile* tiles, uint32_t* TH,
                      cudaStream_t s) {
   if (hi <= lo) return 0;
   k_node_scan<<<hi - lo, 256, 0, s>>>(nodes, lo, tiles, TH);

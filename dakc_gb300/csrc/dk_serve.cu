@@ -44,6 +44,7 @@ struct Request {
   uint64_t nbytes = 0;
   dk_input_desc desc{};
   uint64_t est = 0;
+  uint64_t kmers = 0;  // upper bound: lines * (line_width - k + 1)
   Clock::time_point t_submit, t_start, t_end;
   int status = DK_ERR_PENDING;
   dk_table table{};
@@ -58,6 +59,10 @@ struct Worker {
 };
 
 struct Server {
+  // k-mers (upper bound) a worker gathers into one batch: about 5 ms of
+  // device time -- enough to amortise a batch's fixed costs, short enough
+  // that small jobs are not held behind large ones
+  static constexpr uint64_t kBatchKmers = 128ull << 20;
   std::mutex mu;
   std::condition_variable cv_work, cv_done;
   std::deque<std::shared_ptr<Request>> queue;
@@ -84,15 +89,19 @@ struct Server {
         std::unique_lock<std::mutex> lk(mu);
         cv_work.wait(lk, [&] { return stop.load() || !queue.empty(); });
         if (stop.load() && queue.empty()) return;
-        // coalesce every queued job that fits this worker's share of the budget
+        // coalesce queued jobs that fit this worker's share of the budget, up
+        // to about kBatchKmers k-mers: a larger queue is left to the other
+        // workers, so that batches run side by side and latency stays bounded
         const dk_input_desc d0 = queue.front()->desc;
-        uint64_t bytes = 0;
-        for (auto it = queue.begin(); it != queue.end() && (int)batch.size() < max_batch;) {
+        uint64_t bytes = 0, kmers = 0;
+        for (auto it = queue.begin();
+             it != queue.end() && (int)batch.size() < max_batch && kmers < kBatchKmers;) {
           const auto& r = *it;
           const bool same = r->desc.line_width == d0.line_width && r->desc.k == d0.k &&
                             r->desc.variant == d0.variant;
           if (same && (batch.empty() || bytes + r->est <= (uint64_t)(0.7 * (double)me.budget))) {
             bytes += r->est;
+            kmers += r->kmers;
             batch.push_back(r);
             it = queue.erase(it);
           } else {
@@ -118,10 +127,7 @@ struct Server {
           r->t_end = now;
           r->batch_jobs = (int)batch.size();
           if (r->status == DK_ERR_CANCELLED) {
-            if (rc == DK_OK) {
-              std::lock_guard<std::mutex> g(me.eng->mu);
-              me.eng->release_table(outs[i].handle);
-            }
+            if (rc == DK_OK) me.eng->release_table(outs[i].handle);
             continue;  // stays CANCELLED; dk_poll reports it
           }
           r->status = rc;
@@ -188,6 +194,10 @@ int dk_submit(dk_ctx* ctx, const char* text, uint64_t nbytes, const dk_input_des
   r->nbytes = nbytes;
   r->desc = *desc;
   r->est = Server::estimate(*desc, nbytes);
+  {
+    const uint64_t lines = (nbytes + desc->line_width) / ((uint64_t)desc->line_width + 1);
+    r->kmers = lines * (desc->line_width >= desc->k ? (uint64_t)(desc->line_width - desc->k + 1) : 0);
+  }
   if (r->est > (uint64_t)(0.7 * (double)s->workers[0].budget)) return DK_ERR_ADMISSION;
   {
     std::lock_guard<std::mutex> lk(s->mu);
@@ -280,7 +290,6 @@ int serve_release(Server* s, uint64_t handle) {
   const int w = (int)(handle >> 48) - 1;
   if (!s || w < 0 || w >= (int)s->workers.size()) return DK_ERR_NOT_FOUND;
   Engine* e = s->workers[w].eng.get();
-  std::lock_guard<std::mutex> g(e->mu);
-  return e->release_table(handle & ((1ull << 48) - 1));
+  return e->release_table(handle & ((1ull << 48) - 1));  // the pool has its own lock
 }
 }  // namespace dk
