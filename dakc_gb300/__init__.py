@@ -285,6 +285,31 @@ class Engine:
                 self.free_table(outs[j])
         return nk, nd
 
+    def count_batch_raw(self, texts, line_width: int, k: int, variant: int = VARIANT_AUTO):
+        """dk_count_batch returning the raw dk_table structs (still owned by the
+        engine: copy with table_result, release with free_table)."""
+        keep = [_buf_ptr(t) for t in texts]
+        jobs = (Job * max(1, len(texts)))()
+        for j, (ptr, n, _) in enumerate(keep):
+            jobs[j].text = ptr
+            jobs[j].nbytes = n
+        outs = (Table * max(1, len(texts)))()
+        d = self.desc(line_width, k, variant)
+        self._check(self.lib.dk_count_batch(self.h, jobs, len(texts), ctypes.byref(d), outs),
+                    "dk_count_batch")
+        return [outs[j] for j in range(len(texts))]
+
+    @staticmethod
+    def table_result(t: Table) -> CountResult:
+        """Copy a host-resident dk_table into numpy arrays."""
+        nd = int(t.n)
+        if nd:
+            kmers = np.ctypeslib.as_array(t.kmers, shape=(nd,)).copy()
+            counts = np.ctypeslib.as_array(t.counts, shape=(nd,)).copy()
+        else:
+            kmers, counts = np.zeros(0, np.uint64), np.zeros(0, np.uint32)
+        return CountResult(kmers, counts, int(t.n_kmers), int(t.variant_used))
+
     def count_batch(self, texts, line_width: int, k: int, variant: int = VARIANT_AUTO
                     ) -> list[CountResult]:
         """Count each read set of `texts` (one pipeline, memory-bounded waves)."""

@@ -64,3 +64,55 @@ def test_batch_many_small_jobs(engine):
     for j, t in enumerate(texts):
         keys, counts, nk = pyoracle.count(t, 100, 21)
         assert got[j].n_kmers == nk and np.array_equal(got[j].kmers, keys)
+
+
+def test_batch_mixes_pinned_and_pageable_reads():
+    """Page-locked jobs go straight to DMA, pageable ones through the staging
+    slots; a staged run must never overwrite a pinned job's bytes."""
+    texts = job_texts(18, seed=7, max_reads=2500)
+    pin = [dk.PinnedBuffer(t.size) for t in texts[::2]]
+    mixed = []
+    for j, t in enumerate(texts):
+        if j % 2 == 0:
+            b = pin[j // 2]
+            b.array[:] = t
+            mixed.append(b.array)
+        else:
+            mixed.append(t)
+    with dk.Engine(0, mem_budget=160 << 20) as eng:      # several pipelined waves
+        got = eng.count_batch(mixed, 250, 31, dk.VARIANT_HASH)
+        st = eng.stats()
+    assert st["n_waves"] >= 2
+    for j, t in enumerate(texts):
+        keys, counts, nk = pyoracle.count(t, 250, 31)
+        assert got[j].n_kmers == nk and np.array_equal(got[j].kmers, keys), j
+        assert np.array_equal(got[j].counts, counts), j
+    for b in pin:
+        b.free()
+
+
+def test_batch_tables_free_while_another_batch_runs():
+    """Tables are returned to the pool under their own lock: freeing results of
+    one batch while the next runs keeps every table intact."""
+    import threading
+    texts = job_texts(30, seed=9, max_reads=3000)
+    expect = [pyoracle.count(t, 250, 31) for t in texts]
+    with dk.Engine(0) as eng:
+        first = eng.count_batch_raw(texts[:15], 250, 31, dk.VARIANT_HASH)
+        out = {}
+
+        def run_second():
+            out["second"] = eng.count_batch(texts[15:], 250, 31, dk.VARIANT_HASH)
+
+        th = threading.Thread(target=run_second)
+        th.start()
+        for j, t in enumerate(first):                   # free while the second runs
+            r = dk.Engine.table_result(t)
+            eng.free_table(t)
+            keys, counts, nk = expect[j]
+            assert r.n_kmers == nk and np.array_equal(r.kmers, keys), j
+            assert np.array_equal(r.counts, counts), j
+        th.join()
+    for j, r in enumerate(out["second"]):
+        keys, counts, nk = expect[15 + j]
+        assert r.n_kmers == nk and np.array_equal(r.kmers, keys), 15 + j
