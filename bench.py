@@ -304,6 +304,62 @@ def run_served(texts, rate, n_jobs, variant, workers, max_batch, seed=5):
             "max_batch": max_batch}
 
 
+def run_formats(steps: int):
+    """The next rows of the path, timed end to end through their C calls on
+    the C1-sized read set (100,000 reads of 100-250 bp from a 1 Mbp genome):
+    FASTQ -> DAKC lines -> count, FASTA with the PakMan* convention, and the
+    table operations (histogram + cut-off, filter, lookups, packed records)
+    on the C2 table kept on the device."""
+    import dakc_gb300 as dk
+    from dakc_gb300 import synth
+    spec = synth.batch_specs(1, seed=11)[0]
+    spec = synth.JobSpec(spec.job_id, spec.seed, 1_000_000, 100_000)
+    text = synth.batch_job_text(spec, line_width=250)
+    reads = [bytes(l).rstrip(b"M") for l in text.reshape(-1, 251)[:, :250]]
+    fq = b"".join(b"@r%d\n%s\n+\n%s\n" % (i, r, b"I" * len(r)) for i, r in enumerate(reads))
+    fa = b"".join(b">r%d\n%s\n" % (i, r) for i, r in enumerate(reads))
+    out = {"mode": "formats", "workload": "100,000 reads of 100-250 bp, k = 31"}
+
+    def timed(fn):
+        fn()
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            r = fn()
+        return (time.perf_counter() - t0) / steps, r
+
+    with dk.Engine(0) as eng:
+        for name, buf, fmt, conv in (("fastq_dakc", fq, dk.FORMAT_FASTQ, dk.CONV_DAKC),
+                                     ("fasta_pakman", fa, dk.FORMAT_FASTA, dk.CONV_PAKMAN)):
+            pin = dk.PinnedBuffer(len(buf))
+            pin.array[:] = np.frombuffer(buf, np.uint8)
+            sec, (res, width) = timed(lambda: eng.count_format(pin.array, fmt, 31, conv))
+            out[name] = {"input_bytes": len(buf), "line_width": width, "k_mers": res.n_kmers,
+                         "distinct": int(res.kmers.size), "ms": 1e3 * sec,
+                         "kmers_per_s": res.n_kmers / sec, "input_gb_per_s": len(buf) / sec / 1e9,
+                         "note": "host FASTQ/FASTA in, host table out (dk_count_format)"}
+            pin.free()
+        rs, _ = make_workload("large_100m", 1.0)
+        t = eng.count_table(rs.text, 150, 31, dk.VARIANT_AUTO, dk.RESIDENT_DEVICE)
+        n = int(t.n)
+        sec, (hist, mb) = timed(lambda: eng.histogram(t, 256))
+        out["histogram_cutoff"] = {"entries": n, "ms": 1e3 * sec, "entries_per_s": n / sec,
+                                   "num_buckets": 256, "min_bucket": mb}
+
+        def filt():
+            f = eng.filter_table(t, mb)
+            kept = int(f.n)
+            eng.free_table(f)
+            return kept
+        sec, kept = timed(filt)
+        out["filter"] = {"entries": n, "kept": kept, "ms": 1e3 * sec, "entries_per_s": n / sec}
+        q = np.random.Generator(np.random.PCG64(3)).integers(0, 1 << 62, 10_000_000, dtype=np.uint64)
+        sec, _ = timed(lambda: eng.lookup(t, q))
+        out["lookup"] = {"queries": int(q.size), "table": n, "ms": 1e3 * sec,
+                         "queries_per_s": q.size / sec, "note": "host queries in, host counts out"}
+        eng.free_table(t)
+    return out
+
+
 def alg_bytes(st: dict, nbytes: int) -> list[float]:
     nk, nd, npart = st["n_kmers"], st["n_distinct"], st["n_partitioned"]
     return [nbytes,                    # extract_count: read the text
@@ -332,7 +388,7 @@ def main():
     ap.add_argument("--no-autotune", action="store_true",
                     help="count with the automatic parameters instead of the autotuned ones")
     ap.add_argument("--e2e-steps", type=int, default=3)
-    ap.add_argument("--mode", default="count", choices=["count", "batch", "serve"],
+    ap.add_argument("--mode", default="count", choices=["count", "batch", "serve", "formats"],
                     help="count: the headline line; batch / serve: batched and served forms")
     ap.add_argument("--jobs", type=int, default=256, help="read sets for batch / serve modes")
     ap.add_argument("--rates", default="10,30,100,300,1000,2000")
@@ -343,6 +399,10 @@ def main():
                     help="skip the batched / served summaries in the headline line")
     args = ap.parse_args()
     rank, world, local = dist_env()
+
+    if args.mode == "formats" and args.impl == "engine":
+        print(json.dumps(run_formats(args.steps)), flush=True)
+        return 0
 
     if args.mode in ("batch", "serve") and args.impl == "engine":
         import dakc_gb300 as dk

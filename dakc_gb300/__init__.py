@@ -37,8 +37,9 @@ DK_ERR_CANCELLED = -9
 DK_ERR_NO_DEVICE = -10
 
 VARIANT_AUTO, VARIANT_SORT, VARIANT_HASH = 0, 1, 2
+CONV_DAKC, CONV_PAKMAN = 0, 1
+FORMAT_LINES, FORMAT_FASTQ, FORMAT_FASTA = 0, 1, 2
 RESIDENT_HOST, RESIDENT_DEVICE = 0, 1
-CONV_DAKC = 0
 
 # exported symbols, in the order include/dakc_gb300.h declares them
 ABI_SYMBOLS = [
@@ -47,6 +48,8 @@ ABI_SYMBOLS = [
     "dk_host_alloc", "dk_host_free", "dk_count_small_noalloc", "dk_count_batch",
     "dk_serve_start", "dk_submit", "dk_poll", "dk_wait", "dk_cancel", "dk_serve_stop",
     "dk_autotune", "dk_autotune_reset",
+    "dk_table_histogram", "dk_table_filter", "dk_table_lookup", "dk_table_pairs",
+    "dk_count_format",
 ]
 
 
@@ -139,6 +142,13 @@ def load_library(path: str = LIB_PATH):
     lib.dk_last_stats.argtypes = [vp, ctypes.POINTER(Stats)]
     lib.dk_autotune.argtypes = [vp, vp, u64, ctypes.POINTER(InputDesc), ctypes.POINTER(Tune)]
     lib.dk_autotune_reset.argtypes = [vp]
+    lib.dk_table_histogram.argtypes = [vp, ctypes.POINTER(Table), ctypes.c_uint32, vp,
+                                       ctypes.POINTER(ctypes.c_uint32)]
+    lib.dk_table_filter.argtypes = [vp, ctypes.POINTER(Table), ctypes.c_uint32, ctypes.POINTER(Table)]
+    lib.dk_table_lookup.argtypes = [vp, ctypes.POINTER(Table), vp, u64, vp]
+    lib.dk_table_pairs.argtypes = [vp, ctypes.POINTER(Table), vp]
+    lib.dk_count_format.argtypes = [vp, vp, u64, i32, ctypes.POINTER(InputDesc),
+                                    ctypes.POINTER(Table), ctypes.POINTER(ctypes.c_int)]
     lib.dk_num_lines.argtypes = [vp, u64, i32]
     lib.dk_num_lines.restype = ctypes.c_int64
     lib.dk_count_batch.argtypes = [vp, ctypes.POINTER(Job), i32, ctypes.POINTER(InputDesc),
@@ -247,6 +257,61 @@ class Engine:
         self._check(fn(self.h, ctypes.c_void_p(ptr), nbytes, ctypes.byref(d), ctypes.byref(t)),
                     "dk_count")
         return t
+
+    def count_format(self, text, fmt: int, k: int, convention: int = 0, line_width: int = 0,
+                     variant: int = VARIANT_AUTO):
+        """Count reads given as FASTQ / FASTA / one per line (dk_count_format);
+        returns (CountResult, the line width they were laid out at)."""
+        ptr, n, keep = _buf_ptr(text)
+        d = self.desc(max(line_width, 0), k, variant)
+        d.convention = convention
+        d.line_width = line_width
+        t, w = Table(), ctypes.c_int(0)
+        self._check(self.lib.dk_count_format(self.h, ctypes.c_void_p(ptr), n, fmt, ctypes.byref(d),
+                                             ctypes.byref(t), ctypes.byref(w)), "dk_count_format")
+        try:
+            return self.table_result(t), int(w.value)
+        finally:
+            self.free_table(t)
+
+    def count_table(self, text, line_width: int, k: int, variant: int = VARIANT_AUTO,
+                    residency: int = RESIDENT_HOST) -> Table:
+        """dk_count keeping the raw table (release it with free_table)."""
+        ptr, n, keep = _buf_ptr(text)
+        return self.count_raw(ptr, n, self.desc(line_width, k, variant, residency))
+
+    def histogram(self, t: Table, num_buckets: int):
+        """(hist[0..num_buckets), PakMan*'s min bucket) of a table (dk_table_histogram)."""
+        hist = np.zeros(num_buckets, np.uint64)
+        mb = ctypes.c_uint32(0)
+        self._check(self.lib.dk_table_histogram(self.h, ctypes.byref(t), num_buckets,
+                                                hist.ctypes.data, ctypes.byref(mb)),
+                    "dk_table_histogram")
+        return hist, int(mb.value)
+
+    def filter_table(self, t: Table, min_count: int) -> Table:
+        """The entries of t with count >= min_count, as a new table (dk_table_filter)."""
+        out = Table()
+        self._check(self.lib.dk_table_filter(self.h, ctypes.byref(t), min_count, ctypes.byref(out)),
+                    "dk_table_filter")
+        return out
+
+    def lookup(self, t: Table, queries) -> np.ndarray:
+        """Counts of query k-mers in t, 0 when absent (dk_table_lookup)."""
+        q = np.ascontiguousarray(queries, dtype=np.uint64)
+        out = np.zeros(q.size, np.uint32)
+        self._check(self.lib.dk_table_lookup(self.h, ctypes.byref(t), q.ctypes.data, q.size,
+                                             out.ctypes.data), "dk_table_lookup")
+        return out
+
+    PAIR_DTYPE = np.dtype([("kmer", "<u8"), ("count", "<u4")], align=False)  # 12-byte records
+
+    def pairs(self, t: Table) -> np.ndarray:
+        """The table as packed 12-byte (k-mer, count) records (dk_table_pairs)."""
+        out = np.zeros(int(t.n), dtype=self.PAIR_DTYPE)
+        self._check(self.lib.dk_table_pairs(self.h, ctypes.byref(t), out.ctypes.data),
+                    "dk_table_pairs")
+        return out
 
     def free_table(self, t: Table):
         self._check(self.lib.dk_table_free(self.h, ctypes.byref(t)), "dk_table_free")

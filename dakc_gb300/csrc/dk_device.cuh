@@ -9,16 +9,26 @@ namespace dev {
 
 __device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31; }
 
-// base code of one text byte: C=0 A=1 T=2 G=3 (either case), M/m=0xF0, else 0xFF
-__device__ __forceinline__ void init_lut(uint8_t* lut) {
+// Code of one text byte.
+// DAKC (conv 0): C=0 A=1 T=2 G=3 (either case), M/m=0xF0 (ends the line),
+//   anything else 0xFF (splits the run) -- char2base, dakc/src/common/common.hpp:72-92.
+// PakMan* (conv 1): (byte >> 1) & 7 for every byte (A=0 C=1 T=2 G=3; other
+//   bytes give 4..7 and are OR'ed into the window as PakMan* does,
+//   char_to_el / kmer_shift, pakman_star/includes/distribute_kmers.h), and
+//   '\n' (the end of a read) = 0xF0.
+__device__ __forceinline__ void init_lut(uint8_t* lut, int conv = 0) {
   for (int c = threadIdx.x; c < 256; c += blockDim.x) {
     uint8_t v = 0xFF;
-    const int u = c | 0x20;  // exact case fold for the five letters below
-    if (u == 'c') v = 0;
-    else if (u == 'a') v = 1;
-    else if (u == 't') v = 2;
-    else if (u == 'g') v = 3;
-    else if (u == 'm') v = 0xF0;
+    if (conv == 1) {
+      v = c == '\n' ? 0xF0 : (uint8_t)((c >> 1) & 7);
+    } else {
+      const int u = c | 0x20;  // exact case fold for the five letters below
+      if (u == 'c') v = 0;
+      else if (u == 'a') v = 1;
+      else if (u == 't') v = 2;
+      else if (u == 'g') v = 3;
+      else if (u == 'm') v = 0xF0;
+    }
     lut[c] = v;
   }
 }

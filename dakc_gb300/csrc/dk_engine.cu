@@ -72,21 +72,6 @@ void Arena::release(Engine* e, DevBuf& b) {
   b.cap = 0;
 }
 
-#define DK_CUDA(call)                                                        \
-  do {                                                                       \
-    cudaError_t _e = (call);                                                 \
-    if (_e != cudaSuccess) {                                                 \
-      e->set_error(std::string(#call) + ": " + cudaGetErrorString(_e));     \
-      return DK_ERR_CUDA;                                                    \
-    }                                                                        \
-  } while (0)
-
-#define DK_TRY(expr)            \
-  do {                          \
-    int _rc = (expr);           \
-    if (_rc != DK_OK) return _rc; \
-  } while (0)
-
 void Engine::set_error(const std::string& m) {
   std::lock_guard<std::mutex> g(err_mu);
   last_error = m;
@@ -167,7 +152,8 @@ int Engine::init(const dk_config* cfg) {
 Engine::~Engine() {
   for (cudaStream_t st : {stream, s_in, s_out})
     if (st) cudaStreamSynchronize(st);
-  for (DevBuf* b : {&text, &text2, &keysA, &keysB, &cnt, &H, &O, &nodes, &tiles, &TH, &finals, &ctrs})
+  for (DevBuf* b : {&text, &text2, &keysA, &keysB, &cnt, &H, &O, &nodes, &tiles, &TH, &finals, &ctrs,
+                    &aux})
     Arena::release(this, *b);
   for (auto& t : tables) {
     if (t.on_device) {
@@ -221,6 +207,12 @@ int Engine::write_small(void* ddst, const void* hsrc, size_t bytes) {
     DK_CUDA(cudaStreamSynchronize(stream));  // the mailbox is refilled next
   }
   return DK_OK;
+}
+
+// DAKC's convention for any line width; PakMan*'s on the thread-per-line
+// kernels (lines of at most kLineMaxW bytes)
+bool convention_ok(const dk_input_desc& d) {
+  return d.convention == DK_CONV_DAKC || (d.convention == DK_CONV_PAKMAN && d.line_width <= kLineMaxW);
 }
 
 // framing: lines in a buffer of nbytes (host-side part; NUL lines are found on device)
@@ -355,7 +347,7 @@ int Engine::count_batch(const dk_job* jobs, int njobs, const dk_input_desc* desc
   }
   for (int j = 0; j < njobs; ++j) std::memset(&outs[j], 0, sizeof(dk_table));
   if (desc->k < 1 || desc->k > 32 || desc->line_width < 1 || desc->line_width > 1024 ||
-      desc->convention != DK_CONV_DAKC || desc->variant < DK_VARIANT_AUTO ||
+      !convention_ok(*desc) || desc->variant < DK_VARIANT_AUTO ||
       desc->variant > DK_VARIANT_HASH || desc->residency != DK_RESIDENT_HOST) {
     set_error("invalid input descriptor (batch results are host-resident)");
     return DK_ERR_INVALID_ARG;
@@ -762,6 +754,7 @@ int Engine::count_device(const uint8_t* d_text, uint64_t nbytes, const dk_input_
   a.kmask = (~0ull) >> (64 - 2 * k);
   a.shift1 = shift1;
   a.F1 = F1;
+  a.conv = desc.convention;
   a.njobs = js ? js->njobs : 0;
   a.job_start = js ? js->d_start : nullptr;
   a.job_end = js ? js->d_end : nullptr;
@@ -946,7 +939,7 @@ int Engine::autotune(const char* text, uint64_t nbytes, const dk_input_desc* des
   Engine* e = this;
   std::lock_guard<std::mutex> g(mu);
   if (!desc || (!text && nbytes) || desc->k < 1 || desc->k > 32 || desc->line_width < 1 ||
-      desc->line_width > 1024 || desc->convention != DK_CONV_DAKC) {
+      desc->line_width > 1024 || !convention_ok(*desc)) {
     set_error("invalid autotune arguments");
     return DK_ERR_INVALID_ARG;
   }
@@ -1031,15 +1024,21 @@ int Engine::autotune(const char* text, uint64_t nbytes, const dk_input_desc* des
 
 int Engine::count(const char* text, uint64_t nbytes, bool text_on_device, const dk_input_desc* desc,
                   dk_table* out) {
-  Engine* e = this;
   std::lock_guard<std::mutex> g(mu);
+  return count_locked(text, nbytes, text_on_device, desc, out);
+}
+
+// dk_count's body; the caller holds `mu`
+int Engine::count_locked(const char* text, uint64_t nbytes, bool text_on_device,
+                         const dk_input_desc* desc, dk_table* out) {
+  Engine* e = this;
   const auto w0 = std::chrono::steady_clock::now();
   if (!desc || !out || (!text && nbytes)) {
     set_error("null argument");
     return DK_ERR_INVALID_ARG;
   }
   std::memset(out, 0, sizeof(*out));
-  if (desc->k < 1 || desc->k > 32 || desc->line_width < 1 || desc->convention != DK_CONV_DAKC ||
+  if (desc->k < 1 || desc->k > 32 || desc->line_width < 1 || !convention_ok(*desc) ||
       desc->variant < DK_VARIANT_AUTO || desc->variant > DK_VARIANT_HASH ||
       (desc->residency != DK_RESIDENT_HOST && desc->residency != DK_RESIDENT_DEVICE)) {
     set_error("invalid input descriptor");

@@ -13,6 +13,23 @@
 
 namespace dk {
 
+// status plumbing of the engine's host code: a failed CUDA call records its
+// text on engine `e` (in scope) and returns DK_ERR_CUDA
+#define DK_CUDA(call)                                                        \
+  do {                                                                       \
+    cudaError_t _e = (call);                                                 \
+    if (_e != cudaSuccess) {                                                 \
+      e->set_error(std::string(#call) + ": " + cudaGetErrorString(_e));     \
+      return DK_ERR_CUDA;                                                    \
+    }                                                                        \
+  } while (0)
+
+#define DK_TRY(expr)            \
+  do {                          \
+    int _rc = (expr);           \
+    if (_rc != DK_OK) return _rc; \
+  } while (0)
+
 struct DevBuf {
   void* p = nullptr;
   size_t cap = 0;
@@ -45,6 +62,7 @@ struct DeviceTable {
 };
 
 int64_t frame_lines(uint64_t nbytes, int W);
+bool convention_ok(const dk_input_desc& d);
 
 struct Engine;
 
@@ -128,6 +146,13 @@ struct Engine {
   static uint64_t shape_key(int W, int k, uint64_t n_upper);
   int autotune(const char* text, uint64_t nbytes, const dk_input_desc* desc, dk_tune* out);
 
+  // operations on finished tables (dk_table_ops.cu)
+  DevBuf aux;  // their scratch
+  int table_histogram(const dk_table* t, uint32_t nb, uint64_t* hist, uint32_t* min_bucket);
+  int table_filter(const dk_table* t, uint32_t min_count, dk_table* out);
+  int table_lookup(const dk_table* t, const uint64_t* q, uint64_t nq, uint32_t* counts);
+  int table_pairs(const dk_table* t, void* out);
+
   int init(const dk_config* cfg);
   ~Engine();
   void set_error(const std::string& m);
@@ -147,6 +172,11 @@ struct Engine {
   DevBuf jobmeta;  // device job_start / job_end / job_nul
   int count(const char* text, uint64_t nbytes, bool text_on_device, const dk_input_desc* desc,
             dk_table* out);
+  int count_locked(const char* text, uint64_t nbytes, bool text_on_device,
+                   const dk_input_desc* desc, dk_table* out);
+  // reads in another layout (dk_ingest.cu)
+  int count_format(const char* text, uint64_t nbytes, int format, const dk_input_desc* desc,
+                   dk_table* out, int* width);
 };
 
 }  // namespace dk

@@ -72,7 +72,6 @@ constexpr size_t kMaxSmemPerBlock = 232448;  // opt-in shared memory per block (
 constexpr int kLineThreads = 256;        // thread-per-line level-1 kernels: lines per tile
 constexpr int kLineMaxW = 256;           // longer lines use the warp-per-line kernels
 constexpr int kLineChunk = 16;           // positions per line in one chunked-scatter chunk
-constexpr bool kPlainChunkedScatter = true;  // plain counts: chunked thread-per-line scatter
 
 struct ExtractArgs {
   const uint8_t* text;  // device text, 16-byte aligned
@@ -83,6 +82,7 @@ struct ExtractArgs {
   uint64_t kmask;
   int shift1;  // level-1 bucket = key >> shift1 (plain mode)
   int F1;      // number of level-1 buckets
+  int conv;    // k-mer convention: 0 DAKC, 1 PakMan* (thread-per-line kernels only)
   // batch ("jobs") mode when njobs > 0: the text is the concatenation of njobs
   // read sets; job j owns lines [job_start[j], job_start[j+1]) of which lines
   // >= job_end[j] are not parsed (a NUL-led line ends that job), and the

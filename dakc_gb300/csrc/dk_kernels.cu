@@ -295,14 +295,24 @@ __global__ void k_l1_offsets_rows(const uint32_t* __restrict__ H, int G, int F1,
 // says whether a k-mer ends there (DAKC's rules: 'M' ends the line, any other
 // non-base splits it, and k = 1 keeps a final run only if it starts before
 // W-1, kcounter_funcs.cpp:69-111).
+// With the PakMan* convention (pak) no byte splits a run: every code is
+// OR'ed into the shifted window ((key << 2) | code) and a k-mer ends at every
+// position from the k-th on (Sliding_window, pakman_star/src/
+// kmer_counting.cpp:313-341).
 struct LineRoll {
   uint64_t key;
   int run;
   uint32_t prev;
   bool stopped;
   __device__ __forceinline__ void reset() { key = 0; run = 0; prev = 0; stopped = false; }
-  __device__ __forceinline__ bool step(uint32_t c, int p, int W, int k, uint64_t kmask) {
+  __device__ __forceinline__ bool step(uint32_t c, int p, int W, int k, uint64_t kmask,
+                                       bool pak = false) {
     if (stopped || c == 0xF0u) { stopped = true; return false; }
+    if (pak) {
+      key = ((key << 2) | c) & kmask;
+      ++run;
+      return run >= k;
+    }
     bool emit = false;
     if (c >= 4u) {
       run = 0;
@@ -368,7 +378,7 @@ __global__ void __launch_bounds__(kLineThreads) k_l1_lines_count(ExtractArgs a,
   TextTiles T;
   setup_tiles(&T, a, smraw, bb);
   for (int b = threadIdx.x; b < a.F1; b += blockDim.x) cnt[b] = 0;
-  init_lut(lut);
+  init_lut(lut, a.conv);
   __syncthreads();
   uint32_t mine = 0;
   const uint32_t nt = T.ntiles();
@@ -395,7 +405,7 @@ __global__ void __launch_bounds__(kLineThreads) k_l1_lines_count(ExtractArgs a,
         for (int u = 0; u < 4; ++u) c4[u] = p0 + u < W ? lut[line[p0 + u]] : 0xF0u;
 #pragma unroll
         for (int u = 0; u < 4; ++u)
-          if (r.step(c4[u], p0 + u, W, k, a.kmask)) {
+          if (r.step(c4[u], p0 + u, W, k, a.kmask, a.conv == 1)) {
             atomicAdd(&cnt[a.njobs ? jb(r.key) : (uint32_t)(r.key >> a.shift1)], 1u);
             ++mine;
           }
@@ -440,7 +450,7 @@ __global__ void __launch_bounds__(kLineThreads, 2) k_l1_lines_chunked(ExtractArg
     cursor[b] = O[(size_t)blockIdx.x * F1 + b];
     ccount[b] = 0;
   }
-  init_lut(lut);
+  init_lut(lut, a.conv);
   __syncthreads();
   const uint32_t nt = T.ntiles();
   if (threadIdx.x == 0 && nt) T.issue(0);
@@ -459,12 +469,12 @@ __global__ void __launch_bounds__(kLineThreads, 2) k_l1_lines_chunked(ExtractArg
     if (!live) r.stopped = true;
     // warm-up: positions before the first possible k-mer end emit nothing
     const int warm = min(k - 1, W);
-    for (int p = 0; p < warm; ++p) r.step(r.stopped ? 0xF0u : lut[line[p]], p, W, k, a.kmask);
+    for (int p = 0; p < warm; ++p) r.step(r.stopped ? 0xF0u : lut[line[p]], p, W, k, a.kmask, a.conv == 1);
     for (int p0 = warm; p0 < W; p0 += kLineChunk) {  // uniform over the block
       const int p1 = min(W, p0 + kLineChunk);
       const LineRoll r0 = r;
       for (int p = p0; p < p1 && !r.stopped; ++p)
-        if (r.step(lut[line[p]], p, W, k, a.kmask))
+        if (r.step(lut[line[p]], p, W, k, a.kmask, a.conv == 1))
           atomicAdd(&ccount[(uint32_t)(r.key >> a.shift1)], 1u);
       __syncthreads();
       for (int b = threadIdx.x; b < F1; b += blockDim.x) {
@@ -475,7 +485,7 @@ __global__ void __launch_bounds__(kLineThreads, 2) k_l1_lines_chunked(ExtractArg
       const uint32_t Tn = block_scan_array<uint32_t>(coff, F1, tmp);
       r = r0;
       for (int p = p0; p < p1 && !r.stopped; ++p)
-        if (r.step(lut[line[p]], p, W, k, a.kmask)) {
+        if (r.step(lut[line[p]], p, W, k, a.kmask, a.conv == 1)) {
           const uint32_t b = (uint32_t)(r.key >> a.shift1);
           const uint32_t pos = coff[b] + atomicAdd(&ccount[b], 1u);
           if (DK_OK_IDX(pos < (uint32_t)blockDim.x * kLineChunk, 41, pos)) stage[pos] = r.key;
@@ -525,7 +535,7 @@ __global__ void __launch_bounds__(kLineThreads) k_l1_lines_direct(ExtractArgs a,
     cursor[b] = O[(size_t)blockIdx.x * a.F1 + b];
     cnt[b] = 0;
   }
-  init_lut(lut);
+  init_lut(lut, a.conv);
   __syncthreads();
   const uint32_t nt = T.ntiles();
   if (threadIdx.x == 0 && nt) T.issue(0);
@@ -551,7 +561,7 @@ __global__ void __launch_bounds__(kLineThreads) k_l1_lines_direct(ExtractArgs a,
         for (int u = 0; u < 4; ++u) c4[u] = p0 + u < W ? lut[line[p0 + u]] : 0xF0u;
 #pragma unroll
         for (int u = 0; u < 4; ++u)
-          if (r.step(c4[u], p0 + u, W, k, a.kmask)) {
+          if (r.step(c4[u], p0 + u, W, k, a.kmask, a.conv == 1)) {
             const uint32_t b = a.njobs ? jb(r.key) : (uint32_t)(r.key >> a.shift1);
             keys_out[cursor[b] + atomicAdd(&cnt[b], 1u)] = r.key;
           }
@@ -1723,8 +1733,7 @@ static size_t chunked_smem(const ExtractArgs& a) {
 }
 // plain counts whose chunked thread-per-line scatter fits two CTAs per SM
 static bool chunked_scatter(const ExtractArgs& a) {
-  return kPlainChunkedScatter && !a.njobs && a.W <= kLineMaxW &&
-         chunked_smem(a) <= kMaxSmemPerBlock / 2 - 1024;
+  return !a.njobs && a.W <= kLineMaxW && chunked_smem(a) <= kMaxSmemPerBlock / 2 - 1024;
 }
 
 int launch_l1_count(const ExtractArgs& a, int grid, uint32_t* H, unsigned long long* counters,
@@ -1767,11 +1776,15 @@ static size_t scatter_smem(int W, int F1, bool jobs) {
 
 int l1_max_buckets(int W, bool jobs) {
   int f = 1 << kMaxL1Bits;
+  ExtractArgs a{};
+  a.W = W;
+  a.F1 = f;
   if (direct_scatter(W, jobs)) {
-    ExtractArgs a{};
-    a.W = W;
-    a.F1 = f;
     while (f > 1 && lines_smem(a, true) > kMaxSmemPerBlock) a.F1 = (f >>= 1);
+    return f;
+  }
+  if (!jobs && W <= kLineMaxW) {  // the chunked thread-per-line scatter, two CTAs per SM
+    while (f > 1 && !chunked_scatter(a)) a.F1 = (f >>= 1);
     return f;
   }
   while (f > 1 && scatter_smem(W, f, jobs) > kMaxSmemPerBlock) f >>= 1;

@@ -187,7 +187,7 @@ int dk_submit(dk_ctx* ctx, const char* text, uint64_t nbytes, const dk_input_des
   Server* s = ctx ? dk::server_of(ctx) : nullptr;
   if (!s || !desc || !ticket || (!text && nbytes)) return DK_ERR_INVALID_ARG;
   if (desc->k < 1 || desc->k > 32 || desc->line_width < 1 || desc->line_width > 1024 ||
-      desc->convention != DK_CONV_DAKC || dk::frame_lines(nbytes, desc->line_width) < 0)
+      !dk::convention_ok(*desc) || dk::frame_lines(nbytes, desc->line_width) < 0)
     return DK_ERR_INVALID_ARG;
   auto r = std::make_shared<dk::Request>();
   r->text = text;

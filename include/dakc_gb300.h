@@ -60,7 +60,16 @@ extern "C" {
 #define DK_VARIANT_HASH 2  /* partition + shared-memory hash aggregation          */
 
 /* k-mer conventions */
-#define DK_CONV_DAKC 0     /* the only one: see above                              */
+#define DK_CONV_DAKC 0     /* DAKC's rules, above                                  */
+#define DK_CONV_PAKMAN 1   /* PakMan*'s: every byte b of a read is the 2-bit code
+                              (b >> 1) & 7 OR'ed into the shifted window (A=0 C=1
+                              T=2 G=3; other bytes give 4..7 as PakMan* computes
+                              them, char_to_el / kmer_shift, pakman_star/includes/
+                              distribute_kmers.h), nothing splits a run, a read
+                              ends at '\n' (padding), and a k-mer ends at each
+                              position from the k-th (Sliding_window,
+                              pakman_star/src/kmer_counting.cpp:283-341).  Lines
+                              of at most 256 bytes.                                */
 
 /* where dk_count leaves the table */
 #define DK_RESIDENT_HOST 0   /* kmers/counts are host arrays owned by the context  */
@@ -78,7 +87,7 @@ typedef struct {
 typedef struct {
   int line_width;  /* READLEN: bytes per line before the terminator (>= 1)      */
   int k;           /* KMERLEN: 1..32                                            */
-  int convention;  /* DK_CONV_DAKC                                               */
+  int convention;  /* DK_CONV_DAKC or DK_CONV_PAKMAN                             */
   int variant;     /* DK_VARIANT_*                                               */
   int residency;   /* DK_RESIDENT_*                                              */
   int l1_bits;     /* tuning: level-1 partition bits, 0 = automatic (<= 12)     */
@@ -162,6 +171,21 @@ int dk_last_stats(dk_ctx* ctx, dk_stats* out);
 int dk_count_batch(dk_ctx* ctx, const dk_job* jobs, int njobs, const dk_input_desc* desc,
                    dk_table* outs);
 
+/* --- reads in other layouts ------------------------------------------- */
+#define DK_FORMAT_LINES 0  /* one read per line, any length                      */
+#define DK_FORMAT_FASTQ 1  /* 4-line records; the reads are line 2 of each
+                              (syngen/fq2txtmaker.sh:12)                          */
+#define DK_FORMAT_FASTA 2  /* from the first '>': header line, sequence line, ...
+                              (pakman_star/src/kmer_counting.cpp:283-300)         */
+/* Count reads given in `format` (host buffer): they are laid out on the GPU
+ * as fixed-width lines -- width desc->line_width, or the longest read when it
+ * is 0 -- padded as the reference's conversion pads them (DAKC convention:
+ * 'M', with spaces turned into 'M' for FASTQ, syngen/fq2txtmaker.sh:12-18;
+ * PakMan* convention: '\n', where its reader ends a read), and counted as
+ * dk_count counts those lines.  *line_width (optional) receives the width. */
+int dk_count_format(dk_ctx* ctx, const char* text, uint64_t nbytes, int format,
+                    const dk_input_desc* desc, dk_table* out, int* line_width);
+
 /* Number of lines dk_count will parse for this buffer under the framing rules
  * above (host-side, no GPU work); negative status for a malformed size. */
 int64_t dk_num_lines(const char* text, uint64_t nbytes, int line_width);
@@ -197,6 +221,31 @@ int dk_autotune(dk_ctx* ctx, const char* text, uint64_t nbytes, const dk_input_d
                 dk_tune* out);
 /* forget every tuned choice of the context */
 int dk_autotune_reset(dk_ctx* ctx);
+
+/* --- operations on finished tables --------------------------------------
+ * `t` is a table the library returned (host- or device-resident); kernels
+ * read it where it lies.  No counterpart in DAKC, which stops at the table;
+ * these are the consumers of the table in PakMan*, the reference's second
+ * implementation of the path. */
+
+/* hist[c] = distinct k-mers whose count is c, for c < num_buckets (hist: host
+ * array of num_buckets); *min_bucket (optional) = PakMan*'s cut-off, the
+ * first minimum of hist[1 .. num_buckets-1] (pakman_star/src/
+ * kmer_histogram.cpp:72-123); 0 when num_buckets == 1. */
+int dk_table_histogram(dk_ctx* ctx, const dk_table* t, uint32_t num_buckets, uint64_t* hist,
+                       uint32_t* min_bucket);
+/* *out = the k-mers of t whose count is >= min_count, in order, with the same
+ * residency (a new table: release both with dk_table_free); out->n_kmers is
+ * the sum of the kept counts.  PakMan* keeps count >= min_bucket
+ * (kmer_histogram.cpp:123-130). */
+int dk_table_filter(dk_ctx* ctx, const dk_table* t, uint32_t min_count, dk_table* out);
+/* counts[i] = count of queries[i] in t, 0 when absent (host arrays of n). */
+int dk_table_lookup(dk_ctx* ctx, const dk_table* t, const uint64_t* queries, uint64_t n,
+                    uint32_t* counts);
+/* The table as t->n packed 12-byte records {uint64 k-mer; uint32 count}, the
+ * layout of PakMan*'s KmerPairs (pakman_star/includes/distribute_kmers.h:
+ * 690-696); `out` (host or device, 4-byte aligned) holds 12 * t->n bytes. */
+int dk_table_pairs(dk_ctx* ctx, const dk_table* t, void* out);
 
 /* --- serving ----------------------------------------------------------- */
 /* A request loop over `workers` engine workers (each with its own CUDA

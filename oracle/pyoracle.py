@@ -177,3 +177,96 @@ def ref_table(text, line_width: int, k: int, pes: int = 1, hitter: int = 0, time
         if p.returncode != 0:
             raise OracleError(f"reference exited {p.returncode}: {p.stderr.strip()[:200]}")
         return read_table_file(out), p.stdout
+
+
+def pakman_histogram_cutoff(counts, num_buckets: int):
+    """PakMan*'s count histogram and min-bucket cut-off, restated from
+    pakman_star/src/kmer_histogram.cpp:72-130: hist[c] = distinct k-mers with
+    count c < num_buckets; min_bucket = the first minimum over hist[1:]
+    (std::min_element, :109-110), 0 when num_buckets == 0; the kept k-mers are
+    those with count >= min_bucket (:123-130)."""
+    counts = np.asarray(counts, dtype=np.uint64)
+    if num_buckets <= 0:
+        return np.zeros(0, np.uint64), 0
+    hist = np.zeros(num_buckets, np.uint64)
+    small = counts[counts < num_buckets].astype(np.int64)
+    if small.size:
+        hist += np.bincount(small, minlength=num_buckets).astype(np.uint64)[:num_buckets]
+    if num_buckets == 1:
+        return hist, 0
+    return hist, 1 + int(np.argmin(hist[1:]))
+
+
+def fq2txt(fastq: bytes) -> tuple[bytes, int]:
+    """syngen/fq2txtmaker.sh:12-18 restated: keep lines NR%4==2 (the reads of
+    4-line FASTQ records), pad each with spaces to the longest (printf
+    "%-Ns"), then turn every space into 'M' (sed 's/ /M/g').  Returns the
+    DAKC text and its line width."""
+    lines = fastq.split(b"\n")
+    if fastq.endswith(b"\n"):
+        lines = lines[:-1]
+    seqs = lines[1::4]
+    if not seqs:
+        return b"", 0
+    w = max(len(s) for s in seqs)
+    return b"".join(s.ljust(w, b" ").replace(b" ", b"M") + b"\n" for s in seqs), w
+
+
+def pakman_kmers(buf: bytes, k: int) -> np.ndarray:
+    """PakMan*'s k-mer walk over a FASTA buffer, restated from
+    Sliding_window, pakman_star/src/kmer_counting.cpp:283-341: start at the
+    first '>'; repeatedly skip a line (the header), then roll the next line
+    with kmer = ((kmer << 2) | ((byte >> 1) & 7)) & mask (char_to_el /
+    kmer_shift, pakman_star/includes/distribute_kmers.h), emitting a k-mer at
+    every byte from the k-th on; stop when fewer than k bytes remain after a
+    header (:301).  Pure Python: small inputs only."""
+    mask = (1 << (2 * k)) - 1
+    L = len(buf)
+    p = buf.find(b">")
+    if p < 0:
+        return np.zeros(0, np.uint64)
+    out = []
+    nl = 10
+    while p < L:
+        while p < L and buf[p] != nl:
+            p += 1
+        p += 1
+        if p + k > L:
+            break
+        kmer = 0
+        i = 0
+        while p < L and buf[p] != nl and i < k - 1:
+            kmer = ((kmer << 2) | ((buf[p] >> 1) & 7)) & mask
+            p += 1
+            i += 1
+        while p < L and buf[p] != nl:
+            kmer = ((kmer << 2) | ((buf[p] >> 1) & 7)) & mask
+            p += 1
+            out.append(kmer)
+        p += 1
+    return np.array(out, dtype=np.uint64)
+
+
+def table_of(kmers: np.ndarray):
+    """(sorted distinct k-mers, their counts as uint32, occurrences)."""
+    keys, counts = np.unique(np.asarray(kmers, dtype=np.uint64), return_counts=True)
+    return keys, counts.astype(np.uint32), int(np.asarray(kmers).size)
+
+
+def format_lines(text: bytes, fmt: str) -> list[bytes]:
+    """The reads of `text` in layout fmt ('lines', 'fastq', 'fasta'): the
+    bytes of each read line (FASTQ line 2 of each record, fq2txtmaker.sh:12;
+    FASTA: from the line holding the first '>', every second line,
+    kmer_counting.cpp:288-300)."""
+    lines = text.split(b"\n")
+    if text.endswith(b"\n"):
+        lines = lines[:-1]
+    if fmt == "lines":
+        return lines
+    if fmt == "fastq":
+        return lines[1::4]
+    g = text.find(b">")
+    if g < 0:
+        return []
+    h = text[:g].count(b"\n")
+    return lines[h + 1::2]

@@ -69,7 +69,7 @@ def test_batch_many_small_jobs(engine):
 def test_batch_mixes_pinned_and_pageable_reads():
     """Page-locked jobs go straight to DMA, pageable ones through the staging
     slots; a staged run must never overwrite a pinned job's bytes."""
-    texts = job_texts(18, seed=7, max_reads=2500)
+    texts = job_texts(24, seed=7, max_reads=4000)
     pin = [dk.PinnedBuffer(t.size) for t in texts[::2]]
     mixed = []
     for j, t in enumerate(texts):
@@ -79,7 +79,7 @@ def test_batch_mixes_pinned_and_pageable_reads():
             mixed.append(b.array)
         else:
             mixed.append(t)
-    with dk.Engine(0, mem_budget=160 << 20) as eng:      # several pipelined waves
+    with dk.Engine(0, mem_budget=96 << 20) as eng:       # several pipelined waves
         got = eng.count_batch(mixed, 250, 31, dk.VARIANT_HASH)
         st = eng.stats()
     assert st["n_waves"] >= 2

@@ -131,3 +131,35 @@ def test_oracle_matches_live_reference():
     mine = pyoracle.count(text, 150, 31)
     assert "kmer counting time" in out
     assert ref[2] == mine[2] and np.array_equal(ref[0], mine[0]) and np.array_equal(ref[1], mine[1])
+
+
+def test_pakman_histogram_cutoff_known_answer():
+    # counts 1,1,1,2,3,3,5,7 with 6 buckets: hist = [0,3,1,2,0,1]; first min of
+    # hist[1:] is bucket 4 (hist 0), so k-mers with count >= 4 are kept
+    hist, mb = pyoracle.pakman_histogram_cutoff([1, 1, 1, 2, 3, 3, 5, 7], 6)
+    assert list(hist) == [0, 3, 1, 2, 0, 1]
+    assert mb == 4
+    # ties: the first minimum wins (std::min_element)
+    hist, mb = pyoracle.pakman_histogram_cutoff([1, 2, 3, 3], 4)
+    assert list(hist) == [0, 1, 1, 2] and mb == 1
+    assert pyoracle.pakman_histogram_cutoff([5, 6], 1)[1] == 0
+
+
+def test_fq2txt_known_answer():
+    fq = b"@r1\nACGT\n+\nIIII\n@r2\nAC GTA\n+\nIIIII\n@r3\nA\n+\nI"
+    txt, w = pyoracle.fq2txt(fq)
+    assert w == 6
+    assert txt == b"ACGTMM\nACMGTA\nAMMMMM\n"
+
+
+def test_pakman_kmers_known_answer():
+    # A=0 C=1 T=2 G=3 via (byte >> 1) & 7; k = 3
+    fa = b"junk\n>h1\nACGTA\n>h2\nGG\n>h3\nTTT"
+    got = pyoracle.pakman_kmers(fa, 3)
+    enc = lambda s: sum(((b >> 1) & 7) << (2 * (len(s) - 1 - i)) for i, b in enumerate(s))
+    assert got.tolist() == [enc(b"ACG"), enc(b"CGT"), enc(b"GTA"), enc(b"TTT")]
+    # 'N' (0x4E -> 7) is OR'ed into the window as PakMan* does, not skipped
+    got = pyoracle.pakman_kmers(b">h\nANC\n", 2)
+    assert got.tolist() == [((0 << 2) | 7) & 15, ((7 << 2) | 1) & 15]
+    assert pyoracle.format_lines(fa, "fasta") == [b"ACGTA", b"GG", b"TTT"]
+    assert pyoracle.format_lines(b"x\n>a\nC\n", "fasta") == [b"C"]
