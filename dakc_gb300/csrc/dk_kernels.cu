@@ -79,45 +79,47 @@ struct TextTiles {
   const uint8_t* text;
   uint64_t nbytes, stride, lo, hi;
   uint32_t lt;  // lines per tile
-  uint8_t* buf[2];
+  uint8_t* buf0;  // tile buffers (even / odd tiles); two members, not an array,
+  uint8_t* buf1;  // so that the struct stays in registers
+  __device__ __forceinline__ uint8_t* bufof(uint32_t t) const { return (t & 1) ? buf1 : buf0; }
   uint64_t* bar;  // 2 mbarriers
 
-  __device__ uint32_t ntiles() const { return (uint32_t)((hi - lo + lt - 1) / lt); }
-  __device__ void range(uint32_t t, uint64_t* l0, uint64_t* l1) const {
+  __device__ __forceinline__ uint32_t ntiles() const { return (uint32_t)((hi - lo + lt - 1) / lt); }
+  __device__ __forceinline__ void range(uint32_t t, uint64_t* l0, uint64_t* l1) const {
     *l0 = lo + (uint64_t)t * lt;
     *l1 = min(hi, *l0 + lt);
   }
-  __device__ StagedCopy plan(uint32_t t) const {
+  __device__ __forceinline__ StagedCopy plan(uint32_t t) const {
     uint64_t l0, l1;
     range(t, &l0, &l1);
     const uint64_t b0 = l0 * stride, b1 = min(l1 * stride, nbytes);
     return plan_stage(text + b0, b1 - b0, text + nbytes);
   }
   // one thread: start the copy of tile t into buffer t&1
-  __device__ void issue(uint32_t t) const {
+  __device__ __forceinline__ void issue(uint32_t t) const {
     uint64_t l0, l1;
     range(t, &l0, &l1);
     const StagedCopy c = plan(t);
     uint64_t* b = &bar[t & 1];
     fence_barrier_init();  // order earlier generic writes of the buffer before the async copy
     mbar_arrive_expect_tx(b, c.bulk);
-    if (c.bulk) tma_load_1d(buf[t & 1], text + l0 * stride - c.lead, c.bulk, b);
+    if (c.bulk) tma_load_1d(bufof(t), text + l0 * stride - c.lead, c.bulk, b);
   }
   // whole block: wait for tile t, fetch its unaligned tail, return its first
   // line in shared memory (nullptr, with *err set, when the copy timed out)
-  __device__ const uint8_t* acquire(uint32_t t, unsigned long long* err) const {
+  __device__ __forceinline__ const uint8_t* acquire(uint32_t t, unsigned long long* err) const {
     const StagedCopy c = plan(t);
     const bool ok = mbar_wait_bounded(&bar[t & 1], (t >> 1) & 1);
     for (uint32_t i = threadIdx.x; i < c.tail_len; i += blockDim.x)
-      buf[t & 1][c.tail_dst + i] = c.tail_src[i];
+      bufof(t)[c.tail_dst + i] = c.tail_src[i];
     if (__syncthreads_or(!ok)) {
       if (threadIdx.x == 0) atomicMax(err, 1ull);
       return nullptr;
     }
-    return buf[t & 1] + c.lead;
+    return bufof(t) + c.lead;
   }
   // after a timeout: bounded wait for a copy still in flight into our smem
-  __device__ void drain(uint32_t t_next) const {
+  __device__ __forceinline__ void drain(uint32_t t_next) const {
     if (threadIdx.x == 0 && t_next < ntiles()) mbar_wait_bounded(&bar[t_next & 1], (t_next >> 1) & 1);
     __syncthreads();
   }
@@ -184,8 +186,8 @@ __global__ void __launch_bounds__(512) k_l1_count(ExtractArgs a, uint32_t* __res
   T.stride = stride;
   lines_of_block(a.n_lines, &T.lo, &T.hi);
   T.lt = lt;
-  T.buf[0] = tb;
-  T.buf[1] = tb + bb;
+  T.buf0 = tb;
+  T.buf1 = tb + bb;
   T.bar = bar;
   if (threadIdx.x == 0) {
     mbar_init(&bar[0], 1);
@@ -305,10 +307,10 @@ struct LineRoll {
   uint32_t prev;
   bool stopped;
   __device__ __forceinline__ void reset() { key = 0; run = 0; prev = 0; stopped = false; }
-  __device__ __forceinline__ bool step(uint32_t c, int p, int W, int k, uint64_t kmask,
-                                       bool pak = false) {
+  template <bool PAK = false>
+  __device__ __forceinline__ bool step(uint32_t c, int p, int W, int k, uint64_t kmask) {
     if (stopped || c == 0xF0u) { stopped = true; return false; }
-    if (pak) {
+    if (PAK) {
       key = ((key << 2) | c) & kmask;
       ++run;
       return run >= k;
@@ -355,8 +357,8 @@ __device__ __forceinline__ void setup_tiles(TextTiles* T, const ExtractArgs& a, 
   lines_of_block(a.n_lines, &T->lo, &T->hi);
   T->lt = blockDim.x;
   T->bar = reinterpret_cast<uint64_t*>(smraw);
-  T->buf[0] = smraw + 128;
-  T->buf[1] = smraw + 128 + bb;
+  T->buf0 = smraw + 128;
+  T->buf1 = smraw + 128 + bb;
   if (threadIdx.x == 0) {
     mbar_init(&T->bar[0], 1);
     mbar_init(&T->bar[1], 1);
@@ -365,6 +367,7 @@ __device__ __forceinline__ void setup_tiles(TextTiles* T, const ExtractArgs& a, 
 }
 
 // COUNT: per-CTA bucket histogram H[cta][bucket] and the k-mer total.
+template <bool PAK>
 __global__ void __launch_bounds__(kLineThreads) k_l1_lines_count(ExtractArgs a,
                                                                  uint32_t* __restrict__ H,
                                                                  unsigned long long* __restrict__ counters) {
@@ -405,7 +408,7 @@ __global__ void __launch_bounds__(kLineThreads) k_l1_lines_count(ExtractArgs a,
         for (int u = 0; u < 4; ++u) c4[u] = p0 + u < W ? lut[line[p0 + u]] : 0xF0u;
 #pragma unroll
         for (int u = 0; u < 4; ++u)
-          if (r.step(c4[u], p0 + u, W, k, a.kmask, a.conv == 1)) {
+          if (r.template step<PAK>(c4[u], p0 + u, W, k, a.kmask)) {
             atomicAdd(&cnt[a.njobs ? jb(r.key) : (uint32_t)(r.key >> a.shift1)], 1u);
             ++mine;
           }
@@ -429,6 +432,7 @@ __global__ void __launch_bounds__(kLineThreads) k_l1_lines_count(ExtractArgs a,
 // keys then leave as one contiguous run at this CTA's cursor of the bucket.
 // One text buffer (the next tile is fetched after the current one is done)
 // keeps shared memory at two CTAs per SM.
+template <bool PAK>
 __global__ void __launch_bounds__(kLineThreads, 2) k_l1_lines_chunked(ExtractArgs a,
                                                                      const uint64_t* __restrict__ O,
                                                                      uint64_t* __restrict__ keys_out,
@@ -445,7 +449,7 @@ __global__ void __launch_bounds__(kLineThreads, 2) k_l1_lines_chunked(ExtractArg
   uint8_t* lut = reinterpret_cast<uint8_t*>(tmp + 32);                                    // 256
   TextTiles T;
   setup_tiles(&T, a, smraw, bb);
-  T.buf[1] = T.buf[0];  // one buffer: tile t+1 is fetched once tile t is done
+  T.buf1 = T.buf0;  // one buffer: tile t+1 is fetched once tile t is done
   for (int b = threadIdx.x; b < F1; b += blockDim.x) {
     cursor[b] = O[(size_t)blockIdx.x * F1 + b];
     ccount[b] = 0;
@@ -469,12 +473,12 @@ __global__ void __launch_bounds__(kLineThreads, 2) k_l1_lines_chunked(ExtractArg
     if (!live) r.stopped = true;
     // warm-up: positions before the first possible k-mer end emit nothing
     const int warm = min(k - 1, W);
-    for (int p = 0; p < warm; ++p) r.step(r.stopped ? 0xF0u : lut[line[p]], p, W, k, a.kmask, a.conv == 1);
+    for (int p = 0; p < warm; ++p) r.template step<PAK>(r.stopped ? 0xF0u : lut[line[p]], p, W, k, a.kmask);
     for (int p0 = warm; p0 < W; p0 += kLineChunk) {  // uniform over the block
       const int p1 = min(W, p0 + kLineChunk);
       const LineRoll r0 = r;
       for (int p = p0; p < p1 && !r.stopped; ++p)
-        if (r.step(lut[line[p]], p, W, k, a.kmask, a.conv == 1))
+        if (r.template step<PAK>(lut[line[p]], p, W, k, a.kmask))
           atomicAdd(&ccount[(uint32_t)(r.key >> a.shift1)], 1u);
       __syncthreads();
       for (int b = threadIdx.x; b < F1; b += blockDim.x) {
@@ -485,7 +489,7 @@ __global__ void __launch_bounds__(kLineThreads, 2) k_l1_lines_chunked(ExtractArg
       const uint32_t Tn = block_scan_array<uint32_t>(coff, F1, tmp);
       r = r0;
       for (int p = p0; p < p1 && !r.stopped; ++p)
-        if (r.step(lut[line[p]], p, W, k, a.kmask, a.conv == 1)) {
+        if (r.template step<PAK>(lut[line[p]], p, W, k, a.kmask)) {
           const uint32_t b = (uint32_t)(r.key >> a.shift1);
           const uint32_t pos = coff[b] + atomicAdd(&ccount[b], 1u);
           if (DK_OK_IDX(pos < (uint32_t)blockDim.x * kLineChunk, 41, pos)) stage[pos] = r.key;
@@ -517,6 +521,7 @@ __global__ void __launch_bounds__(kLineThreads, 2) k_l1_lines_chunked(ExtractArg
 // key per bucket and staging would not lengthen the runs; writing directly
 // keeps shared memory small (text tiles and cursors only).  Consecutive keys
 // of a bucket land next to each other, so L2 merges the 8-byte stores.
+template <bool PAK>
 __global__ void __launch_bounds__(kLineThreads) k_l1_lines_direct(ExtractArgs a,
                                                                   const uint64_t* __restrict__ O,
                                                                   uint64_t* __restrict__ keys_out,
@@ -561,7 +566,7 @@ __global__ void __launch_bounds__(kLineThreads) k_l1_lines_direct(ExtractArgs a,
         for (int u = 0; u < 4; ++u) c4[u] = p0 + u < W ? lut[line[p0 + u]] : 0xF0u;
 #pragma unroll
         for (int u = 0; u < 4; ++u)
-          if (r.step(c4[u], p0 + u, W, k, a.kmask, a.conv == 1)) {
+          if (r.template step<PAK>(c4[u], p0 + u, W, k, a.kmask)) {
             const uint32_t b = a.njobs ? jb(r.key) : (uint32_t)(r.key >> a.shift1);
             keys_out[cursor[b] + atomicAdd(&cnt[b], 1u)] = r.key;
           }
@@ -597,8 +602,8 @@ __global__ void __launch_bounds__(512, 2) k_l1_scatter(ExtractArgs a, const uint
   T.stride = stride;
   lines_of_block(a.n_lines, &T.lo, &T.hi);
   T.lt = lt;
-  T.buf[0] = tb;
-  T.buf[1] = tb + bb;
+  T.buf0 = tb;
+  T.buf1 = tb + bb;
   T.bar = bar;
   if (threadIdx.x == 0) {
     mbar_init(&bar[0], 1);
@@ -1739,8 +1744,9 @@ static bool chunked_scatter(const ExtractArgs& a) {
 int launch_l1_count(const ExtractArgs& a, int grid, uint32_t* H, unsigned long long* counters,
                     cudaStream_t s) {
   if (a.W <= kLineMaxW) {
-    allow_max_smem(k_l1_lines_count);
-    k_l1_lines_count<<<grid, kLineThreads, lines_smem(a, false), s>>>(a, H, counters);
+    auto* kern = a.conv == 1 ? k_l1_lines_count<true> : k_l1_lines_count<false>;
+    allow_max_smem(kern);
+    kern<<<grid, kLineThreads, lines_smem(a, false), s>>>(a, H, counters);
     return 1;
   }
   switch (choose_c(a.W)) {
@@ -1806,13 +1812,15 @@ static void scatter_launch(const ExtractArgs& a, int grid, const uint64_t* O, ui
 int launch_l1_scatter(const ExtractArgs& a, int grid, const uint64_t* O, uint64_t* keys,
                       unsigned long long* counters, cudaStream_t s) {
   if (chunked_scatter(a)) {
-    allow_max_smem(k_l1_lines_chunked);
-    k_l1_lines_chunked<<<grid, kLineThreads, chunked_smem(a), s>>>(a, O, keys, counters);
+    auto* kern = a.conv == 1 ? k_l1_lines_chunked<true> : k_l1_lines_chunked<false>;
+    allow_max_smem(kern);
+    kern<<<grid, kLineThreads, chunked_smem(a), s>>>(a, O, keys, counters);
     return 1;
   }
   if (direct_scatter(a.W, a.njobs != 0)) {
-    allow_max_smem(k_l1_lines_direct);
-    k_l1_lines_direct<<<grid, kLineThreads, lines_smem(a, true), s>>>(a, O, keys, counters);
+    auto* kern = a.conv == 1 ? k_l1_lines_direct<true> : k_l1_lines_direct<false>;
+    allow_max_smem(kern);
+    kern<<<grid, kLineThreads, lines_smem(a, true), s>>>(a, O, keys, counters);
     return 1;
   }
   switch (choose_c(a.W)) {

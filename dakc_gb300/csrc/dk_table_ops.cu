@@ -33,12 +33,15 @@ __global__ void __launch_bounds__(kOpsThreads) k_count_hist(const uint32_t* __re
   if (local)
     for (uint32_t j = threadIdx.x; j < nb; j += blockDim.x) sh[j] = 0;
   __syncthreads();
-  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-       i += (uint64_t)gridDim.x * blockDim.x) {
-    const uint32_t c = counts[i];
-    if (c < nb) {
-      if (local) atomicAdd(&sh[c], 1u);
-      else atomicAdd(&hist[c], 1ull);
+  // most k-mers share a few small counts: lanes with the same count add once
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  const uint64_t span = (n + stride - 1) / stride * stride;  // whole warps stay in the loop
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < span; i += stride) {
+    const uint32_t c = i < n ? counts[i] : 0xFFFFFFFFu;
+    const uint32_t peers = __match_any_sync(0xFFFFFFFFu, c);
+    if (c < nb && (int)(threadIdx.x & 31) == __ffs(peers) - 1) {
+      if (local) atomicAdd(&sh[c], (uint32_t)__popc(peers));
+      else atomicAdd(&hist[c], (unsigned long long)__popc(peers));
     }
   }
   __syncthreads();
@@ -57,10 +60,10 @@ __global__ void __launch_bounds__(kOpsThreads) k_filter_count(const uint32_t* __
                                                               uint64_t n, uint32_t min_count,
                                                               uint64_t* __restrict__ kept) {
   __shared__ uint64_t tmp[32];
-  const uint64_t c0 = blockIdx.x * kChunk + (uint64_t)threadIdx.x * kPer;
+  const uint64_t c0 = blockIdx.x * kChunk;
   uint64_t mine = 0;
   for (int u = 0; u < kPer; ++u) {
-    const uint64_t i = c0 + u;
+    const uint64_t i = c0 + (uint64_t)u * kOpsThreads + threadIdx.x;  // coalesced
     if (i < n && counts[i] >= min_count) ++mine;
   }
   uint64_t total;
@@ -80,27 +83,37 @@ __global__ void k_exclusive_scan_serial(uint64_t* v, uint64_t n, uint64_t* total
   *total = run;
 }
 
+// Rounds of 256 consecutive entries: a warp ballot orders the kept entries
+// of each 32, a scan over the eight warps orders the round.
 __global__ void __launch_bounds__(kOpsThreads) k_filter_write(const uint64_t* __restrict__ kmers,
                                                               const uint32_t* __restrict__ counts,
                                                               uint64_t n, uint32_t min_count,
                                                               const uint64_t* __restrict__ base,
                                                               uint64_t* __restrict__ out_k,
                                                               uint32_t* __restrict__ out_c) {
-  __shared__ uint64_t tmp[32];
-  const uint64_t c0 = blockIdx.x * kChunk + (uint64_t)threadIdx.x * kPer;
-  uint64_t mine = 0;
+  __shared__ uint32_t wsum[kOpsThreads / 32];
+  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const uint64_t c0 = blockIdx.x * kChunk;
+  uint64_t pos = base[blockIdx.x];
   for (int u = 0; u < kPer; ++u) {
-    const uint64_t i = c0 + u;
-    if (i < n && counts[i] >= min_count) ++mine;
-  }
-  uint64_t pos = base[blockIdx.x] + block_excl_scan<uint64_t>(mine, tmp, nullptr);
-  for (int u = 0; u < kPer; ++u) {
-    const uint64_t i = c0 + u;
-    if (i < n && counts[i] >= min_count) {
-      out_k[pos] = kmers[i];
-      out_c[pos] = counts[i];
-      ++pos;
+    const uint64_t i = c0 + (uint64_t)u * kOpsThreads + threadIdx.x;
+    const bool keep = i < n && counts[i] >= min_count;
+    const uint32_t bal = __ballot_sync(0xFFFFFFFFu, keep);
+    if (lane == 0) wsum[warp] = __popc(bal);
+    __syncthreads();
+    uint32_t before = 0, round = 0;
+#pragma unroll
+    for (int w = 0; w < kOpsThreads / 32; ++w) {
+      before += (w < (int)warp) ? wsum[w] : 0u;
+      round += wsum[w];
     }
+    if (keep) {
+      const uint64_t o = pos + before + __popc(bal & ((1u << lane) - 1u));
+      out_k[o] = kmers[i];
+      out_c[o] = counts[i];
+    }
+    pos += round;
+    __syncthreads();
   }
 }
 
