@@ -98,7 +98,8 @@ class Stats(ctypes.Structure):
                 ("partition_levels", ctypes.c_int), ("n_bins", ctypes.c_uint64),
                 ("ms_kernel", ctypes.c_double * 8), ("launches_kernel", ctypes.c_uint64 * 8),
                 ("n_partitioned", ctypes.c_uint64), ("n_waves", ctypes.c_uint64),
-                ("n_bins_resorted", ctypes.c_uint64)]
+                ("n_bins_resorted", ctypes.c_uint64), ("n_bins_big", ctypes.c_uint64),
+                ("n_bins_retried", ctypes.c_uint64)]
 
     KERNEL_NAMES = ["extract_count", "extract_scatter", "partition_hist", "partition_scatter",
                     "bin_count", "compact", "hash_insert", "other"]

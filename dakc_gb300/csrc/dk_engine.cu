@@ -766,8 +766,9 @@ int Engine::count_device(const uint8_t* d_text, uint64_t nbytes, const dk_input_
   DK_TRY(Arena::ensure(this, O, (size_t)G * F1 * 8));
   DK_TRY(Arena::ensure(this, ctrs, 256));
   // device counters: [0] k-mers, [1] NUL-led line marker, [2] distinct total,
-  // [3] device error (a bounded wait ran out), [4] bin ticket, [5] count overflow;
-  // LevelCounters at byte 64
+  // [3] device error (a bounded wait ran out), [4] bin ticket, [5] count overflow,
+  // [6] hash bins sorted instead, [7] big bins to re-partition; LevelCounters at
+  // byte 64; [16] proxy counter, [17] big bins counted
   unsigned long long* c64 = (unsigned long long*)ctrs.p;
   LevelCounters* lc = (LevelCounters*)((char*)ctrs.p + 64);
 
@@ -811,11 +812,27 @@ int Engine::count_device(const uint8_t* d_text, uint64_t nbytes, const dk_input_
   TIMED(1, launch_l1_scatter(a, G, (const uint64_t*)O.p, (uint64_t*)keysA.p, c64, stream));
   DK_CUDA(cudaEventRecord(ev_stage[2], stream));
 
-  // partition levels
+  // partition levels, then the bin count of the final nodes.  With the hash
+  // variant a skewed node (most of its parent's keys: a hot k-mer) larger
+  // than a bin is counted whole by one hash bin; one that turns out to hold
+  // too many distinct keys is re-partitioned through a proxy child and the
+  // levels resume from the proxies (a pass per round of such bins).
   std::vector<std::pair<uint32_t, uint32_t>> levels;  // node ranges per level
   uint32_t lo = 0, hi = (uint32_t)F1;
   DK_TRY(Arena::ensure(this, finals, (size_t)hi * 4));
-  for (int lvl = 0; lvl < 16; ++lvl) {
+  const int big_ok = use_hash ? 1 : 0;
+  uint32_t fin_lo = 0;  // first final node of this pass
+  uint32_t n_final = 0;
+  stats.partition_levels = 0;
+  // Every split fixes at least one more key bit and nodes with at most
+  // kDenseBits free bits are final, so the levels end within 2k - kDenseBits
+  // splits (a proxy level fixes no bit, but follows a split of its own); the
+  // loop runs until a level splits nothing.
+  for (int lvl = 0;; ++lvl) {
+    if (lvl > 4 * k + 2) {
+      set_error("internal: the partition did not converge");
+      return DK_ERR_INVALID_ARG;
+    }
     levels.emplace_back(lo, hi);
     // the final list can grow by at most this level's node count
     LevelCounters lv;
@@ -836,13 +853,42 @@ int Engine::count_device(const uint8_t* d_text, uint64_t nbytes, const dk_input_
     }
     DK_CUDA(cudaMemsetAsync((char*)lc + 4, 0, sizeof(LevelCounters) - 4, stream));  // keep n_final
     TIMED(7, launch_classify((Node*)nodes.p, lo, hi, (uint32_t*)finals.p, lc, kBinCap,
-                             2 * bin_target, stream));
+                             2 * bin_target, big_ok, stream));
     DK_TRY(sync_read(lc, sizeof(LevelCounters), &lv));
     if (lv.too_big) {
       set_error("a partition node holds >= 2^32 keys");
       return DK_ERR_INVALID_ARG;
     }
-    if (lv.n_split == 0) break;
+    if (lv.n_split == 0) {
+      // this pass's levels are done: count its final nodes
+      if (fin_lo == 0) DK_CUDA(cudaEventRecord(ev_stage[3], stream));
+      n_final = lv.n_final;
+      DK_CUDA(cudaMemsetAsync(c64 + 4, 0, 8, stream));  // bin ticket
+      TIMED(4, launch_bin_count((Node*)nodes.p, (uint32_t*)finals.p + fin_lo, n_final - fin_lo,
+                                (uint64_t*)keysA.p, (uint64_t*)keysB.p, (uint32_t*)cnt.p,
+                                use_hash ? 1 : 0, c64, sm_count, stream));
+      if (!big_ok) break;
+      uint64_t retry = 0;
+      DK_TRY(sync_read(c64 + 7, 8, &retry));
+      if (retry == 0) break;
+      stats.n_bins_retried += retry;
+      const size_t need_nodes = (size_t)hi + (size_t)retry;
+      if (nodes.cap < need_nodes * sizeof(Node)) {
+        DevBuf nb;
+        DK_TRY(Arena::ensure(this, nb, need_nodes * sizeof(Node)));
+        DK_CUDA(cudaMemcpyAsync(nb.p, nodes.p, (size_t)hi * sizeof(Node), cudaMemcpyDeviceToDevice, stream));
+        Arena::release(this, nodes);
+        nodes = nb;
+      }
+      DK_CUDA(cudaMemsetAsync(c64 + 7, 0, 8, stream));
+      DK_CUDA(cudaMemsetAsync(c64 + 16, 0, 8, stream));  // proxy counter
+      TIMED(7, launch_make_proxies((Node*)nodes.p, (uint32_t*)finals.p + fin_lo, n_final - fin_lo,
+                                   hi, (unsigned int*)(c64 + 16), stream));
+      fin_lo = n_final;
+      lo = hi;
+      hi = hi + (uint32_t)retry;
+      continue;
+    }
     stats.n_partitioned += lv.split_keys;
     // grow node storage for the children (copying existing nodes)
     const size_t need_nodes = (size_t)hi + (size_t)lv.n_children;
@@ -866,24 +912,19 @@ int Engine::count_device(const uint8_t* d_text, uint64_t nbytes, const dk_input_
     hi = hi + lv.n_children;
   }
   stats.partition_levels = (int)levels.size();
-  DK_CUDA(cudaEventRecord(ev_stage[3], stream));
-  LevelCounters lvf;
-  DK_TRY(sync_read(lc, sizeof(LevelCounters), &lvf));
-  const uint32_t n_final = lvf.n_final;
-  stats.n_bins = n_final;
-  TIMED(4, launch_bin_count((Node*)nodes.p, (uint32_t*)finals.p, n_final, (uint64_t*)keysA.p,
-                            (uint64_t*)keysB.p, (uint32_t*)cnt.p, use_hash ? 1 : 0, c64, sm_count,
-                            stream));
+  stats.n_bins = n_final - (uint32_t)stats.n_bins_retried;
   DK_CUDA(cudaEventRecord(ev_stage[4], stream));
-  // distinct counts up the tree, offsets down
+  // distinct counts up the tree, offsets down (the last level splits nothing;
+  // a proxy level comes after the level of the node it stands in for)
   for (int l = (int)levels.size() - 2; l >= 0; --l)
     TIMED(7, launch_aggregate((Node*)nodes.p, levels[l].first, levels[l].second, stream));
   TIMED(7, launch_l1_offsets((Node*)nodes.p, (uint32_t)F1, c64 + 2, stream));
   for (size_t l = 0; l + 1 < levels.size(); ++l)
     TIMED(7, launch_child_offsets((Node*)nodes.p, levels[l].first, levels[l].second, stream));
-  uint64_t tail[5];
-  DK_TRY(sync_read(c64 + 2, 40, tail));
+  uint64_t tail[16];
+  DK_TRY(sync_read(c64 + 2, 128, tail));
   stats.n_bins_resorted = tail[4];
+  stats.n_bins_big = tail[15];
   const uint64_t n_distinct = tail[0];
   if (tail[1]) {
     set_error("a bounded device wait (TMA copy) timed out");

@@ -28,7 +28,9 @@ struct Node {
   uint8_t pad[6];
 };
 static_assert(sizeof(Node) == 64, "Node layout");
-enum : uint8_t { NODE_FINAL = 1, NODE_SPLIT = 2, NODE_EMPTY = 3 };
+// NODE_RETRY: a large skewed node counted as one hash bin (k_bin_count) that
+// held too many distinct keys; the host re-partitions it through a proxy child
+enum : uint8_t { NODE_FINAL = 1, NODE_SPLIT = 2, NODE_EMPTY = 3, NODE_RETRY = 4 };
 
 struct Tile {  // a slice of a split node's keys, partitioned by one CTA
   uint64_t start;
@@ -114,8 +116,14 @@ int l1_max_buckets(int W, bool jobs);
 int launch_l1_scatter(const ExtractArgs& a, int grid, const uint64_t* O, uint64_t* keys,
                       unsigned long long* counters, cudaStream_t s);
 // split nodes get a digit width that makes their children ~split_target/2 keys
+// big_ok: a skewed node (it kept most of its parent's keys: a hot k-mer) larger
+// than a bin becomes a final hash bin instead of splitting again
 int launch_classify(Node* nodes, uint32_t node_lo, uint32_t node_hi, uint32_t* final_list,
-                    LevelCounters* ctr, int bin_cap, int split_target, cudaStream_t s);
+                    LevelCounters* ctr, int bin_cap, int split_target, int big_ok, cudaStream_t s);
+// for each NODE_RETRY node of the final list: a proxy copy at n_nodes + i (i
+// from *count), the node itself becomes a split node of width 0 over its proxy
+int launch_make_proxies(Node* nodes, const uint32_t* final_list, uint32_t n_final,
+                        uint32_t n_nodes, unsigned int* count, cudaStream_t s);
 int launch_assign(Node* nodes, uint32_t node_lo, uint32_t node_hi, uint32_t child_base,
                   Tile* tiles, LevelCounters* ctr, cudaStream_t s);
 int launch_tile_hist(const Node* nodes, const Tile* tiles, uint32_t n_tiles,
@@ -125,7 +133,9 @@ int launch_node_scan(Node* nodes, uint32_t node_lo, uint32_t node_hi, Tile* tile
 int launch_tile_scatter(const Node* nodes, const Tile* tiles, uint32_t n_tiles, uint64_t* A,
                         uint64_t* B, const uint32_t* TH, int max_width, cudaStream_t s);
 // ctr: [4] (low 32 bits) = bin ticket, [5] = count overflow flag, [6] = hash bins that fell
-// back to sorting (all zeroed by the caller); use_hash selects the hash-first bin count
+// back to sorting, [7] = big skewed bins that must be re-partitioned (NODE_RETRY),
+// [17] = big skewed bins counted (all zeroed by the caller); use_hash selects
+// the hash-first bin count
 int launch_bin_count(Node* nodes, const uint32_t* final_list, uint32_t n_final, uint64_t* A,
                      uint64_t* B, uint32_t* C, int use_hash, unsigned long long* ctr, int sm_count,
                      cudaStream_t s);

@@ -740,7 +740,7 @@ __device__ __forceinline__ uint32_t rank_in_digit(uint32_t* ctr, uint32_t v, boo
 // Mark each node of the level final / split / empty; count what the split
 // nodes need (children, tiles, histogram entries).
 __global__ void k_classify(Node* nodes, uint32_t lo, uint32_t hi, uint32_t* final_list,
-                           LevelCounters* ctr, int bin_cap, int split_target) {
+                           LevelCounters* ctr, int bin_cap, int split_target, int big_ok) {
   const uint32_t i = lo + blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= hi) return;
   const Node nd = nodes[i];
@@ -749,7 +749,11 @@ __global__ void k_classify(Node* nodes, uint32_t lo, uint32_t hi, uint32_t* fina
     nodes[i].d = 0;
     return;
   }
-  if (nd.n <= (uint64_t)bin_cap || nd.shift <= kDenseBits) {
+  // a skewed node holds a hot k-mer: splitting peels off few keys per level,
+  // while one hash bin streams any number of copies (it is re-partitioned if
+  // it holds too many distinct keys)
+  if (nd.n <= (uint64_t)bin_cap || nd.shift <= kDenseBits ||
+      (big_ok && nd.skewed && nd.n < (1ull << 31))) {
     nodes[i].state = NODE_FINAL;
     final_list[atomicAdd(&ctr->n_final, 1u)] = i;
     return;
@@ -1443,6 +1447,9 @@ __device__ bool bin_hashed(Node* nodes, uint32_t ni, const Node& nd, uint64_t* k
   __syncthreads();
   constexpr int kBatch = 8;  // keys in flight per thread
   for (uint32_t i0 = 0; i0 < n; i0 += kBatch * T) {
+    // a failed table stops the pass early (a large bin would otherwise probe
+    // the full table for every remaining key); warp-uniform exit
+    if (__any_sync(0xFFFFFFFFu, *reinterpret_cast<volatile uint32_t*>(&flags[1]) != 0)) break;
     unsigned long long kk[kBatch];
 #pragma unroll
     for (int u = 0; u < kBatch; ++u) {
@@ -1585,6 +1592,17 @@ __global__ void __launch_bounds__(kBinThreads, kBinBlocksPerSM) k_bin_count(Node
     if (nd.shift <= kDenseBits) {
       bin_dense(nodes, ni, nd, keys, cnt, skeys, reinterpret_cast<unsigned long long*>(tmp),
                 &ctr[5]);
+    } else if (nd.n > (uint64_t)kBinCap) {
+      // a large skewed bin: the hash bin streams its keys; with too many
+      // distinct keys it is left, unwritten, for the host to re-partition
+      const bool done = bin_hashed(nodes, ni, nd, keys, cnt, skeys, hist, tmp, mark, hflags, hot);
+      if (threadIdx.x == 0) {
+        atomicAdd(&ctr[17], 1ull);
+        if (!done) {
+          nodes[ni].state = NODE_RETRY;
+          atomicAdd(&ctr[7], 1ull);
+        }
+      }
     } else {
       bool done = false;
       if (use_hash) {
@@ -1642,6 +1660,33 @@ __global__ void __launch_bounds__(256) k_child_offsets(Node* nodes, uint32_t lo)
   }
 }
 
+// Re-partition NODE_RETRY nodes: each gets a proxy copy appended after the
+// existing nodes (which then splits like any other node) and becomes a split
+// node of width 0 whose one child is that proxy, so the tree passes sum and
+// place its keys through the proxy.
+__global__ void k_make_proxies(Node* nodes, const uint32_t* __restrict__ finals, uint32_t n_final,
+                               uint32_t n_nodes, unsigned int* count) {
+  const uint32_t f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= n_final) return;
+  const uint32_t i = finals[f];
+  if (nodes[i].state != NODE_RETRY) return;
+  const uint32_t j = n_nodes + atomicAdd(count, 1u);
+  Node px = nodes[i];
+  px.d = 0;
+  px.out_off = 0;
+  px.first_child = 0;
+  px.state = 0;
+  px.tile_base = 0;
+  px.ntiles = 0;
+  px.th_base = 0;
+  px.width = 0;
+  px.skewed = 0;  // split normally from here
+  nodes[j] = px;
+  nodes[i].state = NODE_SPLIT;
+  nodes[i].width = 0;
+  nodes[i].first_child = j;
+}
+
 // one warp per final node: staged pairs -> output table
 __global__ void k_compact(const Node* nodes, const uint32_t* __restrict__ finals, uint32_t n_final,
                           const uint64_t* A, const uint64_t* B, const uint32_t* C,
@@ -1649,6 +1694,7 @@ __global__ void k_compact(const Node* nodes, const uint32_t* __restrict__ finals
   const uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (w >= n_final) return;
   const Node nd = nodes[finals[w]];
+  if (nd.state != NODE_FINAL) return;  // re-partitioned after its bin count failed
   const uint64_t* sk = (nd.buf ? B : A) + nd.start;
   const uint32_t* sc = C + nd.start;
   for (uint64_t i = lane_id(); i < nd.d; i += 32) {
@@ -1836,11 +1882,18 @@ int launch_l1_scatter(const ExtractArgs& a, int grid, const uint64_t* O, uint64_
 }
 
 int launch_classify(Node* nodes, uint32_t lo, uint32_t hi, uint32_t* final_list,
-                    LevelCounters* ctr, int bin_cap, int split_target, cudaStream_t s) {
+                    LevelCounters* ctr, int bin_cap, int split_target, int big_ok, cudaStream_t s) {
   const uint32_t n = hi - lo;
   if (!n) return 0;
   k_classify<<<(n + 255) / 256, 256, 0, s>>>(nodes, lo, hi, final_list, ctr, bin_cap,
-                                            split_target);
+                                            split_target, big_ok);
+  return 1;
+}
+
+int launch_make_proxies(Node* nodes, const uint32_t* final_list, uint32_t n_final,
+                        uint32_t n_nodes, unsigned int* count, cudaStream_t s) {
+  if (!n_final) return 0;
+  k_make_proxies<<<(n_final + 255) / 256, 256, 0, s>>>(nodes, final_list, n_final, n_nodes, count);
   return 1;
 }
 

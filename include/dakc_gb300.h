@@ -130,6 +130,10 @@ typedef struct {
   uint64_t n_waves;        /* dk_count_batch: memory-bounded waves run         */
   uint64_t n_bins_resorted; /* hash variant: bins the hash pass handed to sorting
                                (too many distinct keys or a long probe run)      */
+  uint64_t n_bins_big;      /* hash variant: nodes larger than a bin that hold one
+                               hot k-mer, counted whole by one hash bin          */
+  uint64_t n_bins_retried;  /* of those, bins with too many distinct keys, which
+                               were partitioned further                          */
 } dk_stats;
 
 /* One read set of a batch (dk_count_batch). */

@@ -188,3 +188,57 @@ def test_invalid_arguments(engine):
         with pytest.raises(dk.DkError) as e:
             engine.count(b"A" * n, W, k)
         assert e.value.status == dk.DK_ERR_INVALID_ARG
+
+
+@pytest.mark.parametrize("variant", VARIANTS)
+def test_hot_kmer_needs_many_partition_levels(engine, variant):
+    """One 31-mer 20,000 times (just above a bin's capacity) among random
+    reads: its node splits by only a couple of bits per level, so the
+    partition runs many levels (more than 16) before it is counted densely."""
+    rng = np.random.Generator(np.random.PCG64(77))
+    hot = rng.choice(np.frombuffer(b"ACGT", np.uint8), 31)
+    W = 31
+    lines = np.empty((20_000 + 30_000, W + 1), np.uint8)
+    lines[:20_000, :W] = hot
+    lines[20_000:, :W] = rng.choice(np.frombuffer(b"ACGT", np.uint8), (30_000, W))
+    lines[:, W] = ord("\n")
+    rng.shuffle(lines[:-1])
+    text = lines.reshape(-1)
+    keys, counts, nk = pyoracle.count(text, W, 31)
+    r = engine.count(text, W, 31, variant)
+    st = engine.stats()
+    assert r.n_kmers == nk and np.array_equal(r.kmers, keys) and np.array_equal(r.counts, counts)
+    assert int(counts.max()) >= 20_000
+    if variant == dk.VARIANT_HASH:
+        # the hot node is counted whole by one hash bin, a level or two down
+        assert st["n_bins_big"] >= 1 and st["n_bins_retried"] == 0
+        assert st["partition_levels"] <= 4
+    else:
+        assert st["partition_levels"] > 16
+
+
+@pytest.mark.parametrize("variant", VARIANTS)
+def test_skewed_node_with_many_distinct_kmers_is_repartitioned(engine, variant):
+    """60,000 distinct 31-mers behind one 20-base prefix, a hot 31-mer with the
+    same prefix and random reads: the prefix's node keeps most of its
+    parent's keys at every level, so the hash variant tries it as one big bin,
+    finds too many distinct keys and partitions it further, round after round
+    until the prefix is spent."""
+    rng = np.random.Generator(np.random.PCG64(78))
+    acgt = np.frombuffer(b"ACGT", np.uint8)
+    W = 31
+    prefix = rng.choice(acgt, 20)
+    lines = np.empty((60_000 + 5_000 + 30_000, W + 1), np.uint8)
+    lines[:65_000, :20] = prefix
+    lines[:60_000, 20:W] = rng.choice(acgt, (60_000, W - 20))
+    lines[60_000:65_000, 20:W] = rng.choice(acgt, W - 20)
+    lines[65_000:, :W] = rng.choice(acgt, (30_000, W))
+    lines[:, W] = ord("\n")
+    rng.shuffle(lines)
+    text = lines.reshape(-1)
+    keys, counts, nk = pyoracle.count(text, W, 31)
+    r = engine.count(text, W, 31, variant)
+    st = engine.stats()
+    assert r.n_kmers == nk and np.array_equal(r.kmers, keys) and np.array_equal(r.counts, counts)
+    if variant == dk.VARIANT_HASH:
+        assert st["n_bins_retried"] >= 2
