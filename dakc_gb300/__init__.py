@@ -38,6 +38,8 @@ DK_ERR_NO_DEVICE = -10
 
 VARIANT_AUTO, VARIANT_SORT, VARIANT_HASH = 0, 1, 2
 CONV_DAKC, CONV_PAKMAN = 0, 1
+FLAG_STREAM_ALL = 1  # dk_config.flags: copy every host table out group by group
+
 FORMAT_LINES, FORMAT_FASTQ, FORMAT_FASTA = 0, 1, 2
 RESIDENT_HOST, RESIDENT_DEVICE = 0, 1
 
@@ -99,7 +101,8 @@ class Stats(ctypes.Structure):
                 ("ms_kernel", ctypes.c_double * 8), ("launches_kernel", ctypes.c_uint64 * 8),
                 ("n_partitioned", ctypes.c_uint64), ("n_waves", ctypes.c_uint64),
                 ("n_bins_resorted", ctypes.c_uint64), ("n_bins_big", ctypes.c_uint64),
-                ("n_bins_retried", ctypes.c_uint64)]
+                ("n_bins_retried", ctypes.c_uint64), ("n_groups", ctypes.c_uint64),
+                ("table_streamed", ctypes.c_uint64)]
 
     KERNEL_NAMES = ["extract_count", "extract_scatter", "partition_hist", "partition_scatter",
                     "bin_count", "compact", "hash_insert", "other"]
@@ -216,9 +219,9 @@ class PinnedBuffer:
 class Engine:
     """One engine context: a CUDA stream, its device arenas and table pool."""
 
-    def __init__(self, device: int = 0, mem_budget: int = 0):
+    def __init__(self, device: int = 0, mem_budget: int = 0, flags: int = 0):
         self.lib = load_library()
-        cfg = Config(device, 0, mem_budget, 0)
+        cfg = Config(device, 0, mem_budget, flags)
         h = ctypes.c_void_p()
         rc = self.lib.dk_create(ctypes.byref(cfg), ctypes.byref(h))
         if rc != DK_OK:

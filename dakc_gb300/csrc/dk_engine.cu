@@ -25,6 +25,11 @@
 
 namespace dk {
 
+// host tables of at least this many k-mers (bound) move out while the count
+// runs, in this many groups of level-1 buckets
+constexpr uint64_t kStreamMinKmers = 64ull << 20;
+constexpr int kStreamGroups = 8;
+
 // --------------------------------------------------------------- helpers
 static int ceil_log2(uint64_t x) {
   int b = 0;
@@ -116,6 +121,7 @@ void Engine::kresolve() {
 int Engine::init(const dk_config* cfg) {
   Engine* e = this;
   device = cfg ? cfg->device : 0;
+  flags = cfg ? cfg->flags : 0;
   int n = 0;
   if (cudaGetDeviceCount(&n) != cudaSuccess || n <= device) {
     cudaGetLastError();
@@ -812,115 +818,163 @@ int Engine::count_device(const uint8_t* d_text, uint64_t nbytes, const dk_input_
   TIMED(1, launch_l1_scatter(a, G, (const uint64_t*)O.p, (uint64_t*)keysA.p, c64, stream));
   DK_CUDA(cudaEventRecord(ev_stage[2], stream));
 
-  // partition levels, then the bin count of the final nodes.  With the hash
+  if (!out_k || !out_c) {
+    set_error("internal: no output buffers");
+    return DK_ERR_INVALID_ARG;
+  }
+  // Groups of consecutive level-1 buckets, each taken through its partition
+  // levels, bin count, tree offsets and compact before the next: a group's
+  // slice of the table is then final and is handed to out_sink while the
+  // next group runs.  One group unless a sink is set.
+  std::vector<uint32_t> group_at{0, (uint32_t)F1};  // level-1 bucket boundaries
+  std::vector<uint64_t> group_keys{n_kmers};        // k-mers per group
+  if (out_sink && out_groups > 1 && F1 >= 2 * out_groups) {
+    std::vector<Node> l1n((size_t)F1);
+    DK_TRY(sync_read(nodes.p, (size_t)F1 * sizeof(Node), l1n.data()));
+    group_at.assign(1, 0);
+    group_keys.clear();
+    uint64_t run = 0, run_g = 0;
+    for (int b = 0; b < F1; ++b) {
+      run += l1n[b].n;
+      run_g += l1n[b].n;
+      const uint64_t g = group_at.size();
+      if (g < (uint64_t)out_groups && b + 1 < F1 && run * (uint64_t)out_groups >= g * n_kmers) {
+        group_at.push_back((uint32_t)(b + 1));
+        group_keys.push_back(run_g);
+        run_g = 0;
+      }
+    }
+    group_at.push_back((uint32_t)F1);
+    group_keys.push_back(run_g);
+  }
+
+  // Partition levels, then the bin count of the final nodes.  With the hash
   // variant a skewed node (most of its parent's keys: a hot k-mer) larger
   // than a bin is counted whole by one hash bin; one that turns out to hold
   // too many distinct keys is re-partitioned through a proxy child and the
   // levels resume from the proxies (a pass per round of such bins).
-  std::vector<std::pair<uint32_t, uint32_t>> levels;  // node ranges per level
-  uint32_t lo = 0, hi = (uint32_t)F1;
-  DK_TRY(Arena::ensure(this, finals, (size_t)hi * 4));
   const int big_ok = use_hash ? 1 : 0;
-  uint32_t fin_lo = 0;  // first final node of this pass
-  uint32_t n_final = 0;
-  stats.partition_levels = 0;
-  // Every split fixes at least one more key bit and nodes with at most
-  // kDenseBits free bits are final, so the levels end within 2k - kDenseBits
-  // splits (a proxy level fixes no bit, but follows a split of its own); the
-  // loop runs until a level splits nothing.
-  for (int lvl = 0;; ++lvl) {
-    if (lvl > 4 * k + 2) {
-      set_error("internal: the partition did not converge");
-      return DK_ERR_INVALID_ARG;
-    }
-    levels.emplace_back(lo, hi);
-    // the final list can grow by at most this level's node count
-    LevelCounters lv;
-    DK_TRY(sync_read(lc, sizeof(LevelCounters), &lv));
-    const uint32_t n_final_so_far = lv.n_final;
-    {
-      // finals must hold n_final_so_far + (hi - lo)
-      DevBuf& f = finals;
-      const size_t need = ((size_t)n_final_so_far + (hi - lo)) * 4;
-      if (f.cap < need) {
-        DevBuf nb;
-        DK_TRY(Arena::ensure(this, nb, need));
-        if (n_final_so_far)
-          DK_CUDA(cudaMemcpyAsync(nb.p, f.p, (size_t)n_final_so_far * 4, cudaMemcpyDeviceToDevice, stream));
-        Arena::release(this, f);
-        f = nb;
+  uint32_t node_end = (uint32_t)F1;  // nodes [0, node_end) exist
+  uint32_t n_final = 0;              // final nodes listed so far (all groups)
+  uint64_t keys_done = 0, distinct_done = 0;
+  DK_TRY(Arena::ensure(this, finals, (size_t)F1 * 4));
+  for (size_t grp = 0; grp + 1 < group_at.size(); ++grp) {
+    std::vector<std::pair<uint32_t, uint32_t>> levels;  // node ranges per level
+    uint32_t lo = group_at[grp], hi = group_at[grp + 1];
+    const uint32_t fin_g = n_final;  // first final node of the group
+    uint32_t fin_lo = n_final;       // first final node of this pass
+    // Every split fixes at least one more key bit and nodes with at most
+    // kDenseBits free bits are final, so the levels end within 2k - kDenseBits
+    // splits (a proxy level fixes no bit, but follows a split of its own); the
+    // loop runs until a level splits nothing.
+    for (int lvl = 0;; ++lvl) {
+      if (lvl > 4 * k + 2) {
+        set_error("internal: the partition did not converge");
+        return DK_ERR_INVALID_ARG;
       }
-    }
-    DK_CUDA(cudaMemsetAsync((char*)lc + 4, 0, sizeof(LevelCounters) - 4, stream));  // keep n_final
-    TIMED(7, launch_classify((Node*)nodes.p, lo, hi, (uint32_t*)finals.p, lc, kBinCap,
-                             2 * bin_target, big_ok, stream));
-    DK_TRY(sync_read(lc, sizeof(LevelCounters), &lv));
-    if (lv.too_big) {
-      set_error("a partition node holds >= 2^32 keys");
-      return DK_ERR_INVALID_ARG;
-    }
-    if (lv.n_split == 0) {
-      // this pass's levels are done: count its final nodes
-      if (fin_lo == 0) DK_CUDA(cudaEventRecord(ev_stage[3], stream));
+      levels.emplace_back(lo, hi);
+      {
+        // the final list can grow by at most this level's node count
+        DevBuf& f = finals;
+        const size_t need = ((size_t)n_final + (hi - lo)) * 4;
+        if (f.cap < need) {
+          DevBuf nb;
+          DK_TRY(Arena::ensure(this, nb, need));
+          if (n_final)
+            DK_CUDA(cudaMemcpyAsync(nb.p, f.p, (size_t)n_final * 4, cudaMemcpyDeviceToDevice, stream));
+          Arena::release(this, f);
+          f = nb;
+        }
+      }
+      LevelCounters lv;
+      DK_CUDA(cudaMemsetAsync((char*)lc + 4, 0, sizeof(LevelCounters) - 4, stream));  // keep n_final
+      TIMED(7, launch_classify((Node*)nodes.p, lo, hi, (uint32_t*)finals.p, lc, kBinCap,
+                               2 * bin_target, big_ok, stream));
+      DK_TRY(sync_read(lc, sizeof(LevelCounters), &lv));
+      if (lv.too_big) {
+        set_error("a partition node holds >= 2^32 keys");
+        return DK_ERR_INVALID_ARG;
+      }
       n_final = lv.n_final;
-      DK_CUDA(cudaMemsetAsync(c64 + 4, 0, 8, stream));  // bin ticket
-      TIMED(4, launch_bin_count((Node*)nodes.p, (uint32_t*)finals.p + fin_lo, n_final - fin_lo,
-                                (uint64_t*)keysA.p, (uint64_t*)keysB.p, (uint32_t*)cnt.p,
-                                use_hash ? 1 : 0, c64, sm_count, stream));
-      if (!big_ok) break;
-      uint64_t retry = 0;
-      DK_TRY(sync_read(c64 + 7, 8, &retry));
-      if (retry == 0) break;
-      stats.n_bins_retried += retry;
-      const size_t need_nodes = (size_t)hi + (size_t)retry;
+      if (lv.n_split == 0) {
+        // this pass's levels are done: count its final nodes
+        if (grp == 0 && fin_lo == fin_g) DK_CUDA(cudaEventRecord(ev_stage[3], stream));
+        DK_CUDA(cudaMemsetAsync(c64 + 4, 0, 8, stream));  // bin ticket
+        TIMED(4, launch_bin_count((Node*)nodes.p, (uint32_t*)finals.p + fin_lo, n_final - fin_lo,
+                                  (uint64_t*)keysA.p, (uint64_t*)keysB.p, (uint32_t*)cnt.p,
+                                  use_hash ? 1 : 0, c64, sm_count, stream));
+        DK_CUDA(cudaEventRecord(ev_stage[4], stream));
+        if (!big_ok) break;
+        uint64_t retry = 0;
+        DK_TRY(sync_read(c64 + 7, 8, &retry));
+        if (retry == 0) break;
+        stats.n_bins_retried += retry;
+        const size_t need_nodes = (size_t)node_end + (size_t)retry;
+        if (nodes.cap < need_nodes * sizeof(Node)) {
+          DevBuf nb;
+          DK_TRY(Arena::ensure(this, nb, need_nodes * sizeof(Node)));
+          DK_CUDA(cudaMemcpyAsync(nb.p, nodes.p, (size_t)node_end * sizeof(Node),
+                                  cudaMemcpyDeviceToDevice, stream));
+          Arena::release(this, nodes);
+          nodes = nb;
+        }
+        DK_CUDA(cudaMemsetAsync(c64 + 7, 0, 8, stream));
+        DK_CUDA(cudaMemsetAsync(c64 + 16, 0, 8, stream));  // proxy counter
+        TIMED(7, launch_make_proxies((Node*)nodes.p, (uint32_t*)finals.p + fin_lo, n_final - fin_lo,
+                                     node_end, (unsigned int*)(c64 + 16), stream));
+        fin_lo = n_final;
+        lo = node_end;
+        hi = node_end + (uint32_t)retry;
+        node_end = hi;
+        continue;
+      }
+      stats.n_partitioned += lv.split_keys;
+      // grow node storage for the children (copying existing nodes)
+      const size_t need_nodes = (size_t)node_end + (size_t)lv.n_children;
       if (nodes.cap < need_nodes * sizeof(Node)) {
         DevBuf nb;
         DK_TRY(Arena::ensure(this, nb, need_nodes * sizeof(Node)));
-        DK_CUDA(cudaMemcpyAsync(nb.p, nodes.p, (size_t)hi * sizeof(Node), cudaMemcpyDeviceToDevice, stream));
+        DK_CUDA(cudaMemcpyAsync(nb.p, nodes.p, (size_t)node_end * sizeof(Node),
+                                cudaMemcpyDeviceToDevice, stream));
         Arena::release(this, nodes);
         nodes = nb;
       }
-      DK_CUDA(cudaMemsetAsync(c64 + 7, 0, 8, stream));
-      DK_CUDA(cudaMemsetAsync(c64 + 16, 0, 8, stream));  // proxy counter
-      TIMED(7, launch_make_proxies((Node*)nodes.p, (uint32_t*)finals.p + fin_lo, n_final - fin_lo,
-                                   hi, (unsigned int*)(c64 + 16), stream));
-      fin_lo = n_final;
-      lo = hi;
-      hi = hi + (uint32_t)retry;
-      continue;
+      const uint32_t n_tiles = lv.n_tiles;
+      DK_TRY(Arena::ensure(this, tiles, (size_t)n_tiles * sizeof(Tile)));
+      DK_TRY(Arena::ensure(this, TH, (size_t)lv.th_entries * 4));
+      TIMED(7, launch_assign((Node*)nodes.p, lo, hi, node_end, (Tile*)tiles.p, lc, stream));
+      TIMED(2, launch_tile_hist((Node*)nodes.p, (Tile*)tiles.p, n_tiles, (uint64_t*)keysA.p,
+                                (uint64_t*)keysB.p, (uint32_t*)TH.p, stream));
+      TIMED(7, launch_node_scan((Node*)nodes.p, lo, hi, (Tile*)tiles.p, (uint32_t*)TH.p, stream));
+      TIMED(3, launch_tile_scatter((Node*)nodes.p, (Tile*)tiles.p, n_tiles, (uint64_t*)keysA.p,
+                                   (uint64_t*)keysB.p, (uint32_t*)TH.p, (int)lv.max_width, stream));
+      lo = node_end;
+      hi = node_end + lv.n_children;
+      node_end = hi;
     }
-    stats.n_partitioned += lv.split_keys;
-    // grow node storage for the children (copying existing nodes)
-    const size_t need_nodes = (size_t)hi + (size_t)lv.n_children;
-    if (nodes.cap < need_nodes * sizeof(Node)) {
-      DevBuf nb;
-      DK_TRY(Arena::ensure(this, nb, need_nodes * sizeof(Node)));
-      DK_CUDA(cudaMemcpyAsync(nb.p, nodes.p, (size_t)hi * sizeof(Node), cudaMemcpyDeviceToDevice, stream));
-      Arena::release(this, nodes);
-      nodes = nb;
+    stats.partition_levels = std::max(stats.partition_levels, (int)levels.size());
+    // distinct counts up the tree, offsets down (the last level splits nothing;
+    // a proxy level comes after the level of the node it stands in for); the
+    // group's slice of the table starts after the earlier groups' k-mers
+    for (int l = (int)levels.size() - 2; l >= 0; --l)
+      TIMED(7, launch_aggregate((Node*)nodes.p, levels[l].first, levels[l].second, stream));
+    TIMED(7, launch_l1_offsets((Node*)nodes.p, group_at[grp], group_at[grp + 1], c64 + 2, stream));
+    for (size_t l = 0; l + 1 < levels.size(); ++l)
+      TIMED(7, launch_child_offsets((Node*)nodes.p, levels[l].first, levels[l].second, stream));
+    TIMED(5, launch_compact((Node*)nodes.p, (uint32_t*)finals.p + fin_g, n_final - fin_g,
+                            (uint64_t*)keysA.p, (uint64_t*)keysB.p, (uint32_t*)cnt.p, out_k, out_c,
+                            stream));
+    DK_CUDA(cudaGetLastError());
+    keys_done += group_keys[grp];
+    if (out_sink) {
+      uint64_t total = 0;
+      DK_TRY(sync_read(c64 + 2, 8, &total));  // the group's compact has finished
+      DK_TRY(out_sink(distinct_done, total - distinct_done, keys_done, n_kmers));
+      distinct_done = total;
     }
-    const uint32_t n_tiles = lv.n_tiles;
-    DK_TRY(Arena::ensure(this, tiles, (size_t)n_tiles * sizeof(Tile)));
-    DK_TRY(Arena::ensure(this, TH, (size_t)lv.th_entries * 4));
-    TIMED(7, launch_assign((Node*)nodes.p, lo, hi, hi, (Tile*)tiles.p, lc, stream));
-    TIMED(2, launch_tile_hist((Node*)nodes.p, (Tile*)tiles.p, n_tiles, (uint64_t*)keysA.p,
-                              (uint64_t*)keysB.p, (uint32_t*)TH.p, stream));
-    TIMED(7, launch_node_scan((Node*)nodes.p, lo, hi, (Tile*)tiles.p, (uint32_t*)TH.p, stream));
-    TIMED(3, launch_tile_scatter((Node*)nodes.p, (Tile*)tiles.p, n_tiles, (uint64_t*)keysA.p,
-                                 (uint64_t*)keysB.p, (uint32_t*)TH.p, (int)lv.max_width, stream));
-    lo = hi;
-    hi = hi + lv.n_children;
   }
-  stats.partition_levels = (int)levels.size();
   stats.n_bins = n_final - (uint32_t)stats.n_bins_retried;
-  DK_CUDA(cudaEventRecord(ev_stage[4], stream));
-  // distinct counts up the tree, offsets down (the last level splits nothing;
-  // a proxy level comes after the level of the node it stands in for)
-  for (int l = (int)levels.size() - 2; l >= 0; --l)
-    TIMED(7, launch_aggregate((Node*)nodes.p, levels[l].first, levels[l].second, stream));
-  TIMED(7, launch_l1_offsets((Node*)nodes.p, (uint32_t)F1, c64 + 2, stream));
-  for (size_t l = 0; l + 1 < levels.size(); ++l)
-    TIMED(7, launch_child_offsets((Node*)nodes.p, levels[l].first, levels[l].second, stream));
+  stats.n_groups = group_at.size() - 1;
   uint64_t tail[16];
   DK_TRY(sync_read(c64 + 2, 128, tail));
   stats.n_bins_resorted = tail[4];
@@ -938,13 +992,6 @@ int Engine::count_device(const uint8_t* d_text, uint64_t nbytes, const dk_input_
   out->n_kmers = n_kmers;
   out->k = out_k;
   out->c = out_c;
-  if (!out->k || !out->c) {
-    set_error("internal: no output buffers");
-    return DK_ERR_INVALID_ARG;
-  }
-  TIMED(5, launch_compact((Node*)nodes.p, (uint32_t*)finals.p, n_final, (uint64_t*)keysA.p,
-                          (uint64_t*)keysB.p, (uint32_t*)cnt.p, out_k, out_c, stream));
-  DK_CUDA(cudaGetLastError());
   if (js) {
     js->nodes.resize(F1);
     DK_TRY(sync_read(nodes.p, (size_t)F1 * sizeof(Node), js->nodes.data()));
@@ -1115,8 +1162,52 @@ int Engine::count_locked(const char* text, uint64_t nbytes, bool text_on_device,
   DK_TRY(acquire_table(upper, true, &dev_tb));
   out_k = (uint64_t*)dev_tb->k;
   out_c = (uint32_t*)dev_tb->c;
+  // A large table for the host moves out group by group on s_out while the
+  // next group is counted.  The host table is sized after the first group,
+  // from its distinct k-mers per k-mer; if a later slice does not fit, the
+  // streaming stops and the whole table is copied at the end instead.
+  TableBuf* h_tb = nullptr;
+  bool streaming = desc->residency == DK_RESIDENT_HOST &&
+                   (upper >= kStreamMinKmers || (flags & DK_FLAG_STREAM_ALL));
+  uint64_t streamed = 0;
+  if (streaming) {
+    out_groups = kStreamGroups;
+    out_sink = [&](uint64_t first, uint64_t n, uint64_t kmers_done, uint64_t kmers_total) -> int {
+      if (!streaming) return DK_OK;
+      if (!h_tb) {
+        const double f = kmers_total ? (double)kmers_done / (double)kmers_total : 1.0;
+        uint64_t est = (uint64_t)((double)(first + n) / std::max(f, 1e-6) * 1.2) + 4096;
+        est = std::min(est, upper);
+        if (acquire_table(est, false, &h_tb) != DK_OK) {
+          h_tb = nullptr;
+          streaming = false;
+          return DK_OK;
+        }
+      }
+      if (first + n > h_tb->cap) {
+        streaming = false;
+        return DK_OK;
+      }
+      if (n) {
+        DK_CUDA(cudaMemcpyAsync((uint64_t*)h_tb->k + first, out_k + first, n * 8,
+                                cudaMemcpyDeviceToHost, s_out));
+        DK_CUDA(cudaMemcpyAsync((uint32_t*)h_tb->c + first, out_c + first, n * 4,
+                                cudaMemcpyDeviceToHost, s_out));
+      }
+      streamed = first + n;
+      return DK_OK;
+    };
+  }
   DeviceTable dt;
   int rc = count_device(d_text, nbytes, *desc, &dt);
+  out_sink = nullptr;
+  out_groups = 1;
+  if (h_tb && (rc != DK_OK || !streaming || streamed != dt.n)) {
+    // copies into it may still run
+    cudaStreamSynchronize(s_out);
+    release_table(h_tb->id);
+    h_tb = nullptr;
+  }
   if (rc != DK_OK) {
     release_table(dev_tb->id);
     return rc;
@@ -1134,21 +1225,27 @@ int Engine::count_locked(const char* text, uint64_t nbytes, bool text_on_device,
     out->on_device = 1;
     out->handle = dev_tb->id;
   } else {
-    TableBuf* h_tb = nullptr;
-    rc = acquire_table(dt.n, false, &h_tb);
-    if (rc != DK_OK) {
-      release_table(dev_tb->id);
-      return rc;
+    if (h_tb) {
+      // streamed: the last slice's copies end the download
+      DK_CUDA(cudaEventRecord(ev_d2h1, s_out));
+      stats.table_streamed = 1;
+    } else {
+      rc = acquire_table(dt.n, false, &h_tb);
+      if (rc != DK_OK) {
+        release_table(dev_tb->id);
+        return rc;
+      }
+      if (dt.n) {
+        DK_CUDA(cudaMemcpyAsync(h_tb->k, dev_tb->k, dt.n * 8, cudaMemcpyDeviceToHost, stream));
+        DK_CUDA(cudaMemcpyAsync(h_tb->c, dev_tb->c, dt.n * 4, cudaMemcpyDeviceToHost, stream));
+      }
+      DK_CUDA(cudaEventRecord(ev_d2h1, stream));
     }
-    if (dt.n) {
-      DK_CUDA(cudaMemcpyAsync(h_tb->k, dev_tb->k, dt.n * 8, cudaMemcpyDeviceToHost, stream));
-      DK_CUDA(cudaMemcpyAsync(h_tb->c, dev_tb->c, dt.n * 4, cudaMemcpyDeviceToHost, stream));
-    }
-    DK_CUDA(cudaEventRecord(ev_d2h1, stream));
     DK_CUDA(cudaEventSynchronize(ev_d2h1));
     float ms_d2h = 0;
     cudaEventElapsedTime(&ms_d2h, ev_stage[5], ev_d2h1);
-    stats.ms_d2h = dt.n ? ms_d2h : 0.0;
+    // the part of the download after the device finished (all of it unless streamed)
+    stats.ms_d2h = dt.n ? std::max(0.0f, ms_d2h) : 0.0;
     release_table(dev_tb->id);
     out->kmers = (uint64_t*)h_tb->k;
     out->counts = (uint32_t*)h_tb->c;

@@ -6,6 +6,7 @@
 #include <mutex>
 #include <string>
 #include <deque>
+#include <functional>
 #include <vector>
 
 #include "../../include/dakc_gb300.h"
@@ -94,6 +95,7 @@ struct Engine {
   int device = 0;
   int sm_count = 0;
   uint64_t budget = 0;
+  uint64_t flags = 0;  // dk_config.flags
   uint64_t dev_bytes = 0, dev_peak = 0;
   cudaStream_t stream = nullptr;            // kernels
   cudaStream_t s_in = nullptr, s_out = nullptr;  // batch uploads / table downloads
@@ -168,6 +170,12 @@ struct Engine {
   int release_table(uint64_t id);
   int count_device(const uint8_t* d_text, uint64_t nbytes, const dk_input_desc& desc,
                    DeviceTable* out, JobSet* js = nullptr);
+  // When set, count_device counts in out_groups groups of level-1 buckets
+  // (split by k-mers) and calls out_sink(first, n, kmers_done, kmers_total)
+  // once a group's table slice [first, first + n) is final in device memory;
+  // the next group runs while the sink moves that slice.
+  std::function<int(uint64_t, uint64_t, uint64_t, uint64_t)> out_sink;
+  int out_groups = 1;
   int count_batch(const dk_job* jobs, int njobs, const dk_input_desc* desc, dk_table* outs);
   DevBuf jobmeta;  // device job_start / job_end / job_nul
   int count(const char* text, uint64_t nbytes, bool text_on_device, const dk_input_desc* desc,

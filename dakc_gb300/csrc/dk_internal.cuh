@@ -140,7 +140,9 @@ int launch_bin_count(Node* nodes, const uint32_t* final_list, uint32_t n_final, 
                      uint64_t* B, uint32_t* C, int use_hash, unsigned long long* ctr, int sm_count,
                      cudaStream_t s);
 int launch_aggregate(Node* nodes, uint32_t node_lo, uint32_t node_hi, cudaStream_t s);
-int launch_l1_offsets(Node* nodes, uint32_t n1, unsigned long long* total_d, cudaStream_t s);
+// level-1 nodes [b0, b1) follow the *total_d distinct keys before them
+int launch_l1_offsets(Node* nodes, uint32_t b0, uint32_t b1, unsigned long long* total_d,
+                      cudaStream_t s);
 int launch_child_offsets(Node* nodes, uint32_t node_lo, uint32_t node_hi, cudaStream_t s);
 int launch_compact(const Node* nodes, const uint32_t* final_list, uint32_t n_final,
                    const uint64_t* A, const uint64_t* B, const uint32_t* C, uint64_t* out_k,

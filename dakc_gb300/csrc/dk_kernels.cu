@@ -1628,19 +1628,25 @@ __global__ void k_aggregate(Node* nodes, uint32_t lo, uint32_t hi) {
   nodes[i].d = d;
 }
 
-__global__ void k_l1_out_offsets(Node* nodes, uint32_t n1, unsigned long long* total_d) {
+// output offsets of level-1 nodes [b0, b1): they follow the *total_d distinct
+// keys placed before them, and *total_d grows by theirs
+__global__ void k_l1_out_offsets(Node* nodes, uint32_t b0, uint32_t b1,
+                                 unsigned long long* total_d) {
   __shared__ unsigned long long tmp[32];
+  const uint32_t n1 = b1 - b0;
+  const unsigned long long before = *total_d;
   const uint32_t per = (n1 + blockDim.x - 1) / blockDim.x;
-  const uint32_t lo = min(n1, threadIdx.x * per), hi = min(n1, lo + per);
+  const uint32_t lo = b0 + min(n1, threadIdx.x * per), hi = min(b1, lo + per);
   unsigned long long s = 0;
   for (uint32_t i = lo; i < hi; ++i) s += nodes[i].d;
   unsigned long long tot;
-  unsigned long long base = block_excl_scan<unsigned long long>(s, tmp, &tot);
+  // the block scan synchronises: every thread has read *total_d before it changes
+  unsigned long long base = before + block_excl_scan<unsigned long long>(s, tmp, &tot);
   for (uint32_t i = lo; i < hi; ++i) {
     nodes[i].out_off = base;
     base += nodes[i].d;
   }
-  if (threadIdx.x == 0) *total_d = tot;
+  if (threadIdx.x == 0) *total_d = before + tot;
 }
 
 __global__ void __launch_bounds__(256) k_child_offsets(Node* nodes, uint32_t lo) {
@@ -1947,8 +1953,9 @@ int launch_aggregate(Node* nodes, uint32_t lo, uint32_t hi, cudaStream_t s) {
   return 1;
 }
 
-int launch_l1_offsets(Node* nodes, uint32_t n1, unsigned long long* total_d, cudaStream_t s) {
-  k_l1_out_offsets<<<1, 1024, 0, s>>>(nodes, n1, total_d);
+int launch_l1_offsets(Node* nodes, uint32_t b0, uint32_t b1, unsigned long long* total_d,
+                      cudaStream_t s) {
+  k_l1_out_offsets<<<1, 1024, 0, s>>>(nodes, b0, b1, total_d);
   return 1;
 }
 

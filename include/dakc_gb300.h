@@ -81,8 +81,13 @@ typedef struct {
   int device;          /* CUDA device ordinal                                    */
   int reserved0;
   uint64_t mem_budget; /* device bytes the context may hold; 0 = 80% of free    */
-  uint64_t flags;      /* reserved, 0                                            */
+  uint64_t flags;      /* DK_FLAG_* bits, 0 by default                           */
 } dk_config;
+
+/* dk_config.flags: a host table is normally copied out group by group, while
+ * the rest of the count runs, only when the input holds at least 64 Mi k-mers;
+ * with this flag every host table is (the same table, other timing) */
+#define DK_FLAG_STREAM_ALL 1ull
 
 typedef struct {
   int line_width;  /* READLEN: bytes per line before the terminator (>= 1)      */
@@ -134,6 +139,9 @@ typedef struct {
                                hot k-mer, counted whole by one hash bin          */
   uint64_t n_bins_retried;  /* of those, bins with too many distinct keys, which
                                were partitioned further                          */
+  uint64_t n_groups;        /* groups of level-1 buckets counted one after another */
+  uint64_t table_streamed;  /* 1: the host table was copied out group by group
+                               while the count ran; 0: after it               */
 } dk_stats;
 
 /* One read set of a batch (dk_count_batch). */

@@ -242,3 +242,42 @@ def test_skewed_node_with_many_distinct_kmers_is_repartitioned(engine, variant):
     assert r.n_kmers == nk and np.array_equal(r.kmers, keys) and np.array_equal(r.counts, counts)
     if variant == dk.VARIANT_HASH:
         assert st["n_bins_retried"] >= 2
+
+
+@pytest.fixture(scope="module")
+def streaming_engine():
+    with dk.Engine(0, flags=dk.FLAG_STREAM_ALL) as e:
+        yield e
+
+
+@pytest.mark.parametrize("variant", VARIANTS)
+def test_streamed_host_table(streaming_engine, variant):
+    """A host table copied out group by group while the count runs is the
+    oracle's table."""
+    rs = synth.plain_1m()
+    text = rs.text[: 40_000 * (rs.line_width + 1)]
+    check(streaming_engine, text, rs.line_width, rs.k, variant)
+    st = streaming_engine.stats()
+    assert st["n_groups"] >= 2 and st["table_streamed"] == 1
+
+
+@pytest.mark.parametrize("variant", VARIANTS)
+def test_streamed_table_size_estimate_too_small(variant):
+    """The first group holds ten k-mers copied 10,000 times each, the rest are
+    random: the host table sized from the first group is too small, so the
+    table is copied after the count instead, and is still exact."""
+    rng = np.random.Generator(np.random.PCG64(79))
+    acgt = np.frombuffer(b"ACGT", np.uint8)
+    W = 31
+    hot = rng.choice(acgt, (10, W))
+    hot[:, :4] = ord("C")  # C = 0: the smallest keys, first group
+    lines = np.empty((100_000 + 100_000, W + 1), np.uint8)
+    lines[:100_000, :W] = hot[np.arange(100_000) % 10]
+    lines[100_000:, :W] = rng.choice(acgt, (100_000, W))
+    lines[:, W] = ord("\n")
+    rng.shuffle(lines)
+    # a fresh context: no pooled host table larger than the estimate
+    with dk.Engine(0, flags=dk.FLAG_STREAM_ALL) as e:
+        check(e, lines.reshape(-1), W, 31, variant)
+        st = e.stats()
+    assert st["n_groups"] >= 2 and st["table_streamed"] == 0
