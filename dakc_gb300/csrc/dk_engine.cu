@@ -15,6 +15,7 @@
 
 #include <cuda_runtime.h>
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cstdio>
 #include <cstring>
@@ -161,14 +162,9 @@ Engine::~Engine() {
   for (DevBuf* b : {&text, &text2, &keysA, &keysB, &cnt, &H, &O, &nodes, &tiles, &TH, &finals, &ctrs,
                     &aux})
     Arena::release(this, *b);
-  for (auto& t : tables) {
-    if (t.on_device) {
-      cudaFree(t.k);
-      cudaFree(t.c);
-    } else {
-      cudaFreeHost(t.k);
-      cudaFreeHost(t.c);
-    }
+  for (auto& t : tables) {  // device tables (host tables live in the shared pool)
+    cudaFree(t.k);
+    cudaFree(t.c);
   }
   for (auto& ev : ev_stage)
     if (ev) cudaEventDestroy(ev);
@@ -240,10 +236,22 @@ static uint64_t size_class(uint64_t n) {
   return (n + step - 1) / step * step;
 }
 
-// Table storage: a pool of allocations reused across calls (pinned host or device).
+HostPool::~HostPool() {
+  for (auto& t : tables) {
+    cudaFreeHost(t.k);
+    cudaFreeHost(t.c);
+  }
+}
+
+// table handles are unique across all pools of the process
+static std::atomic<uint64_t> g_table_ids{0};
+
+// Table storage: pools of allocations reused across calls (device tables per
+// engine, page-locked host tables shared with the context's serving workers).
 int Engine::acquire_table(uint64_t n, bool on_device, TableBuf** out) {
   Engine* e = this;
-  std::lock_guard<std::mutex> g(pool_mu);
+  std::deque<TableBuf>& tables = on_device ? this->tables : hpool->tables;
+  std::lock_guard<std::mutex> g(on_device ? pool_mu : hpool->mu);
   TableBuf* best = nullptr;
   for (auto& t : tables)
     if (!t.in_use && t.on_device == on_device && t.cap >= n && (!best || t.cap < best->cap)) best = &t;
@@ -271,7 +279,7 @@ int Engine::acquire_table(uint64_t n, bool on_device, TableBuf** out) {
         return DK_ERR_OOM;
       }
     }
-    t.id = ++table_ids;
+    t.id = ++g_table_ids;
     tables.push_back(t);
     best = &tables.back();
   }
@@ -282,8 +290,7 @@ int Engine::acquire_table(uint64_t n, bool on_device, TableBuf** out) {
   return DK_OK;
 }
 
-int Engine::release_table(uint64_t id) {
-  std::lock_guard<std::mutex> g(pool_mu);
+static int release_in(std::deque<TableBuf>& tables, uint64_t id) {
   for (auto& t : tables)
     if (t.id == id && t.in_use) {
       if (t.refs > 1) {
@@ -295,6 +302,15 @@ int Engine::release_table(uint64_t id) {
       return DK_OK;
     }
   return DK_ERR_NOT_FOUND;
+}
+
+int Engine::release_table(uint64_t id) {
+  {
+    std::lock_guard<std::mutex> g(pool_mu);
+    if (release_in(tables, id) == DK_OK) return DK_OK;
+  }
+  std::lock_guard<std::mutex> g(hpool->mu);
+  return release_in(hpool->tables, id);
 }
 
 // Level-1 split bits for a count of at most n_upper k-mers: one scatter pass
@@ -543,7 +559,7 @@ int Engine::count_batch(const dk_job* jobs, int njobs, const dk_input_desc* desc
       DK_CUDA(cudaEventRecord(ev_out1[b], s_out));
       out_pending[b] = true;
       {
-        std::lock_guard<std::mutex> pg(pool_mu);
+        std::lock_guard<std::mutex> pg(hpool->mu);
         h_tb->refs = (uint32_t)nj;
       }
       for (int j = 0; j < nj; ++j) {
@@ -1345,12 +1361,13 @@ int dk_count_batch(dk_ctx* ctx, const dk_job* jobs, int njobs, const dk_input_de
 int dk_table_free(dk_ctx* ctx, dk_table* t) {
   if (!ctx || !t) return DK_ERR_INVALID_ARG;
   if (!t->handle) return DK_OK;  // empty table
-  if (t->handle >> 48) {  // a served table: owned by one of the serving workers
+  if ((t->handle >> 48) && ctx->server) {  // a served table: released by its worker
     const int rc = dk::serve_release(ctx->server, t->handle);
     std::memset(t, 0, sizeof(*t));
     return rc;
   }
-  const int rc = ctx->eng.release_table(t->handle);  // the pool has its own lock
+  // (a served table freed after dk_serve_stop is in the context's shared host pool)
+  const int rc = ctx->eng.release_table(t->handle & ((1ull << 48) - 1));  // the pool has its own lock
   std::memset(t, 0, sizeof(*t));
   return rc;
 }

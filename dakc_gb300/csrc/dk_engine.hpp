@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 #include <cstdint>
 #include <map>
+#include <memory>
 #include <mutex>
 #include <string>
 #include <deque>
@@ -53,6 +54,14 @@ struct TableBuf {
   bool on_device = false;
   bool in_use = false;
   uint32_t refs = 0;  // tables handed out on this buffer (batch results share one)
+};
+
+// Page-locked host tables, shared by a context's engine and its serving
+// workers: a table released by any of them is reused by the next count of any.
+struct HostPool {
+  std::mutex mu;
+  std::deque<TableBuf> tables;  // deque: stable addresses
+  ~HostPool();
 };
 
 struct DeviceTable {
@@ -111,9 +120,9 @@ struct Engine {
   size_t node_cap_needed = 0;
   uint64_t* out_k = nullptr;
   uint32_t* out_c = nullptr;
-  std::deque<TableBuf> tables;  // deque: stable addresses; guarded by pool_mu
+  std::deque<TableBuf> tables;  // device tables; deque: stable addresses; guarded by pool_mu
   std::mutex pool_mu;           // tables may be released while a count runs
-  uint64_t table_ids = 0;
+  std::shared_ptr<HostPool> hpool = std::make_shared<HostPool>();  // host tables
 
   cudaEvent_t ev_stage[8] = {};
   static constexpr int kKEvents = 512;

@@ -774,23 +774,30 @@ __global__ void k_classify(Node* nodes, uint32_t lo, uint32_t hi, uint32_t* fina
 }
 
 // Give each split node its children block, its partition tiles and their
-// histogram rows (buffers sized by the host from k_classify's counts).
+// histogram rows (buffers sized by the host from k_classify's counts); one
+// warp per node, its lanes write the tiles.
 __global__ void k_assign(Node* nodes, uint32_t lo, uint32_t hi, uint32_t child_base, Tile* tiles,
                          LevelCounters* ctr) {
-  const uint32_t i = lo + blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= hi) return;
+  const uint32_t i = lo + ((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  if (i >= hi) return;  // warp-uniform
   const Node nd = nodes[i];
   if (nd.state != NODE_SPLIT) return;
   const uint32_t R = 1u << nd.width;
   const uint32_t nt = (uint32_t)((nd.n + kTileKeys - 1) / kTileKeys);
-  const uint32_t tb = atomicAdd(&ctr->n_tiles_assigned, nt);
-  const uint32_t fc = child_base + atomicAdd(&ctr->n_children_assigned, R);
-  const unsigned long long thb = atomicAdd(&ctr->th_assigned, (unsigned long long)nt * R);
-  nodes[i].first_child = fc;
-  nodes[i].tile_base = tb;
-  nodes[i].ntiles = nt;
-  nodes[i].th_base = thb;
-  for (uint32_t t = 0; t < nt; ++t) {
+  uint32_t tb = 0, fc = 0;
+  unsigned long long thb = 0;
+  if (lane_id() == 0) {
+    tb = atomicAdd(&ctr->n_tiles_assigned, nt);
+    fc = child_base + atomicAdd(&ctr->n_children_assigned, R);
+    thb = atomicAdd(&ctr->th_assigned, (unsigned long long)nt * R);
+    nodes[i].first_child = fc;
+    nodes[i].tile_base = tb;
+    nodes[i].ntiles = nt;
+    nodes[i].th_base = thb;
+  }
+  tb = __shfl_sync(0xFFFFFFFFu, tb, 0);
+  thb = __shfl_sync(0xFFFFFFFFu, thb, 0);
+  for (uint32_t t = lane_id(); t < nt; t += 32) {
     Tile tl;
     tl.start = nd.start + (uint64_t)t * kTileKeys;
     tl.n = (uint32_t)min((uint64_t)kTileKeys, nd.n - (uint64_t)t * kTileKeys);
@@ -834,8 +841,8 @@ __global__ void __launch_bounds__(256) k_tile_hist(const Node* nodes, const Tile
 
 // one CTA per node of the level; split nodes turn their tiles' counts into
 // offsets within each child and create the 2^width children
-__global__ void __launch_bounds__(256) k_node_scan(Node* nodes, uint32_t lo, Tile* tiles,
-                                                   uint32_t* TH) {
+__global__ void __launch_bounds__(1024) k_node_scan(Node* nodes, uint32_t lo, Tile* tiles,
+                                                    uint32_t* TH) {
   __shared__ unsigned long long csize[1u << kMaxSplitBits];
   __shared__ unsigned long long tmp[32];
   const uint32_t i = lo + blockIdx.x;
@@ -845,25 +852,25 @@ __global__ void __launch_bounds__(256) k_node_scan(Node* nodes, uint32_t lo, Til
   for (uint32_t j = threadIdx.x; j < R; j += blockDim.x) {
     uint32_t run = 0;
     uint32_t* col = TH + nd.th_base + j;
-    // eight tiles at a time: their loads are independent, only the running
+    // sixteen tiles at a time: their loads are independent, only the running
     // sum is serial
     uint32_t t = 0;
     // a digit with more than a quarter of a full tile marks that tile hot
     constexpr uint32_t kHotCount = kTileKeys / 4;
-    for (; t + 8 <= nd.ntiles; t += 8) {
-      uint32_t c[8];
+    for (; t + 16 <= nd.ntiles; t += 16) {
+      uint32_t c[16];
 #pragma unroll
-      for (int u = 0; u < 8; ++u) c[u] = col[(uint64_t)(t + u) * R];
+      for (int u = 0; u < 16; ++u) c[u] = col[(t + u) * R];  // < 2^32: a node's ntiles * R
 #pragma unroll
-      for (int u = 0; u < 8; ++u) {
-        col[(uint64_t)(t + u) * R] = run;
+      for (int u = 0; u < 16; ++u) {
+        col[(t + u) * R] = run;
         run += c[u];
         if (c[u] > kHotCount) tiles[nd.tile_base + t + u].hot = 1;
       }
     }
     for (; t < nd.ntiles; ++t) {
-      const uint32_t c = col[(uint64_t)t * R];
-      col[(uint64_t)t * R] = run;
+      const uint32_t c = col[t * R];
+      col[t * R] = run;
       run += c;
       if (c > kHotCount) tiles[nd.tile_base + t].hot = 1;
     }
@@ -1617,15 +1624,18 @@ __global__ void __launch_bounds__(kBinThreads, kBinBlocksPerSM) k_bin_count(Node
 }
 
 // ----------------------------------------------------- tree reductions
+// one warp per node: a split node's distinct keys are its children's
 __global__ void k_aggregate(Node* nodes, uint32_t lo, uint32_t hi) {
-  const uint32_t i = lo + blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= hi) return;
-  const Node nd = nodes[i];
-  if (nd.state != NODE_SPLIT) return;
-  uint64_t d = 0;
-  const uint32_t R = 1u << nd.width;
-  for (uint32_t j = 0; j < R; ++j) d += nodes[nd.first_child + j].d;
-  nodes[i].d = d;
+  const uint32_t i = lo + ((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  if (i >= hi) return;  // warp-uniform
+  const uint32_t state = nodes[i].state;
+  if (state != NODE_SPLIT) return;
+  const uint32_t R = 1u << nodes[i].width, fc = nodes[i].first_child;
+  unsigned long long d = 0;
+  for (uint32_t j = lane_id(); j < R; j += 32) d += nodes[fc + j].d;
+#pragma unroll
+  for (int o = 16; o; o >>= 1) d += __shfl_xor_sync(0xFFFFFFFFu, d, o);
+  if (lane_id() == 0) nodes[i].d = d;
 }
 
 // output offsets of level-1 nodes [b0, b1): they follow the *total_d distinct
@@ -1907,7 +1917,8 @@ int launch_assign(Node* nodes, uint32_t lo, uint32_t hi, uint32_t child_base, Ti
                   LevelCounters* ctr, cudaStream_t s) {
   const uint32_t n = hi - lo;
   if (!n) return 0;
-  k_assign<<<(n + 255) / 256, 256, 0, s>>>(nodes, lo, hi, child_base, tiles, ctr);
+  k_assign<<<(uint32_t)(((uint64_t)n * 32 + 255) / 256), 256, 0, s>>>(nodes, lo, hi, child_base,
+                                                                      tiles, ctr);
   return 1;
 }
 
@@ -1921,7 +1932,8 @@ int launch_tile_hist(const Node* nodes, const Tile* tiles, uint32_t n_tiles, con
 int launch_node_scan(Node* nodes, uint32_t lo, uint32_t hi, Tile* tiles, uint32_t* TH,
                      cudaStream_t s) {
   if (hi <= lo) return 0;
-  k_node_scan<<<hi - lo, 256, 0, s>>>(nodes, lo, tiles, TH);
+  // few nodes (large ones) get wide CTAs: each thread then scans fewer digits
+  k_node_scan<<<hi - lo, (hi - lo) <= 4096 ? 1024 : 256, 0, s>>>(nodes, lo, tiles, TH);
   return 1;
 }
 
@@ -1949,7 +1961,7 @@ int launch_bin_count(Node* nodes, const uint32_t* final_list, uint32_t n_final, 
 
 int launch_aggregate(Node* nodes, uint32_t lo, uint32_t hi, cudaStream_t s) {
   if (hi <= lo) return 0;
-  k_aggregate<<<(hi - lo + 255) / 256, 256, 0, s>>>(nodes, lo, hi);
+  k_aggregate<<<(uint32_t)(((uint64_t)(hi - lo) * 32 + 255) / 256), 256, 0, s>>>(nodes, lo, hi);
   return 1;
 }
 

@@ -176,6 +176,9 @@ int dk_serve_start(dk_ctx* ctx, int workers, int max_batch_jobs) {
       return rc;
     }
     s->workers[w].budget = share;
+    // host tables come from (and return to) the context's pool, so a table
+    // size any worker has used is ready for every worker
+    s->workers[w].eng->hpool = base->hpool;
   }
   for (int w = 0; w < workers; ++w) s->workers[w].th = std::thread([s, w] { s->run_worker(w); });
   dk::set_server(ctx, s);

@@ -70,3 +70,27 @@ def test_admission_rejects_oversized_job():
             eng.submit(big, 250, 31)
         assert e.value.status == dk.DK_ERR_ADMISSION
         eng.serve_stop()
+
+
+def test_served_tables_share_the_context_pool_and_outlive_the_server():
+    """Host tables of every serving worker come from the context's pool: a
+    table handed out by dk_wait stays readable after dk_serve_stop and is
+    freed through the context; sizes one worker used are reused by others."""
+    import ctypes
+    jobs = texts(8, 12)
+    with dk.Engine(0) as eng:
+        eng.serve_start(workers=2, max_batch_jobs=1)
+        held = []
+        for t in jobs:
+            tk = eng.submit(t, 250, 31, dk.VARIANT_HASH)
+            tab, info = dk.Table(), dk.JobInfo()
+            assert eng.lib.dk_wait(eng.h, tk, 60_000, ctypes.byref(tab), ctypes.byref(info)) == 0
+            held.append(tab)
+        eng.serve_stop()
+        for j, tab in enumerate(held):
+            keys, counts, nk = pyoracle.count(jobs[j], 250, 31)
+            n = int(tab.n)
+            assert tab.n_kmers == nk and n == keys.size
+            assert np.array_equal(np.ctypeslib.as_array(tab.kmers, shape=(n,)), keys), j
+            assert np.array_equal(np.ctypeslib.as_array(tab.counts, shape=(n,)), counts), j
+            eng.free_table(tab)
