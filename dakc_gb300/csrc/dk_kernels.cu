@@ -436,15 +436,16 @@ template <bool PAK>
 __global__ void __launch_bounds__(kLineThreads, 2) k_l1_lines_chunked(ExtractArgs a,
                                                                      const uint64_t* __restrict__ O,
                                                                      uint64_t* __restrict__ keys_out,
-                                                                     unsigned long long* __restrict__ counters) {
+                                                                     unsigned long long* __restrict__ counters,
+                                                                     int chunk) {
   extern __shared__ __align__(128) uint8_t smraw[];
   const int W = a.W, k = a.k, F1 = a.F1;
   const uint64_t stride = (uint64_t)W + 1;
   const uint32_t bb = tile_buf_bytes(blockDim.x, stride);
   unsigned long long* stage = reinterpret_cast<unsigned long long*>(smraw + 128 + bb);  // chunk keys
-  unsigned long long* cursor = stage + (size_t)blockDim.x * kLineChunk;                  // F1
-  uint32_t* ccount = reinterpret_cast<uint32_t*>(cursor + F1);                            // F1
-  uint32_t* coff = ccount + F1;                                                           // F1
+  unsigned long long* cursor = stage + (size_t)blockDim.x * chunk;                       // F1
+  uint32_t* cnt2 = reinterpret_cast<uint32_t*>(cursor + F1);                              // 2 x F1
+  uint32_t* coff = cnt2 + 2 * F1;                                                         // F1
   uint32_t* tmp = coff + F1;                                                              // 32
   uint8_t* lut = reinterpret_cast<uint8_t*>(tmp + 32);                                    // 256
   TextTiles T;
@@ -452,8 +453,14 @@ __global__ void __launch_bounds__(kLineThreads, 2) k_l1_lines_chunked(ExtractArg
   T.buf1 = T.buf0;  // one buffer: tile t+1 is fetched once tile t is done
   for (int b = threadIdx.x; b < F1; b += blockDim.x) {
     cursor[b] = O[(size_t)blockIdx.x * F1 + b];
-    ccount[b] = 0;
+    cnt2[b] = 0;
+    cnt2[F1 + b] = 0;
   }
+  // Bucket counts alternate between two arrays by chunk: chunk c counts in
+  // cnt2[c & 1], and the next chunk advances the cursors by them (after its
+  // first barrier, when every thread has finished chunk c's flush) and clears
+  // them for the chunk after.
+  int cur = 0;
   init_lut(lut, a.conv);
   __syncthreads();
   const uint32_t nt = T.ntiles();
@@ -474,8 +481,10 @@ __global__ void __launch_bounds__(kLineThreads, 2) k_l1_lines_chunked(ExtractArg
     // warm-up: positions before the first possible k-mer end emit nothing
     const int warm = min(k - 1, W);
     for (int p = 0; p < warm; ++p) r.template step<PAK>(r.stopped ? 0xF0u : lut[line[p]], p, W, k, a.kmask);
-    for (int p0 = warm; p0 < W; p0 += kLineChunk) {  // uniform over the block
-      const int p1 = min(W, p0 + kLineChunk);
+    for (int p0 = warm; p0 < W; p0 += chunk) {  // uniform over the block
+      const int p1 = min(W, p0 + chunk);
+      uint32_t* ccount = cnt2 + (cur ? F1 : 0);  // this chunk's counts
+      uint32_t* cprev = cnt2 + (cur ? 0 : F1);   // the previous chunk's
       const LineRoll r0 = r;
       for (int p = p0; p < p1 && !r.stopped; ++p)
         if (r.template step<PAK>(lut[line[p]], p, W, k, a.kmask))
@@ -484,6 +493,8 @@ __global__ void __launch_bounds__(kLineThreads, 2) k_l1_lines_chunked(ExtractArg
       for (int b = threadIdx.x; b < F1; b += blockDim.x) {
         coff[b] = ccount[b];
         ccount[b] = 0;
+        cursor[b] += cprev[b];
+        cprev[b] = 0;
       }
       __syncthreads();
       const uint32_t Tn = block_scan_array<uint32_t>(coff, F1, tmp);
@@ -492,7 +503,7 @@ __global__ void __launch_bounds__(kLineThreads, 2) k_l1_lines_chunked(ExtractArg
         if (r.template step<PAK>(lut[line[p]], p, W, k, a.kmask)) {
           const uint32_t b = (uint32_t)(r.key >> a.shift1);
           const uint32_t pos = coff[b] + atomicAdd(&ccount[b], 1u);
-          if (DK_OK_IDX(pos < (uint32_t)blockDim.x * kLineChunk, 41, pos)) stage[pos] = r.key;
+          if (DK_OK_IDX(pos < (uint32_t)blockDim.x * chunk, 41, pos)) stage[pos] = r.key;
         }
       __syncthreads();
       for (uint32_t i = threadIdx.x; i < Tn; i += blockDim.x) {
@@ -500,12 +511,7 @@ __global__ void __launch_bounds__(kLineThreads, 2) k_l1_lines_chunked(ExtractArg
         const uint32_t b = (uint32_t)(key >> a.shift1);
         keys_out[cursor[b] + (i - coff[b])] = key;
       }
-      __syncthreads();
-      for (int b = threadIdx.x; b < F1; b += blockDim.x) {
-        cursor[b] += ccount[b];
-        ccount[b] = 0;
-      }
-      __syncthreads();
+      cur ^= 1;
     }
     // every thread's generic accesses of the buffer are ordered before the
     // bulk copy that refills it
@@ -1794,13 +1800,20 @@ static size_t lines_smem(const ExtractArgs& a, bool scatter) {
 // directly; plain counts stage their tiles (k_l1_scatter)
 static bool direct_scatter(int W, bool jobs) { return jobs && W <= kLineMaxW; }
 
-static size_t chunked_smem(const ExtractArgs& a) {
+static size_t chunked_smem(const ExtractArgs& a, int chunk) {
   return 128 + (size_t)tile_buf_bytes(kLineThreads, (uint64_t)a.W + 1) +
-         (size_t)kLineThreads * kLineChunk * 8 + (size_t)a.F1 * 16 + 32 * 4 + 256;
+         (size_t)kLineThreads * chunk * 8 + (size_t)a.F1 * 20 + 32 * 4 + 256;
 }
 // plain counts whose chunked thread-per-line scatter fits two CTAs per SM
 static bool chunked_scatter(const ExtractArgs& a) {
-  return !a.njobs && a.W <= kLineMaxW && chunked_smem(a) <= kMaxSmemPerBlock / 2 - 1024;
+  return !a.njobs && a.W <= kLineMaxW &&
+         chunked_smem(a, kLineChunk) <= kMaxSmemPerBlock / 2 - 1024;
+}
+// positions per chunk: twice kLineChunk where that still fits two CTAs per SM
+// (half the chunk barriers and bucket scans, bucket runs twice as long)
+static int chunk_positions(const ExtractArgs& a) {
+  return chunked_smem(a, 2 * kLineChunk) <= kMaxSmemPerBlock / 2 - 1024 ? 2 * kLineChunk
+                                                                        : kLineChunk;
 }
 
 int launch_l1_count(const ExtractArgs& a, int grid, uint32_t* H, unsigned long long* counters,
@@ -1876,7 +1889,8 @@ int launch_l1_scatter(const ExtractArgs& a, int grid, const uint64_t* O, uint64_
   if (chunked_scatter(a)) {
     auto* kern = a.conv == 1 ? k_l1_lines_chunked<true> : k_l1_lines_chunked<false>;
     allow_max_smem(kern);
-    kern<<<grid, kLineThreads, chunked_smem(a), s>>>(a, O, keys, counters);
+    const int chunk = chunk_positions(a);
+    kern<<<grid, kLineThreads, chunked_smem(a, chunk), s>>>(a, O, keys, counters, chunk);
     return 1;
   }
   if (direct_scatter(a.W, a.njobs != 0)) {
