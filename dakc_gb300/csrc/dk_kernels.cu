@@ -1447,8 +1447,9 @@ __device__ bool bin_hashed(Node* nodes, uint32_t ni, const Node& nd, uint64_t* k
   const uint32_t n = (uint32_t)nd.n;
   const uint32_t T = blockDim.x;
   DK_PHASE_BEGIN();
-  // digits: the top D free bits, D from the bin size (a bound on its distinct keys)
-  int D = ceil_log2_u64(n);
+  // digits: the top D free bits, about n / 8 of them (ranks within a digit
+  // range compare its few keys; the digit scan and marks shrink with R)
+  int D = ceil_log2_u64(n) - 3;
   D = max(4, min(D, kBinDigitBits));
   D = min(D, (int)nd.shift);
   const int sh = nd.shift - D;
