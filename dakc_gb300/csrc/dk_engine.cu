@@ -29,7 +29,7 @@ namespace dk {
 // host tables of at least this many k-mers (bound) move out while the count
 // runs, in this many groups of level-1 buckets
 constexpr uint64_t kStreamMinKmers = 64ull << 20;
-constexpr int kStreamGroups = 8;
+constexpr int kStreamGroups = 16;
 
 // --------------------------------------------------------------- helpers
 static int ceil_log2(uint64_t x) {
@@ -879,6 +879,7 @@ int Engine::count_device(const uint8_t* d_text, uint64_t nbytes, const dk_input_
     uint32_t lo = group_at[grp], hi = group_at[grp + 1];
     const uint32_t fin_g = n_final;  // first final node of the group
     uint32_t fin_lo = n_final;       // first final node of this pass
+    uint32_t pass_big = 0;           // big hash bins among them
     // Every split fixes at least one more key bit and nodes with at most
     // kDenseBits free bits are final, so the levels end within 2k - kDenseBits
     // splits (a proxy level fixes no bit, but follows a split of its own); the
@@ -912,6 +913,7 @@ int Engine::count_device(const uint8_t* d_text, uint64_t nbytes, const dk_input_
         return DK_ERR_INVALID_ARG;
       }
       n_final = lv.n_final;
+      pass_big += lv.n_big;
       if (lv.n_split == 0) {
         // this pass's levels are done: count its final nodes
         if (grp == 0 && fin_lo == fin_g) DK_CUDA(cudaEventRecord(ev_stage[3], stream));
@@ -920,7 +922,8 @@ int Engine::count_device(const uint8_t* d_text, uint64_t nbytes, const dk_input_
                                   (uint64_t*)keysA.p, (uint64_t*)keysB.p, (uint32_t*)cnt.p,
                                   use_hash ? 1 : 0, c64, sm_count, stream));
         DK_CUDA(cudaEventRecord(ev_stage[4], stream));
-        if (!big_ok) break;
+        if (!big_ok || pass_big == 0) break;  // only big bins can ask for a retry
+        pass_big = 0;
         uint64_t retry = 0;
         DK_TRY(sync_read(c64 + 7, 8, &retry));
         if (retry == 0) break;

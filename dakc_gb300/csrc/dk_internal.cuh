@@ -56,7 +56,8 @@ struct LevelCounters {
   uint32_t n_tiles_assigned;
   uint32_t n_children_assigned;
   unsigned long long th_assigned;
-  uint32_t pad[2];
+  uint32_t n_big;  // final nodes larger than a bin (big hash bins) at this level
+  uint32_t pad;
 };
 static_assert(sizeof(LevelCounters) == 64, "LevelCounters is read back as 64 bytes");
 

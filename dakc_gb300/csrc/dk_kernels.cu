@@ -762,6 +762,7 @@ __global__ void k_classify(Node* nodes, uint32_t lo, uint32_t hi, uint32_t* fina
       (big_ok && nd.skewed && nd.n < (1ull << 31))) {
     nodes[i].state = NODE_FINAL;
     final_list[atomicAdd(&ctr->n_final, 1u)] = i;
+    if (nd.n > (uint64_t)bin_cap && nd.shift > kDenseBits) atomicAdd(&ctr->n_big, 1u);
     return;
   }
   const uint64_t target = (uint64_t)max(1, split_target / 2);  // children ~ target keys
