@@ -159,7 +159,7 @@ int Engine::init(const dk_config* cfg) {
 Engine::~Engine() {
   for (cudaStream_t st : {stream, s_in, s_out})
     if (st) cudaStreamSynchronize(st);
-  for (DevBuf* b : {&text, &text2, &keysA, &keysB, &cnt, &H, &O, &nodes, &tiles, &TH, &finals, &ctrs,
+  for (DevBuf* b : {&text, &text2, &keysA, &keysB, &cnt, &H, &O, &nodes, &tiles, &TH, &finals, &bigs, &ctrs,
                     &aux})
     Arena::release(this, *b);
   for (auto& t : tables) {  // device tables (host tables live in the shared pool)
@@ -872,14 +872,17 @@ int Engine::count_device(const uint8_t* d_text, uint64_t nbytes, const dk_input_
   const int big_ok = use_hash ? 1 : 0;
   uint32_t node_end = (uint32_t)F1;  // nodes [0, node_end) exist
   uint32_t n_final = 0;              // final nodes listed so far (all groups)
+  uint32_t n_bigf = 0;               // big-bin final nodes listed so far
   uint64_t keys_done = 0, distinct_done = 0;
   DK_TRY(Arena::ensure(this, finals, (size_t)F1 * 4));
+  DK_TRY(Arena::ensure(this, bigs, (size_t)F1 * 4));
   for (size_t grp = 0; grp + 1 < group_at.size(); ++grp) {
     std::vector<std::pair<uint32_t, uint32_t>> levels;  // node ranges per level
     uint32_t lo = group_at[grp], hi = group_at[grp + 1];
     const uint32_t fin_g = n_final;  // first final node of the group
+    const uint32_t big_g = n_bigf;   // first big bin of the group
     uint32_t fin_lo = n_final;       // first final node of this pass
-    uint32_t pass_big = 0;           // big hash bins among them
+    uint32_t big_lo = n_bigf;        // first big bin of this pass
     // Every split fixes at least one more key bit and nodes with at most
     // kDenseBits free bits are final, so the levels end within 2k - kDenseBits
     // splits (a proxy level fixes no bit, but follows a split of its own); the
@@ -891,39 +894,43 @@ int Engine::count_device(const uint8_t* d_text, uint64_t nbytes, const dk_input_
       }
       levels.emplace_back(lo, hi);
       {
-        // the final list can grow by at most this level's node count
-        DevBuf& f = finals;
-        const size_t need = ((size_t)n_final + (hi - lo)) * 4;
-        if (f.cap < need) {
-          DevBuf nb;
-          DK_TRY(Arena::ensure(this, nb, need));
-          if (n_final)
-            DK_CUDA(cudaMemcpyAsync(nb.p, f.p, (size_t)n_final * 4, cudaMemcpyDeviceToDevice, stream));
-          Arena::release(this, f);
-          f = nb;
+        // each final list can grow by at most this level's node count
+        for (auto fl : {std::make_pair(&finals, n_final), std::make_pair(&bigs, n_bigf)}) {
+          DevBuf& f = *fl.first;
+          const size_t need = ((size_t)fl.second + (hi - lo)) * 4;
+          if (f.cap < need) {
+            DevBuf nb;
+            DK_TRY(Arena::ensure(this, nb, need));
+            if (fl.second)
+              DK_CUDA(cudaMemcpyAsync(nb.p, f.p, (size_t)fl.second * 4, cudaMemcpyDeviceToDevice,
+                                      stream));
+            Arena::release(this, f);
+            f = nb;
+          }
         }
       }
       LevelCounters lv;
-      DK_CUDA(cudaMemsetAsync((char*)lc + 4, 0, sizeof(LevelCounters) - 4, stream));  // keep n_final
-      TIMED(7, launch_classify((Node*)nodes.p, lo, hi, (uint32_t*)finals.p, lc, kBinCap,
-                               2 * bin_target, big_ok, stream));
+      // keep n_final and n_big_final
+      DK_CUDA(cudaMemsetAsync((char*)lc + 8, 0, sizeof(LevelCounters) - 8, stream));
+      TIMED(7, launch_classify((Node*)nodes.p, lo, hi, (uint32_t*)finals.p, (uint32_t*)bigs.p, lc,
+                               kBinCap, 2 * bin_target, big_ok, stream));
       DK_TRY(sync_read(lc, sizeof(LevelCounters), &lv));
       if (lv.too_big) {
         set_error("a partition node holds >= 2^32 keys");
         return DK_ERR_INVALID_ARG;
       }
       n_final = lv.n_final;
-      pass_big += lv.n_big;
+      n_bigf = lv.n_big_final;
       if (lv.n_split == 0) {
         // this pass's levels are done: count its final nodes
         if (grp == 0 && fin_lo == fin_g) DK_CUDA(cudaEventRecord(ev_stage[3], stream));
         DK_CUDA(cudaMemsetAsync(c64 + 4, 0, 8, stream));  // bin ticket
-        TIMED(4, launch_bin_count((Node*)nodes.p, (uint32_t*)finals.p + fin_lo, n_final - fin_lo,
+        TIMED(4, launch_bin_count((Node*)nodes.p, (uint32_t*)bigs.p + big_lo, n_bigf - big_lo,
+                                  (uint32_t*)finals.p + fin_lo, n_final - fin_lo,
                                   (uint64_t*)keysA.p, (uint64_t*)keysB.p, (uint32_t*)cnt.p,
                                   use_hash ? 1 : 0, c64, sm_count, stream));
         DK_CUDA(cudaEventRecord(ev_stage[4], stream));
-        if (!big_ok || pass_big == 0) break;  // only big bins can ask for a retry
-        pass_big = 0;
+        if (!big_ok || n_bigf == big_lo) break;  // only big bins can ask for a retry
         uint64_t retry = 0;
         DK_TRY(sync_read(c64 + 7, 8, &retry));
         if (retry == 0) break;
@@ -939,9 +946,10 @@ int Engine::count_device(const uint8_t* d_text, uint64_t nbytes, const dk_input_
         }
         DK_CUDA(cudaMemsetAsync(c64 + 7, 0, 8, stream));
         DK_CUDA(cudaMemsetAsync(c64 + 16, 0, 8, stream));  // proxy counter
-        TIMED(7, launch_make_proxies((Node*)nodes.p, (uint32_t*)finals.p + fin_lo, n_final - fin_lo,
+        TIMED(7, launch_make_proxies((Node*)nodes.p, (uint32_t*)bigs.p + big_lo, n_bigf - big_lo,
                                      node_end, (unsigned int*)(c64 + 16), stream));
         fin_lo = n_final;
+        big_lo = n_bigf;
         lo = node_end;
         hi = node_end + (uint32_t)retry;
         node_end = hi;
@@ -983,6 +991,9 @@ int Engine::count_device(const uint8_t* d_text, uint64_t nbytes, const dk_input_
     TIMED(5, launch_compact((Node*)nodes.p, (uint32_t*)finals.p + fin_g, n_final - fin_g,
                             (uint64_t*)keysA.p, (uint64_t*)keysB.p, (uint32_t*)cnt.p, out_k, out_c,
                             stream));
+    TIMED(5, launch_compact((Node*)nodes.p, (uint32_t*)bigs.p + big_g, n_bigf - big_g,
+                            (uint64_t*)keysA.p, (uint64_t*)keysB.p, (uint32_t*)cnt.p, out_k, out_c,
+                            stream));
     DK_CUDA(cudaGetLastError());
     keys_done += group_keys[grp];
     if (out_sink) {
@@ -992,7 +1003,7 @@ int Engine::count_device(const uint8_t* d_text, uint64_t nbytes, const dk_input_
       distinct_done = total;
     }
   }
-  stats.n_bins = n_final - (uint32_t)stats.n_bins_retried;
+  stats.n_bins = n_final + n_bigf - (uint32_t)stats.n_bins_retried;
   stats.n_groups = group_at.size() - 1;
   uint64_t tail[16];
   DK_TRY(sync_read(c64 + 2, 128, tail));

@@ -42,22 +42,22 @@ struct Tile {  // a slice of a split node's keys, partitioned by one CTA
 };
 static_assert(sizeof(Tile) == 32, "Tile layout");
 
-// counters written by the classify / assign kernels.  n_final accumulates over
-// all levels; the others are per level (zeroed from byte 4 on).
+// counters written by the classify / assign kernels.  n_final and n_big_final
+// accumulate over all levels; the others are per level (zeroed from byte 8 on).
 struct LevelCounters {
-  uint32_t n_final;
+  uint32_t n_final;      // entries of the final list
+  uint32_t n_big_final;  // entries of the big-bin list (final nodes larger than a bin)
   uint32_t n_split;
   uint32_t n_tiles;
   uint32_t too_big;      // a split node holds >= 2^32 keys
   uint32_t n_children;   // sum of 2^width over split nodes
   uint32_t max_width;
+  uint32_t pad;
   unsigned long long split_keys;  // keys held by this level's split nodes
   unsigned long long th_entries;  // sum of ntiles * 2^width
   uint32_t n_tiles_assigned;
   uint32_t n_children_assigned;
   unsigned long long th_assigned;
-  uint32_t n_big;  // final nodes larger than a bin (big hash bins) at this level
-  uint32_t pad;
 };
 static_assert(sizeof(LevelCounters) == 64, "LevelCounters is read back as 64 bytes");
 
@@ -119,8 +119,11 @@ int launch_l1_scatter(const ExtractArgs& a, int grid, const uint64_t* O, uint64_
 // split nodes get a digit width that makes their children ~split_target/2 keys
 // big_ok: a skewed node (it kept most of its parent's keys: a hot k-mer) larger
 // than a bin becomes a final hash bin instead of splitting again
+// (big bins go to big_list: the bin count takes them first, so that one
+// CTA's long pass over a hot k-mer overlaps the other bins)
 int launch_classify(Node* nodes, uint32_t node_lo, uint32_t node_hi, uint32_t* final_list,
-                    LevelCounters* ctr, int bin_cap, int split_target, int big_ok, cudaStream_t s);
+                    uint32_t* big_list, LevelCounters* ctr, int bin_cap, int split_target,
+                    int big_ok, cudaStream_t s);
 // for each NODE_RETRY node of the final list: a proxy copy at n_nodes + i (i
 // from *count), the node itself becomes a split node of width 0 over its proxy
 int launch_make_proxies(Node* nodes, const uint32_t* final_list, uint32_t n_final,
@@ -137,8 +140,10 @@ int launch_tile_scatter(const Node* nodes, const Tile* tiles, uint32_t n_tiles, 
 // back to sorting, [7] = big skewed bins that must be re-partitioned (NODE_RETRY),
 // [17] = big skewed bins counted (all zeroed by the caller); use_hash selects
 // the hash-first bin count
-int launch_bin_count(Node* nodes, const uint32_t* final_list, uint32_t n_final, uint64_t* A,
-                     uint64_t* B, uint32_t* C, int use_hash, unsigned long long* ctr, int sm_count,
+// bins: big_list[0, n_big) first, then final_list[0, n_final)
+int launch_bin_count(Node* nodes, const uint32_t* big_list, uint32_t n_big,
+                     const uint32_t* final_list, uint32_t n_final, uint64_t* A, uint64_t* B,
+                     uint32_t* C, int use_hash, unsigned long long* ctr, int sm_count,
                      cudaStream_t s);
 int launch_aggregate(Node* nodes, uint32_t node_lo, uint32_t node_hi, cudaStream_t s);
 // level-1 nodes [b0, b1) follow the *total_d distinct keys before them

@@ -746,7 +746,8 @@ __device__ __forceinline__ uint32_t rank_in_digit(uint32_t* ctr, uint32_t v, boo
 // Mark each node of the level final / split / empty; count what the split
 // nodes need (children, tiles, histogram entries).
 __global__ void k_classify(Node* nodes, uint32_t lo, uint32_t hi, uint32_t* final_list,
-                           LevelCounters* ctr, int bin_cap, int split_target, int big_ok) {
+                           uint32_t* big_list, LevelCounters* ctr, int bin_cap, int split_target,
+                           int big_ok) {
   const uint32_t i = lo + blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= hi) return;
   const Node nd = nodes[i];
@@ -761,8 +762,10 @@ __global__ void k_classify(Node* nodes, uint32_t lo, uint32_t hi, uint32_t* fina
   if (nd.n <= (uint64_t)bin_cap || nd.shift <= kDenseBits ||
       (big_ok && nd.skewed && nd.n < (1ull << 31))) {
     nodes[i].state = NODE_FINAL;
-    final_list[atomicAdd(&ctr->n_final, 1u)] = i;
-    if (nd.n > (uint64_t)bin_cap && nd.shift > kDenseBits) atomicAdd(&ctr->n_big, 1u);
+    if (nd.n > (uint64_t)bin_cap && nd.shift > kDenseBits)
+      big_list[atomicAdd(&ctr->n_big_final, 1u)] = i;
+    else
+      final_list[atomicAdd(&ctr->n_final, 1u)] = i;
     return;
   }
   const uint64_t target = (uint64_t)max(1, split_target / 2);  // children ~ target keys
@@ -1561,9 +1564,16 @@ __device__ bool bin_hashed(Node* nodes, uint32_t ni, const Node& nd, uint64_t* k
 
 // Persistent bin counter: CTAs take final nodes from a ticket until none are
 // left.  Two CTAs fit per SM (96 KB keys + 16 KB histogram each).
+__device__ __forceinline__ uint32_t bin_at(const uint32_t* big, uint32_t n_big,
+                                           const uint32_t* finals, uint32_t b) {
+  return b < n_big ? big[b] : finals[b - n_big];
+}
+
 __global__ void __launch_bounds__(kBinThreads, kBinBlocksPerSM) k_bin_count(Node* nodes,
+                                                              const uint32_t* __restrict__ bigs,
+                                                              uint32_t n_big,
                                                               const uint32_t* __restrict__ finals,
-                                                              uint32_t n_final, uint64_t* A,
+                                                              uint32_t n_bins, uint64_t* A,
                                                               uint64_t* B, uint32_t* C,
                                                               unsigned long long* ctr,
                                                               int use_hash) {
@@ -1579,8 +1589,8 @@ __global__ void __launch_bounds__(kBinThreads, kBinBlocksPerSM) k_bin_count(Node
   __syncthreads();
   for (;;) {
     const uint32_t b = s_bin;
-    if (b >= n_final) break;
-    const uint32_t ni = finals[b];
+    if (b >= n_bins) break;
+    const uint32_t ni = bin_at(bigs, n_big, finals, b);
     const Node nd = nodes[ni];
     uint64_t* keys = (nd.buf ? B : A) + nd.start;
     uint32_t* cnt = C + nd.start;
@@ -1589,8 +1599,8 @@ __global__ void __launch_bounds__(kBinThreads, kBinBlocksPerSM) k_bin_count(Node
       // take the next bin now and start pulling its keys into L2 while this one runs
       const uint32_t nb = atomicAdd(reinterpret_cast<unsigned int*>(&ctr[4]), 1u);
       s_bin = nb;
-      if (nb < n_final) {
-        const Node& nx = nodes[finals[nb]];
+      if (nb < n_bins) {
+        const Node& nx = nodes[bin_at(bigs, n_big, finals, nb)];
         prefetch_l2_range((nx.buf ? B : A) + nx.start, nx.n * 8);
       }
     }
@@ -1914,10 +1924,11 @@ int launch_l1_scatter(const ExtractArgs& a, int grid, const uint64_t* O, uint64_
 }
 
 int launch_classify(Node* nodes, uint32_t lo, uint32_t hi, uint32_t* final_list,
-                    LevelCounters* ctr, int bin_cap, int split_target, int big_ok, cudaStream_t s) {
+                    uint32_t* big_list, LevelCounters* ctr, int bin_cap, int split_target,
+                    int big_ok, cudaStream_t s) {
   const uint32_t n = hi - lo;
   if (!n) return 0;
-  k_classify<<<(n + 255) / 256, 256, 0, s>>>(nodes, lo, hi, final_list, ctr, bin_cap,
+  k_classify<<<(n + 255) / 256, 256, 0, s>>>(nodes, lo, hi, final_list, big_list, ctr, bin_cap,
                                             split_target, big_ok);
   return 1;
 }
@@ -1964,14 +1975,16 @@ int launch_tile_scatter(const Node* nodes, const Tile* tiles, uint32_t n_tiles, 
 
 int bin_count_smem_bytes(int) { return kBinCap * 8; }
 
-int launch_bin_count(Node* nodes, const uint32_t* final_list, uint32_t n_final, uint64_t* A,
-                     uint64_t* B, uint32_t* C, int use_hash, unsigned long long* ctr, int sm_count,
+int launch_bin_count(Node* nodes, const uint32_t* big_list, uint32_t n_big,
+                     const uint32_t* final_list, uint32_t n_final, uint64_t* A, uint64_t* B,
+                     uint32_t* C, int use_hash, unsigned long long* ctr, int sm_count,
                      cudaStream_t s) {
-  if (!n_final) return 0;
+  const uint32_t n_bins = n_big + n_final;
+  if (!n_bins) return 0;
   allow_max_smem(k_bin_count);
-  const uint32_t grid = std::min<uint32_t>(n_final, (uint32_t)(kBinBlocksPerSM * sm_count));
-  k_bin_count<<<grid, kBinThreads, kBinCap * 8, s>>>(nodes, final_list, n_final, A, B, C, ctr,
-                                                     use_hash);
+  const uint32_t grid = std::min<uint32_t>(n_bins, (uint32_t)(kBinBlocksPerSM * sm_count));
+  k_bin_count<<<grid, kBinThreads, kBinCap * 8, s>>>(nodes, big_list, n_big, final_list, n_bins,
+                                                     A, B, C, ctr, use_hash);
   return 1;
 }
 
