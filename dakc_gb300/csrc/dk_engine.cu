@@ -30,6 +30,9 @@ namespace dk {
 // runs, in this many groups of level-1 buckets
 constexpr uint64_t kStreamMinKmers = 64ull << 20;
 constexpr int kStreamGroups = 16;
+// page-locked reads of at least this many bytes upload in chunks, each
+// counted as soon as it lands
+constexpr uint64_t kChunkMinBytes = 64ull << 20;
 
 // --------------------------------------------------------------- helpers
 static int ceil_log2(uint64_t x) {
@@ -172,6 +175,8 @@ Engine::~Engine() {
     if (ev) cudaEventDestroy(ev);
   if (ev_h2d0) cudaEventDestroy(ev_h2d0);
   if (ev_d2h1) cudaEventDestroy(ev_d2h1);
+  for (auto& ev : chunks.ev)
+    if (ev) cudaEventDestroy(ev);
   if (h_scratch) cudaFreeHost(h_scratch);
   if (h_up) cudaFreeHost(h_up);
   for (auto& s : stage_pinned)
@@ -743,6 +748,8 @@ int Engine::count_device(const uint8_t* d_text, uint64_t nbytes, const dk_input_
   launches = 0;
   kev.clear();
   kev_next = 0;
+  // with a chunked upload the device time starts when the first chunk has landed
+  if (chunks.n > 1) DK_CUDA(cudaStreamWaitEvent(stream, chunks.ev[0], 0));
   DK_CUDA(cudaEventRecord(ev_stage[0], stream));
   const uint64_t per_line = (W >= k) ? (uint64_t)(W - k + 1) : 0;
   if (L == 0 || per_line == 0) {
@@ -783,9 +790,26 @@ int Engine::count_device(const uint8_t* d_text, uint64_t nbytes, const dk_input_
   a.job_nul = js ? js->d_nul : nullptr;
   a.job_base = js ? js->d_base : nullptr;
   a.job_bits = js ? js->d_bits : nullptr;
+  a.line_base = 0;
+  a.lines_total = (uint64_t)L0;
 
-  DK_TRY(Arena::ensure(this, H, (size_t)G * F1 * 4));
-  DK_TRY(Arena::ensure(this, O, (size_t)G * F1 * 8));
+  // chunked: one level-1 count (and later one scatter) per uploaded chunk;
+  // their per-CTA rows follow one another in H and O
+  bool chunked = !js && chunks.n > 1 && W <= kLineMaxW && chunks.lines[chunks.n] == L;
+  const int NC = chunked ? chunks.n : 1;
+  auto chunk_args = [&](int c) {
+    ExtractArgs ac = a;
+    const uint64_t stride = (uint64_t)W + 1;
+    const uint64_t l0 = chunks.lines[c], l1 = chunks.lines[c + 1];
+    ac.text = d_text + l0 * stride;
+    ac.nbytes = std::min<uint64_t>(nbytes, l1 * stride) - l0 * stride;
+    ac.n_lines = l1 - l0;
+    ac.line_base = l0;
+    ac.lines_total = L;
+    return ac;
+  };
+  DK_TRY(Arena::ensure(this, H, (size_t)NC * G * F1 * 4));
+  DK_TRY(Arena::ensure(this, O, (size_t)NC * G * F1 * 8));
   DK_TRY(Arena::ensure(this, ctrs, 256));
   // device counters: [0] k-mers, [1] NUL-led line marker, [2] distinct total,
   // [3] device error (a bounded wait ran out), [4] bin ticket, [5] count overflow,
@@ -797,15 +821,25 @@ int Engine::count_device(const uint8_t* d_text, uint64_t nbytes, const dk_input_
   uint64_t n_kmers = 0;
   for (int attempt = 0; attempt < 2; ++attempt) {
     a.n_lines = L;
+    a.lines_total = L;
     DK_CUDA(cudaMemsetAsync(ctrs.p, 0, 256, stream));
     if (js) DK_TRY(js->upload_bounds(this));
-    TIMED(0, launch_l1_count(a, G, (uint32_t*)H.p, c64, stream));
+    if (chunked) {
+      for (int c = 0; c < NC; ++c) {
+        DK_CUDA(cudaStreamWaitEvent(stream, chunks.ev[c], 0));
+        TIMED(0, launch_l1_count(chunk_args(c), G, (uint32_t*)H.p + (size_t)c * G * F1, c64, stream));
+      }
+    } else {
+      if (chunks.n > 1) DK_CUDA(cudaStreamWaitEvent(stream, chunks.ev[chunks.n - 1], 0));
+      TIMED(0, launch_l1_count(a, G, (uint32_t*)H.p, c64, stream));
+    }
     uint64_t hc[2];
     DK_TRY(sync_read(c64, 16, hc));
     if (hc[1] == 0) {
       n_kmers = hc[0];
       break;
     }
+    chunked = false;  // a NUL-led line: recount the shortened read set in one pass
     if (js) {
       DK_TRY(js->apply_nul(this));  // each job stops before its first NUL-led line
     } else {
@@ -826,12 +860,18 @@ int Engine::count_device(const uint8_t* d_text, uint64_t nbytes, const dk_input_
   // level-1 nodes and offsets
   node_cap_needed = (size_t)F1;
   DK_TRY(Arena::ensure(this, nodes, node_cap_needed * sizeof(Node)));
-  TIMED(7, launch_l1_scan((uint32_t*)H.p, G, F1, (uint64_t*)O.p, (Node*)nodes.p, shift1,
-                          js ? js->d_bshift : nullptr, stream));
+  TIMED(7, launch_l1_scan((uint32_t*)H.p, (chunked ? NC : 1) * G, F1, (uint64_t*)O.p,
+                          (Node*)nodes.p, shift1, js ? js->d_bshift : nullptr, stream));
   DK_TRY(Arena::ensure(this, keysA, n_kmers * 8));
   DK_TRY(Arena::ensure(this, keysB, n_kmers * 8));
   DK_TRY(Arena::ensure(this, cnt, n_kmers * 4));
-  TIMED(1, launch_l1_scatter(a, G, (const uint64_t*)O.p, (uint64_t*)keysA.p, c64, stream));
+  if (chunked) {
+    for (int c = 0; c < NC; ++c)
+      TIMED(1, launch_l1_scatter(chunk_args(c), G, (const uint64_t*)O.p + (size_t)c * G * F1,
+                                 (uint64_t*)keysA.p, c64, stream));
+  } else {
+    TIMED(1, launch_l1_scatter(a, G, (const uint64_t*)O.p, (uint64_t*)keysA.p, c64, stream));
+  }
   DK_CUDA(cudaEventRecord(ev_stage[2], stream));
 
   if (!out_k || !out_c) {
@@ -1180,9 +1220,40 @@ int Engine::count_locked(const char* text, uint64_t nbytes, bool text_on_device,
   if (!text_on_device) {
     DK_TRY(Arena::ensure(this, this->text, nbytes + 64));
     DK_CUDA(cudaEventRecord(ev_h2d0, stream));
-    if (nbytes) DK_TRY(upload(text, nbytes, (uint8_t*)this->text.p));
+    const int W = desc->line_width;
+    const int64_t Lc = frame_lines(nbytes, W);
+    if (nbytes >= kChunkMinBytes && W <= kLineMaxW && Lc >= 64 * kMaxChunks && is_pinned(text)) {
+      // chunks of lines on s_in (after earlier work on the text buffer); the
+      // level-1 count of each runs as soon as it has landed
+      DK_CUDA(cudaStreamWaitEvent(s_in, ev_h2d0, 0));
+      chunks.n = kMaxChunks;
+      const uint64_t stride = (uint64_t)W + 1;
+      for (int c = 0; c <= kMaxChunks; ++c) chunks.lines[c] = (uint64_t)Lc * c / kMaxChunks;
+      for (int c = 0; c < kMaxChunks; ++c) {
+        if (!chunks.ev[c]) DK_CUDA(cudaEventCreate(&chunks.ev[c]));
+        const uint64_t b0 = chunks.lines[c] * stride;
+        const uint64_t b1 = c + 1 == kMaxChunks ? nbytes : chunks.lines[c + 1] * stride;
+        if (b1 > b0)
+          DK_CUDA(cudaMemcpyAsync((uint8_t*)this->text.p + b0, text + b0, b1 - b0,
+                                  cudaMemcpyHostToDevice, s_in));
+        DK_CUDA(cudaEventRecord(chunks.ev[c], s_in));
+      }
+    } else if (nbytes) {
+      DK_TRY(upload(text, nbytes, (uint8_t*)this->text.p));
+    }
     d_text = (const uint8_t*)this->text.p;
   }
+  // whatever way this call returns, no chunk copy is left in flight and the
+  // next count does not see this call's chunks
+  struct ChunkGuard {
+    Engine* e;
+    ~ChunkGuard() {
+      if (e->chunks.n > 0) {
+        cudaStreamSynchronize(e->s_in);
+        e->chunks.n = 0;
+      }
+    }
+  } chunk_guard{this};
   // output buffers sized by an upper bound of distinct k-mers (<= occurrences)
   const int64_t L = frame_lines(nbytes, desc->line_width);
   const uint64_t per_line = desc->line_width >= desc->k ? (uint64_t)(desc->line_width - desc->k + 1) : 0;
@@ -1232,6 +1303,10 @@ int Engine::count_locked(const char* text, uint64_t nbytes, bool text_on_device,
   int rc = count_device(d_text, nbytes, *desc, &dt);
   out_sink = nullptr;
   out_groups = 1;
+  const bool chunked_up = chunks.n > 1;
+  if (chunked_up && rc != DK_OK) cudaStreamSynchronize(s_in);  // no copy left in flight
+  chunks.n = 0;
+  stats.upload_chunks = chunked_up ? (uint64_t)kMaxChunks : 0;
   if (h_tb && (rc != DK_OK || !streaming || streamed != dt.n)) {
     // copies into it may still run
     cudaStreamSynchronize(s_out);
@@ -1243,7 +1318,7 @@ int Engine::count_locked(const char* text, uint64_t nbytes, bool text_on_device,
     return rc;
   }
   if (!text_on_device) {
-    cudaEventElapsedTime(&ms_h2d, ev_h2d0, ev_stage[0]);
+    cudaEventElapsedTime(&ms_h2d, ev_h2d0, chunked_up ? chunks.ev[kMaxChunks - 1] : ev_stage[0]);
     stats.ms_h2d = ms_h2d;
   }
   out->n = dt.n;

@@ -185,6 +185,17 @@ struct Engine {
   // the next group runs while the sink moves that slice.
   std::function<int(uint64_t, uint64_t, uint64_t, uint64_t)> out_sink;
   int out_groups = 1;
+  // Reads uploaded in chunks of lines on s_in (count_locked): chunk c holds
+  // lines [lines[c], lines[c+1]) and has landed when ev[c] completes.  When
+  // set, count_device counts each chunk as it lands and scatters chunk by
+  // chunk with the same lines per CTA.
+  static constexpr int kMaxChunks = 8;
+  struct ChunkPlan {
+    int n = 0;
+    uint64_t lines[kMaxChunks + 1] = {};
+    cudaEvent_t ev[kMaxChunks] = {};
+  };
+  ChunkPlan chunks;
   int count_batch(const dk_job* jobs, int njobs, const dk_input_desc* desc, dk_table* outs);
   DevBuf jobmeta;  // device job_start / job_end / job_nul
   int count(const char* text, uint64_t nbytes, bool text_on_device, const dk_input_desc* desc,

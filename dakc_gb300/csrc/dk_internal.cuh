@@ -77,9 +77,14 @@ constexpr int kLineMaxW = 256;           // longer lines use the warp-per-line k
 constexpr int kLineChunk = 16;           // positions per line in one chunked-scatter chunk
 
 struct ExtractArgs {
-  const uint8_t* text;  // device text, 16-byte aligned
+  const uint8_t* text;  // device text (the line kernels take any alignment)
   uint64_t nbytes;      // readable bytes at text
   uint64_t n_lines;
+  // the lines at text are lines [line_base, line_base + n_lines) of a read
+  // set of lines_total lines (a chunk counted while later chunks upload);
+  // the NUL-led-line rule uses the read set's line numbers
+  uint64_t line_base;
+  uint64_t lines_total;
   int W;
   int k;
   uint64_t kmask;

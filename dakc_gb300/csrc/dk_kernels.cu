@@ -225,7 +225,8 @@ __global__ void __launch_bounds__(512) k_l1_count(ExtractArgs a, uint32_t* __res
         });
         continue;
       }
-      if (lane_id() == 0 && l > 0 && line[0] == 0) atomicMax(&counters[1], a.n_lines - l);
+      if (lane_id() == 0 && a.line_base + l > 0 && line[0] == 0)
+        atomicMax(&counters[1], a.lines_total - (a.line_base + l));
       warp_line_kmers<C>(line, a.W, a.k, a.kmask, lut, [&](int, uint64_t key, bool valid) {
         if (valid) { atomicAdd(&hist[key >> a.shift1], 1u); ++mine; }
       });
@@ -343,8 +344,8 @@ __device__ __forceinline__ bool line_prologue(const ExtractArgs& a, uint64_t l, 
       atomicMax(&counters[1], 1ull);
     }
     *jb = JobBucket(a, job);
-  } else if (l > 0 && line[0] == 0) {
-    atomicMax(&counters[1], a.n_lines - l);
+  } else if (a.line_base + l > 0 && line[0] == 0) {
+    atomicMax(&counters[1], a.lines_total - (a.line_base + l));
   }
   return true;
 }

@@ -142,6 +142,8 @@ typedef struct {
   uint64_t n_groups;        /* groups of level-1 buckets counted one after another */
   uint64_t table_streamed;  /* 1: the host table was copied out group by group
                                while the count ran; 0: after it               */
+  uint64_t upload_chunks;   /* chunks the reads were uploaded in, each counted as
+                               it landed (0: one upload before the count)     */
 } dk_stats;
 
 /* One read set of a batch (dk_count_batch). */

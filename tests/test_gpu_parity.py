@@ -281,3 +281,34 @@ def test_streamed_table_size_estimate_too_small(variant):
         check(e, lines.reshape(-1), W, 31, variant)
         st = e.stats()
     assert st["n_groups"] >= 2 and st["table_streamed"] == 0
+
+
+def _reads_68mb(seed):
+    g = synth.genome_uniform(seed, 2_000_000)
+    return synth.reads(seed + 1, g, 450_000, 150, 150, 150, rc_frac=0.5, err_rate=0.01)
+
+
+@pytest.mark.parametrize("nul_line", [None, 200_001])
+def test_chunked_upload_equals_single_upload(engine, nul_line):
+    """Page-locked reads of 64 MB or more upload in chunks of lines, each
+    counted as soon as it lands.  The table equals the one counted from the
+    same bytes in pageable memory (uploaded whole), also when a NUL-led line
+    in the middle of a chunk ends the read set there."""
+    text = _reads_68mb(81)
+    if nul_line is not None:
+        text[nul_line * 151] = 0
+    pin = dk.PinnedBuffer(text.size)
+    try:
+        pin.array[:] = text
+        a = engine.count(pin.array, 150, 31, dk.VARIANT_HASH)
+        chunks = engine.stats()["upload_chunks"]
+        b = engine.count(text, 150, 31, dk.VARIANT_HASH)
+        assert engine.stats()["upload_chunks"] == 0
+    finally:
+        pin.free()
+    assert chunks >= 2
+    assert a.n_kmers == b.n_kmers and np.array_equal(a.kmers, b.kmers)
+    assert np.array_equal(a.counts, b.counts)
+    assert int(a.counts.sum(dtype=np.uint64)) == a.n_kmers
+    if nul_line is not None:
+        assert a.n_kmers == nul_line * 120
