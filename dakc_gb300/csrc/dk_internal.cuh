@@ -73,6 +73,8 @@ constexpr int kBinDigitBits = 12;       // counting-sort digit of a bin: at most
 constexpr int kMaxL1Bits = 12;          // level-1 fan-out <= 4096 buckets
 constexpr size_t kMaxSmemPerBlock = 232448;  // opt-in shared memory per block (sm_100 family)
 constexpr int kLineThreads = 256;        // thread-per-line level-1 kernels: lines per tile
+constexpr int kCountThreads = 512;       // ... except the count (one buffer of 512 lines); a
+                                         // CTA's lines do not depend on its tile size
 constexpr int kLineMaxW = 256;           // longer lines use the warp-per-line kernels
 constexpr int kLineChunk = 16;           // positions per line in one chunked-scatter chunk
 

@@ -369,18 +369,19 @@ __device__ __forceinline__ void setup_tiles(TextTiles* T, const ExtractArgs& a, 
 
 // COUNT: per-CTA bucket histogram H[cta][bucket] and the k-mer total.
 template <bool PAK>
-__global__ void __launch_bounds__(kLineThreads) k_l1_lines_count(ExtractArgs a,
+__global__ void __launch_bounds__(kCountThreads) k_l1_lines_count(ExtractArgs a,
                                                                  uint32_t* __restrict__ H,
                                                                  unsigned long long* __restrict__ counters) {
   extern __shared__ __align__(128) uint8_t smraw[];
   const int W = a.W, k = a.k;
   const uint64_t stride = (uint64_t)W + 1;
   const uint32_t bb = tile_buf_bytes(blockDim.x, stride);
-  uint32_t* cnt = reinterpret_cast<uint32_t*>(smraw + 128 + 2 * bb);  // F1
+  uint32_t* cnt = reinterpret_cast<uint32_t*>(smraw + 128 + bb);  // F1
   uint8_t* lut = reinterpret_cast<uint8_t*>(cnt + a.F1);              // 256
   __shared__ uint32_t s_jobs[2];
   TextTiles T;
   setup_tiles(&T, a, smraw, bb);
+  T.buf1 = T.buf0;  // one buffer: tile t+1 is fetched once tile t is done
   for (int b = threadIdx.x; b < a.F1; b += blockDim.x) cnt[b] = 0;
   init_lut(lut, a.conv);
   __syncthreads();
@@ -388,12 +389,8 @@ __global__ void __launch_bounds__(kLineThreads) k_l1_lines_count(ExtractArgs a,
   const uint32_t nt = T.ntiles();
   if (threadIdx.x == 0 && nt) T.issue(0);
   for (uint32_t ti = 0; ti < nt; ++ti) {
-    if (threadIdx.x == 0 && ti + 1 < nt) T.issue(ti + 1);
     const uint8_t* tile = T.acquire(ti, &counters[3]);
-    if (!tile) {
-      T.drain(ti + 1);
-      return;
-    }
+    if (!tile) return;  // nothing else is in flight into this CTA's shared memory
     uint64_t l0, l1;
     T.range(ti, &l0, &l1);
     tile_jobs(a, l0, l1, s_jobs);
@@ -415,7 +412,11 @@ __global__ void __launch_bounds__(kLineThreads) k_l1_lines_count(ExtractArgs a,
           }
       }
     }
-    __syncthreads();  // the buffer is refilled two tiles on
+    // every thread's generic accesses of the buffer are ordered before the
+    // bulk copy that refills it (one buffer: more CTAs per SM hide the wait)
+    fence_barrier_init();
+    __syncthreads();
+    if (threadIdx.x == 0 && ti + 1 < nt) T.issue(ti + 1);
   }
 #pragma unroll
   for (int o = 16; o; o >>= 1) mine += __shfl_xor_sync(0xFFFFFFFFu, mine, o);
@@ -1809,6 +1810,11 @@ static size_t lines_smem(const ExtractArgs& a, bool scatter) {
          (size_t)a.F1 * (scatter ? 12 : 4) + 256;
 }
 
+// the count kernel keeps one tile buffer of kCountThreads lines
+static size_t count_lines_smem(const ExtractArgs& a) {
+  return 128 + (size_t)tile_buf_bytes(kCountThreads, (uint64_t)a.W + 1) + (size_t)a.F1 * 4 + 256;
+}
+
 // batch waves (jobs) with lines the thread-per-line kernels take scatter
 // directly; plain counts stage their tiles (k_l1_scatter)
 static bool direct_scatter(int W, bool jobs) { return jobs && W <= kLineMaxW; }
@@ -1834,7 +1840,7 @@ int launch_l1_count(const ExtractArgs& a, int grid, uint32_t* H, unsigned long l
   if (a.W <= kLineMaxW) {
     auto* kern = a.conv == 1 ? k_l1_lines_count<true> : k_l1_lines_count<false>;
     allow_max_smem(kern);
-    kern<<<grid, kLineThreads, lines_smem(a, false), s>>>(a, H, counters);
+    kern<<<grid, kCountThreads, count_lines_smem(a), s>>>(a, H, counters);
     return 1;
   }
   switch (choose_c(a.W)) {
