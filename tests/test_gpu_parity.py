@@ -312,3 +312,56 @@ def test_chunked_upload_equals_single_upload(engine, nul_line):
     assert int(a.counts.sum(dtype=np.uint64)) == a.n_kmers
     if nul_line is not None:
         assert a.n_kmers == nul_line * 120
+
+
+def _count_conv(engine, text, W, k, conv, variant):
+    d = dk.Engine.desc(W, k, variant)
+    d.convention = conv
+    ptr, n, keep = dk._buf_ptr(text)
+    t = engine.count_raw(ptr, n, d)
+    try:
+        nd = int(t.n)
+        return (np.ctypeslib.as_array(t.kmers, shape=(nd,)).copy(),
+                np.ctypeslib.as_array(t.counts, shape=(nd,)).copy(), int(t.n_kmers))
+    finally:
+        engine.free_table(t)
+
+
+@pytest.mark.parametrize("conv,variant", [(dk.CONV_PAKMAN, dk.VARIANT_HASH),
+                                          (dk.CONV_DAKC, dk.VARIANT_SORT)])
+def test_chunked_upload_other_convention_and_variant(engine, conv, variant):
+    """The chunked upload under PakMan*'s convention and under the sort
+    variant equals the single upload of the same bytes."""
+    text = _reads_68mb(82)
+    pin = dk.PinnedBuffer(text.size)
+    try:
+        pin.array[:] = text
+        a = _count_conv(engine, pin.array, 150, 31, conv, variant)
+        assert engine.stats()["upload_chunks"] >= 2
+        b = _count_conv(engine, text, 150, 31, conv, variant)
+        assert engine.stats()["upload_chunks"] == 0
+    finally:
+        pin.free()
+    assert a[2] == b[2] and np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+    assert int(a[1].sum(dtype=np.uint64)) == a[2]
+
+
+@pytest.mark.parametrize("variant", VARIANTS)
+def test_streamed_and_chunked_together(variant):
+    """A page-locked read set uploaded in chunks whose table also streams out
+    in groups equals the single-upload, single-copy count of the same bytes."""
+    text = _reads_68mb(83)
+    with dk.Engine(0, flags=dk.FLAG_STREAM_ALL) as e1, dk.Engine(0) as e2:
+        pin = dk.PinnedBuffer(text.size)
+        try:
+            pin.array[:] = text
+            a = e1.count(pin.array, 150, 31, variant)
+            st = e1.stats()
+        finally:
+            pin.free()
+        b = e2.count(text, 150, 31, variant)
+        st2 = e2.stats()
+    assert st["upload_chunks"] >= 2 and st["table_streamed"] == 1 and st["n_groups"] >= 2
+    assert st2["upload_chunks"] == 0 and st2["table_streamed"] == 0
+    assert a.n_kmers == b.n_kmers and np.array_equal(a.kmers, b.kmers)
+    assert np.array_equal(a.counts, b.counts)
