@@ -162,7 +162,7 @@ int Engine::init(const dk_config* cfg) {
 Engine::~Engine() {
   for (cudaStream_t st : {stream, s_in, s_out})
     if (st) cudaStreamSynchronize(st);
-  for (DevBuf* b : {&text, &text2, &keysA, &keysB, &cnt, &H, &O, &nodes, &tiles, &TH, &finals, &bigs, &ctrs,
+  for (DevBuf* b : {&text, &text2, &keysA, &keysB, &cnt, &H, &O, &nodes, &tiles, &TH, &finals, &bigs, &rng, &ctrs,
                     &aux})
     Arena::release(this, *b);
   for (auto& t : tables) {  // device tables (host tables live in the shared pool)
@@ -814,9 +814,30 @@ int Engine::count_device(const uint8_t* d_text, uint64_t nbytes, const dk_input_
   // device counters: [0] k-mers, [1] NUL-led line marker, [2] distinct total,
   // [3] device error (a bounded wait ran out), [4] bin ticket, [5] count overflow,
   // [6] hash bins sorted instead, [7] big bins to re-partition; LevelCounters at
-  // byte 64; [16] proxy counter, [17] big bins counted
+  // byte 64; [16] proxy counter, [17] big bins counted, [18] keys placed by the
+  // chunks scattered so far (their regions' running base)
   unsigned long long* c64 = (unsigned long long*)ctrs.p;
   LevelCounters* lc = (LevelCounters*)((char*)ctrs.p + 64);
+
+  // Chunks in their own regions: each chunk is scattered right after its
+  // count, into a region of the key buffer after the earlier chunks' keys, so
+  // the level-1 scatter overlaps the upload too.  A level-1 bucket's keys
+  // then lie in one range per chunk; the first partition level gathers them
+  // (its tiles are cut from each range; its children are single ranges).
+  // Needs the key buffer at the k-mer bound before counting, and level-1
+  // nodes that can always split (more than kDenseBits free bits).
+  bool regions = chunked && shift1 > kDenseBits;
+  if (regions) {
+    const uint64_t bound = (uint64_t)L * ((W >= k) ? (uint64_t)(W - k + 1) : 0);
+    if (budget && dev_bytes - keysA.cap + bound * 8 + (size_t)NC * F1 * 12 > budget) regions = false;
+    if (regions) {
+      DK_TRY(Arena::ensure(this, keysA, bound * 8));
+      DK_TRY(Arena::ensure(this, rng, (size_t)NC * F1 * 12));
+    }
+  }
+  uint64_t* rS = (uint64_t*)rng.p;                          // NC x F1 range starts
+  uint32_t* rT = regions ? (uint32_t*)(rS + (size_t)NC * F1) : nullptr;  // NC x F1 range sizes
+  bool scattered = false;  // the regions' scatter has run
 
   uint64_t n_kmers = 0;
   for (int attempt = 0; attempt < 2; ++attempt) {
@@ -827,8 +848,16 @@ int Engine::count_device(const uint8_t* d_text, uint64_t nbytes, const dk_input_
     if (chunked) {
       for (int c = 0; c < NC; ++c) {
         DK_CUDA(cudaStreamWaitEvent(stream, chunks.ev[c], 0));
-        TIMED(0, launch_l1_count(chunk_args(c), G, (uint32_t*)H.p + (size_t)c * G * F1, c64, stream));
+        uint32_t* Hc = (uint32_t*)H.p + (size_t)c * G * F1;
+        TIMED(0, launch_l1_count(chunk_args(c), G, Hc, c64, stream));
+        if (regions) {
+          uint64_t* Oc = (uint64_t*)O.p + (size_t)c * G * F1;
+          TIMED(7, launch_chunk_scan(Hc, G, F1, rT + (size_t)c * F1, rS + (size_t)c * F1, c64 + 18,
+                                     Oc, stream));
+          TIMED(1, launch_l1_scatter(chunk_args(c), G, Oc, (uint64_t*)keysA.p, c64, stream));
+        }
       }
+      scattered = regions;
     } else {
       if (chunks.n > 1) DK_CUDA(cudaStreamWaitEvent(stream, chunks.ev[chunks.n - 1], 0));
       TIMED(0, launch_l1_count(a, G, (uint32_t*)H.p, c64, stream));
@@ -839,7 +868,10 @@ int Engine::count_device(const uint8_t* d_text, uint64_t nbytes, const dk_input_
       n_kmers = hc[0];
       break;
     }
-    chunked = false;  // a NUL-led line: recount the shortened read set in one pass
+    // a NUL-led line: recount the shortened read set in one pass
+    chunked = false;
+    regions = false;
+    scattered = false;
     if (js) {
       DK_TRY(js->apply_nul(this));  // each job stops before its first NUL-led line
     } else {
@@ -860,12 +892,19 @@ int Engine::count_device(const uint8_t* d_text, uint64_t nbytes, const dk_input_
   // level-1 nodes and offsets
   node_cap_needed = (size_t)F1;
   DK_TRY(Arena::ensure(this, nodes, node_cap_needed * sizeof(Node)));
-  TIMED(7, launch_l1_scan((uint32_t*)H.p, (chunked ? NC : 1) * G, F1, (uint64_t*)O.p,
-                          (Node*)nodes.p, shift1, js ? js->d_bshift : nullptr, stream));
+  if (scattered) {
+    TIMED(7, launch_l1_nodes((uint32_t*)H.p, NC * G, F1, (Node*)nodes.p, shift1, stream));
+  } else {
+    TIMED(7, launch_l1_scan((uint32_t*)H.p, (chunked ? NC : 1) * G, F1, (uint64_t*)O.p,
+                            (Node*)nodes.p, shift1, js ? js->d_bshift : nullptr, stream));
+  }
+  const Ranges rg = scattered ? Ranges{rS, rT, NC, F1} : Ranges{nullptr, nullptr, 0, 0};
   DK_TRY(Arena::ensure(this, keysA, n_kmers * 8));
   DK_TRY(Arena::ensure(this, keysB, n_kmers * 8));
   DK_TRY(Arena::ensure(this, cnt, n_kmers * 4));
-  if (chunked) {
+  if (scattered) {
+    // done chunk by chunk above
+  } else if (chunked) {
     for (int c = 0; c < NC; ++c)
       TIMED(1, launch_l1_scatter(chunk_args(c), G, (const uint64_t*)O.p + (size_t)c * G * F1,
                                  (uint64_t*)keysA.p, c64, stream));
@@ -953,7 +992,7 @@ int Engine::count_device(const uint8_t* d_text, uint64_t nbytes, const dk_input_
       // keep n_final and n_big_final
       DK_CUDA(cudaMemsetAsync((char*)lc + 8, 0, sizeof(LevelCounters) - 8, stream));
       TIMED(7, launch_classify((Node*)nodes.p, lo, hi, (uint32_t*)finals.p, (uint32_t*)bigs.p, lc,
-                               kBinCap, 2 * bin_target, big_ok, stream));
+                               kBinCap, 2 * bin_target, big_ok, rg, stream));
       DK_TRY(sync_read(lc, sizeof(LevelCounters), &lv));
       if (lv.too_big) {
         set_error("a partition node holds >= 2^32 keys");
@@ -1009,7 +1048,7 @@ int Engine::count_device(const uint8_t* d_text, uint64_t nbytes, const dk_input_
       const uint32_t n_tiles = lv.n_tiles;
       DK_TRY(Arena::ensure(this, tiles, (size_t)n_tiles * sizeof(Tile)));
       DK_TRY(Arena::ensure(this, TH, (size_t)lv.th_entries * 4));
-      TIMED(7, launch_assign((Node*)nodes.p, lo, hi, node_end, (Tile*)tiles.p, lc, stream));
+      TIMED(7, launch_assign((Node*)nodes.p, lo, hi, node_end, (Tile*)tiles.p, lc, rg, stream));
       TIMED(2, launch_tile_hist((Node*)nodes.p, (Tile*)tiles.p, n_tiles, (uint64_t*)keysA.p,
                                 (uint64_t*)keysB.p, (uint32_t*)TH.p, stream));
       TIMED(7, launch_node_scan((Node*)nodes.p, lo, hi, (Tile*)tiles.p, (uint32_t*)TH.p, stream));

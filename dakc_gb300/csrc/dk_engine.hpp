@@ -116,7 +116,7 @@ struct Engine {
   uint64_t launches = 0;
 
   // device arenas
-  DevBuf text, text2, keysA, keysB, cnt, H, O, nodes, tiles, TH, finals, bigs, ctrs;
+  DevBuf text, text2, keysA, keysB, cnt, H, O, nodes, tiles, TH, finals, bigs, rng, ctrs;
   size_t node_cap_needed = 0;
   uint64_t* out_k = nullptr;
   uint32_t* out_c = nullptr;

@@ -108,6 +108,16 @@ struct ExtractArgs {
   const uint8_t* job_bits;
 };
 
+// Level-1 buckets whose keys lie in several ranges of the key buffer: one per
+// upload chunk (chunk c's keys of bucket b start at S[c * F1 + b], T[c * F1 + b]
+// of them).  C = 0: every node's keys are one range [start, start + n).
+struct Ranges {
+  const uint64_t* S;
+  const uint32_t* T;
+  int C;
+  int F1;
+};
+
 // ---- launchers (dk_kernels.cu); every launcher returns the number of kernel
 // launches it issued (for the launch count reported in stats)
 int launch_l1_count(const ExtractArgs& a, int grid, uint32_t* H, unsigned long long* n_kmers,
@@ -128,15 +138,24 @@ int launch_l1_scatter(const ExtractArgs& a, int grid, const uint64_t* O, uint64_
 // than a bin becomes a final hash bin instead of splitting again
 // (big bins go to big_list: the bin count takes them first, so that one
 // CTA's long pass over a hot k-mer overlaps the other bins)
+// (level-1 nodes of several ranges always split: a final bin's keys are one range)
 int launch_classify(Node* nodes, uint32_t node_lo, uint32_t node_hi, uint32_t* final_list,
                     uint32_t* big_list, LevelCounters* ctr, int bin_cap, int split_target,
-                    int big_ok, cudaStream_t s);
+                    int big_ok, const Ranges& rg, cudaStream_t s);
 // for each NODE_RETRY node of the final list: a proxy copy at n_nodes + i (i
 // from *count), the node itself becomes a split node of width 0 over its proxy
 int launch_make_proxies(Node* nodes, const uint32_t* final_list, uint32_t n_final,
                         uint32_t n_nodes, unsigned int* count, cudaStream_t s);
 int launch_assign(Node* nodes, uint32_t node_lo, uint32_t node_hi, uint32_t child_base,
-                  Tile* tiles, LevelCounters* ctr, cudaStream_t s);
+                  Tile* tiles, LevelCounters* ctr, const Ranges& rg, cudaStream_t s);
+// one upload chunk's level-1 layout: its rows H_c (G x F1) give its bucket
+// totals T_c and starts S_c (its region follows the *running keys of earlier
+// chunks, which grows by its own) and its per-CTA write offsets O_c
+int launch_chunk_scan(const uint32_t* H_c, int G, int F1, uint32_t* T_c, uint64_t* S_c,
+                      unsigned long long* running, uint64_t* O_c, cudaStream_t s);
+// level-1 nodes from all rows of H (sizes and the starts they would have if
+// each bucket's keys were one range)
+int launch_l1_nodes(const uint32_t* H, int rows, int F1, Node* nodes, int shift1, cudaStream_t s);
 int launch_tile_hist(const Node* nodes, const Tile* tiles, uint32_t n_tiles,
                      const uint64_t* A, const uint64_t* B, uint32_t* TH, cudaStream_t s);
 int launch_node_scan(Node* nodes, uint32_t node_lo, uint32_t node_hi, Tile* tiles,

@@ -288,6 +288,47 @@ __global__ void k_l1_offsets_rows(const uint32_t* __restrict__ H, int G, int F1,
   }
 }
 
+// one upload chunk's bucket totals T_c[b] = sum_g H_c[g][b]
+__global__ void k_chunk_totals(const uint32_t* __restrict__ H, int G, int F1, uint32_t* T) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= F1) return;
+  uint32_t s = 0;
+  for (int g = 0; g < G; ++g) s += H[(size_t)g * F1 + b];
+  T[b] = s;
+}
+
+// its bucket starts (single block): its region follows the *running keys of
+// the earlier chunks, and *running grows by its own
+__global__ void k_chunk_starts(const uint32_t* __restrict__ T, int F1, uint64_t* __restrict__ S,
+                               unsigned long long* running) {
+  __shared__ unsigned long long tmp[32];
+  const unsigned long long before = *running;
+  const int per = (F1 + blockDim.x - 1) / blockDim.x;
+  const int lo = min(F1, (int)threadIdx.x * per), hi = min(F1, lo + per);
+  unsigned long long s = 0;
+  for (int i = lo; i < hi; ++i) s += T[i];
+  unsigned long long tot;
+  // the block scan synchronises: every thread has read *running before it changes
+  unsigned long long base = before + block_excl_scan<unsigned long long>(s, tmp, &tot);
+  for (int i = lo; i < hi; ++i) {
+    S[i] = base;
+    base += T[i];
+  }
+  if (threadIdx.x == 0) *running = before + tot;
+}
+
+// its per-(CTA, bucket) write offsets
+__global__ void k_chunk_offsets_rows(const uint32_t* __restrict__ H, int G, int F1,
+                                     const uint64_t* __restrict__ S, uint64_t* __restrict__ O) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= F1) return;
+  uint64_t run = S[b];
+  for (int g = 0; g < G; ++g) {
+    O[(size_t)g * F1 + b] = run;
+    run += H[(size_t)g * F1 + b];
+  }
+}
+
 // Thread-per-line level-1 passes (lines of at most kLineMaxW bytes).  A tile
 // of blockDim.x lines is staged in shared memory (TMA, double-buffered) and
 // each thread walks one line, rolling its 2-bit key one base at a time.
@@ -745,11 +786,24 @@ __device__ __forceinline__ uint32_t rank_in_digit(uint32_t* ctr, uint32_t v, boo
 // A split node is split on its next `width` bits, width chosen so that the
 // children average about half a bin: wide for big nodes, narrow for small.
 
+// node i's keys lie in several ranges (a level-1 bucket of a chunked upload)
+__device__ __forceinline__ bool multi_range(const Ranges& rg, uint32_t i) {
+  return rg.C > 0 && i < (uint32_t)rg.F1;
+}
+
+// partition tiles of node i: kTileKeys-key slices of each of its ranges
+__device__ __forceinline__ uint32_t node_tiles(const Node& nd, uint32_t i, const Ranges& rg) {
+  if (!multi_range(rg, i)) return (uint32_t)((nd.n + kTileKeys - 1) / kTileKeys);
+  uint32_t nt = 0;
+  for (int c = 0; c < rg.C; ++c) nt += (rg.T[(size_t)c * rg.F1 + i] + kTileKeys - 1) / kTileKeys;
+  return nt;
+}
+
 // Mark each node of the level final / split / empty; count what the split
 // nodes need (children, tiles, histogram entries).
 __global__ void k_classify(Node* nodes, uint32_t lo, uint32_t hi, uint32_t* final_list,
                            uint32_t* big_list, LevelCounters* ctr, int bin_cap, int split_target,
-                           int big_ok) {
+                           int big_ok, Ranges rg) {
   const uint32_t i = lo + blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= hi) return;
   const Node nd = nodes[i];
@@ -760,9 +814,11 @@ __global__ void k_classify(Node* nodes, uint32_t lo, uint32_t hi, uint32_t* fina
   }
   // a skewed node holds a hot k-mer: splitting peels off few keys per level,
   // while one hash bin streams any number of copies (it is re-partitioned if
-  // it holds too many distinct keys)
-  if (nd.n <= (uint64_t)bin_cap || nd.shift <= kDenseBits ||
-      (big_ok && nd.skewed && nd.n < (1ull << 31))) {
+  // it holds too many distinct keys).  A node of several ranges splits (into
+  // one range per child) whatever its size.
+  if (!multi_range(rg, i) &&
+      (nd.n <= (uint64_t)bin_cap || nd.shift <= kDenseBits ||
+       (big_ok && nd.skewed && nd.n < (1ull << 31)))) {
     nodes[i].state = NODE_FINAL;
     if (nd.n > (uint64_t)bin_cap && nd.shift > kDenseBits)
       big_list[atomicAdd(&ctr->n_big_final, 1u)] = i;
@@ -773,7 +829,7 @@ __global__ void k_classify(Node* nodes, uint32_t lo, uint32_t hi, uint32_t* fina
   const uint64_t target = (uint64_t)max(1, split_target / 2);  // children ~ target keys
   int w = ceil_log2_u64((nd.n + target - 1) / target);
   w = max(1, min(w, kMaxSplitBits));
-  const uint32_t nt = (uint32_t)((nd.n + kTileKeys - 1) / kTileKeys);
+  const uint32_t nt = node_tiles(nd, i, rg);
   nodes[i].state = NODE_SPLIT;
   nodes[i].width = (uint8_t)w;
   atomicAdd(&ctr->n_split, 1u);
@@ -789,13 +845,13 @@ __global__ void k_classify(Node* nodes, uint32_t lo, uint32_t hi, uint32_t* fina
 // histogram rows (buffers sized by the host from k_classify's counts); one
 // warp per node, its lanes write the tiles.
 __global__ void k_assign(Node* nodes, uint32_t lo, uint32_t hi, uint32_t child_base, Tile* tiles,
-                         LevelCounters* ctr) {
+                         LevelCounters* ctr, Ranges rg) {
   const uint32_t i = lo + ((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
   if (i >= hi) return;  // warp-uniform
   const Node nd = nodes[i];
   if (nd.state != NODE_SPLIT) return;
   const uint32_t R = 1u << nd.width;
-  const uint32_t nt = (uint32_t)((nd.n + kTileKeys - 1) / kTileKeys);
+  const uint32_t nt = node_tiles(nd, i, rg);
   uint32_t tb = 0, fc = 0;
   unsigned long long thb = 0;
   if (lane_id() == 0) {
@@ -809,6 +865,26 @@ __global__ void k_assign(Node* nodes, uint32_t lo, uint32_t hi, uint32_t child_b
   }
   tb = __shfl_sync(0xFFFFFFFFu, tb, 0);
   thb = __shfl_sync(0xFFFFFFFFu, thb, 0);
+  if (multi_range(rg, i)) {  // the tiles of each range in turn
+    uint32_t t0 = 0;
+    for (int c = 0; c < rg.C; ++c) {
+      const uint32_t cn = rg.T[(size_t)c * rg.F1 + i];
+      const uint64_t cs = rg.S[(size_t)c * rg.F1 + i];
+      const uint32_t ntc = (cn + kTileKeys - 1) / kTileKeys;
+      for (uint32_t u = lane_id(); u < ntc; u += 32) {
+        Tile tl;
+        tl.start = cs + (uint64_t)u * kTileKeys;
+        tl.n = min((uint32_t)kTileKeys, cn - u * (uint32_t)kTileKeys);
+        tl.node = i;
+        tl.th = thb + (uint64_t)(t0 + u) * R;
+        tl.hot = 0;
+        tl.pad = 0;
+        tiles[tb + t0 + u] = tl;
+      }
+      t0 += ntc;
+    }
+    return;
+  }
   for (uint32_t t = lane_id(); t < nt; t += 32) {
     Tile tl;
     tl.start = nd.start + (uint64_t)t * kTileKeys;
@@ -1855,6 +1931,22 @@ int launch_l1_count(const ExtractArgs& a, int grid, uint32_t* H, unsigned long l
   return 1;
 }
 
+int launch_chunk_scan(const uint32_t* H_c, int G, int F1, uint32_t* T_c, uint64_t* S_c,
+                      unsigned long long* running, uint64_t* O_c, cudaStream_t s) {
+  const int tb = 256, nb = (F1 + tb - 1) / tb;
+  k_chunk_totals<<<nb, tb, 0, s>>>(H_c, G, F1, T_c);
+  k_chunk_starts<<<1, 1024, 0, s>>>(T_c, F1, S_c, running);
+  k_chunk_offsets_rows<<<nb, tb, 0, s>>>(H_c, G, F1, S_c, O_c);
+  return 3;
+}
+
+int launch_l1_nodes(const uint32_t* H, int rows, int F1, Node* nodes, int shift1, cudaStream_t s) {
+  const int tb = 256, nb = (F1 + tb - 1) / tb;
+  k_l1_totals<<<nb, tb, 0, s>>>(H, rows, F1, nodes);
+  k_l1_starts<<<1, 1024, 0, s>>>(nodes, F1, shift1, nullptr);
+  return 2;
+}
+
 int launch_l1_scan(const uint32_t* H, int grid, int F1, uint64_t* O, Node* nodes, int shift1,
                    const int16_t* bucket_shift, cudaStream_t s) {
   const int tb = 256, nb = (F1 + tb - 1) / tb;
@@ -1932,11 +2024,11 @@ int launch_l1_scatter(const ExtractArgs& a, int grid, const uint64_t* O, uint64_
 
 int launch_classify(Node* nodes, uint32_t lo, uint32_t hi, uint32_t* final_list,
                     uint32_t* big_list, LevelCounters* ctr, int bin_cap, int split_target,
-                    int big_ok, cudaStream_t s) {
+                    int big_ok, const Ranges& rg, cudaStream_t s) {
   const uint32_t n = hi - lo;
   if (!n) return 0;
   k_classify<<<(n + 255) / 256, 256, 0, s>>>(nodes, lo, hi, final_list, big_list, ctr, bin_cap,
-                                            split_target, big_ok);
+                                            split_target, big_ok, rg);
   return 1;
 }
 
@@ -1948,11 +2040,11 @@ int launch_make_proxies(Node* nodes, const uint32_t* final_list, uint32_t n_fina
 }
 
 int launch_assign(Node* nodes, uint32_t lo, uint32_t hi, uint32_t child_base, Tile* tiles,
-                  LevelCounters* ctr, cudaStream_t s) {
+                  LevelCounters* ctr, const Ranges& rg, cudaStream_t s) {
   const uint32_t n = hi - lo;
   if (!n) return 0;
   k_assign<<<(uint32_t)(((uint64_t)n * 32 + 255) / 256), 256, 0, s>>>(nodes, lo, hi, child_base,
-                                                                      tiles, ctr);
+                                                                      tiles, ctr, rg);
   return 1;
 }
 

@@ -365,3 +365,21 @@ def test_streamed_and_chunked_together(variant):
     assert st2["upload_chunks"] == 0 and st2["table_streamed"] == 0
     assert a.n_kmers == b.n_kmers and np.array_equal(a.kmers, b.kmers)
     assert np.array_equal(a.counts, b.counts)
+
+
+def test_failed_chunked_count_leaves_the_context_usable():
+    """A count that does not fit the context's memory budget fails with an
+    admission or memory status after its chunked upload has started; the
+    same context then counts other reads exactly."""
+    text = _reads_68mb(84)
+    with dk.Engine(0, mem_budget=256 << 20) as e:
+        pin = dk.PinnedBuffer(text.size)
+        try:
+            pin.array[:] = text
+            with pytest.raises(dk.DkError) as ei:
+                e.count(pin.array, 150, 31, dk.VARIANT_HASH)
+            assert ei.value.status in (dk.DK_ERR_ADMISSION, dk.DK_ERR_OOM)
+            small = np.ascontiguousarray(pin.array[: 20_000 * 151])
+        finally:
+            pin.free()
+        check(e, small, 150, 31, dk.VARIANT_HASH)
