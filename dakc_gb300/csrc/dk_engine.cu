@@ -432,7 +432,7 @@ int Engine::count_batch(const dk_job* jobs, int njobs, const dk_input_desc* desc
     js.job_end.assign(js.job_start.begin() + 1, js.job_start.end());
     // level-1 buckets per job: the plain count's split, capped so the wave's
     // buckets fit the scatter kernel (largest jobs give up bits first)
-    std::vector<int> want(nj);
+    std::vector<int> want((size_t)std::max(nj, 1));  // a wave holds at least one job
     for (int j = 0; j < nj; ++j) {
       const int b = desc->l1_bits > 0 ? desc->l1_bits : l1_bits_for(lines[j0 + j] * per_line, target);
       want[j] = std::max(0, std::min({b, kMaxL1Bits, 2 * k}));
