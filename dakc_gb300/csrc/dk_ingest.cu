@@ -42,15 +42,11 @@ __global__ void __launch_bounds__(kIngThreads) k_nl_count(const uint8_t* __restr
   if (threadIdx.x == 0) cnt[blockIdx.x] = total;
 }
 
-__global__ void k_scan_serial(uint64_t* v, uint64_t n, uint64_t* total) {
-  if (blockIdx.x || threadIdx.x) return;
-  uint64_t run = 0;
-  for (uint64_t i = 0; i < n; ++i) {
-    const uint64_t c = v[i];
-    v[i] = run;
-    run += c;
-  }
-  *total = run;
+// exclusive scan of the chunk counts in place, by one block; *total = their sum
+__global__ void __launch_bounds__(1024) k_scan_block(uint64_t* v, uint64_t n, uint64_t* total) {
+  __shared__ uint64_t tmp[32];
+  const uint64_t t = dev::block_scan_array<uint64_t>(v, (int)n, tmp);
+  if (threadIdx.x == 0) *total = t;
 }
 
 // positions of the newlines, in order
@@ -166,7 +162,7 @@ int Engine::count_format(const char* text, uint64_t nbytes, int format, const dk
     DK_TRY(Arena::ensure(this, aux, (chunks + 2) * 8));
     uint64_t* cnt = (uint64_t*)aux.p;
     k_nl_count<<<(uint32_t)chunks, kIngThreads, 0, stream>>>((const uint8_t*)text2.p, nbytes, cnt);
-    k_scan_serial<<<1, 1, 0, stream>>>(cnt, chunks, cnt + chunks);
+    k_scan_block<<<1, 1024, 0, stream>>>(cnt, chunks, cnt + chunks);
     DK_CUDA(cudaGetLastError());
     uint64_t nl = 0;
     DK_TRY(sync_read(cnt + chunks, 8, &nl));

@@ -50,6 +50,39 @@ __global__ void __launch_bounds__(kOpsThreads) k_count_hist(const uint32_t* __re
       if (sh[j]) atomicAdd(&hist[j], (unsigned long long)sh[j]);
 }
 
+// Histogram of at most kLaneHistBuckets buckets: every lane owns a column of
+// the shared histogram (bucket * 32 + lane), so its adds never conflict with
+// another lane of its warp; the 32 columns are summed at the end.
+constexpr uint32_t kLaneHistBuckets = 256;
+__global__ void __launch_bounds__(kOpsThreads) k_count_hist_lanes(const uint32_t* __restrict__ counts,
+                                                                  uint64_t n, uint32_t nb,
+                                                                  unsigned long long* __restrict__ hist) {
+  __shared__ uint32_t sh[kLaneHistBuckets * 32];
+  for (uint32_t j = threadIdx.x; j < nb * 32; j += blockDim.x) sh[j] = 0;
+  __syncthreads();
+  const uint32_t lane = threadIdx.x & 31;
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  for (; i + 3 * stride < n; i += 4 * stride) {  // four loads in flight
+    const uint32_t c0 = counts[i], c1 = counts[i + stride], c2 = counts[i + 2 * stride],
+                   c3 = counts[i + 3 * stride];
+    if (c0 < nb) atomicAdd(&sh[c0 * 32 + lane], 1u);
+    if (c1 < nb) atomicAdd(&sh[c1 * 32 + lane], 1u);
+    if (c2 < nb) atomicAdd(&sh[c2 * 32 + lane], 1u);
+    if (c3 < nb) atomicAdd(&sh[c3 * 32 + lane], 1u);
+  }
+  for (; i < n; i += stride) {
+    const uint32_t c = counts[i];
+    if (c < nb) atomicAdd(&sh[c * 32 + lane], 1u);
+  }
+  __syncthreads();
+  for (uint32_t j = threadIdx.x; j < nb; j += blockDim.x) {
+    unsigned long long s = 0;
+    for (uint32_t l = 0; l < 32; ++l) s += sh[j * 32 + ((l + j) & 31)];  // rotated: no bank conflict
+    if (s) atomicAdd(&hist[j], s);
+  }
+}
+
 // Stable compaction of the entries with count >= min_count, in chunks of
 // kOpsThreads * kPer consecutive entries per block.  Pass 1 counts the kept
 // entries per chunk; pass 2 writes them at the chunk's offset.
@@ -71,16 +104,11 @@ __global__ void __launch_bounds__(kOpsThreads) k_filter_count(const uint32_t* __
   if (threadIdx.x == 0) kept[blockIdx.x] = total;
 }
 
-__global__ void k_exclusive_scan_serial(uint64_t* v, uint64_t n, uint64_t* total) {
-  // one thread: the chunk counts of a table (n = entries / 4096) are few
-  if (blockIdx.x || threadIdx.x) return;
-  uint64_t run = 0;
-  for (uint64_t i = 0; i < n; ++i) {
-    const uint64_t c = v[i];
-    v[i] = run;
-    run += c;
-  }
-  *total = run;
+// exclusive scan of the chunk counts in place, by one block; *total = their sum
+__global__ void __launch_bounds__(1024) k_exclusive_scan_block(uint64_t* v, uint64_t n, uint64_t* total) {
+  __shared__ uint64_t tmp[32];
+  const uint64_t t = dev::block_scan_array<uint64_t>(v, (int)n, tmp);
+  if (threadIdx.x == 0) *total = t;
 }
 
 // Rounds of 256 consecutive entries: a warp ballot orders the kept entries
@@ -185,7 +213,10 @@ int Engine::table_histogram(const dk_table* t, uint32_t nb, uint64_t* hist, uint
   DK_CUDA(cudaSetDevice(device));
   DK_TRY(Arena::ensure(this, aux, (size_t)nb * 8));
   DK_CUDA(cudaMemsetAsync(aux.p, 0, (size_t)nb * 8, stream));
-  if (t->n)
+  if (t->n && nb <= kLaneHistBuckets)
+    k_count_hist_lanes<<<grid_for(t->n, sm_count), kOpsThreads, 0, stream>>>(
+        t->counts, t->n, nb, (unsigned long long*)aux.p);
+  else if (t->n)
     k_count_hist<<<grid_for(t->n, sm_count), kOpsThreads, 0, stream>>>(
         t->counts, t->n, nb, (unsigned long long*)aux.p);
   DK_CUDA(cudaGetLastError());
@@ -217,7 +248,7 @@ int Engine::table_filter(const dk_table* t, uint32_t min_count, dk_table* out) {
   uint64_t total = 0;
   if (n) {
     k_filter_count<<<(uint32_t)chunks, kOpsThreads, 0, stream>>>(t->counts, n, min_count, kept);
-    k_exclusive_scan_serial<<<1, 1, 0, stream>>>(kept, chunks, kept + chunks);
+    k_exclusive_scan_block<<<1, 1024, 0, stream>>>(kept, chunks, kept + chunks);
     DK_CUDA(cudaGetLastError());
     DK_TRY(sync_read(kept + chunks, 8, &total));
   }

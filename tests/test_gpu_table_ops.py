@@ -22,7 +22,7 @@ def test_histogram_filter_lookup_pairs(engine, reads, residency):
     t = engine.count_table(reads, 150, 31, dk.VARIANT_HASH, residency)
     try:
         assert int(t.n) == keys.size and int(t.on_device) == (residency == dk.RESIDENT_DEVICE)
-        for nb in (1, 2, 40, 100, 20000):
+        for nb in (1, 2, 40, 100, 256, 257, 20000):  # per-lane columns up to 256 buckets
             hist, mb = engine.histogram(t, nb)
             ref_hist, ref_mb = pyoracle.pakman_histogram_cutoff(counts, nb)
             assert np.array_equal(hist, ref_hist), nb
