@@ -263,9 +263,11 @@ class Engine:
         return t
 
     def count_format(self, text, fmt: int, k: int, convention: int = 0, line_width: int = 0,
-                     variant: int = VARIANT_AUTO):
+                     variant: int = VARIANT_AUTO, copy: bool = True):
         """Count reads given as FASTQ / FASTA / one per line (dk_count_format);
-        returns (CountResult, the line width they were laid out at)."""
+        returns (CountResult, the line width they were laid out at).  With
+        copy=False the host table is released without being copied out and the
+        result is (distinct k-mers, k-mer occurrences) instead."""
         ptr, n, keep = _buf_ptr(text)
         d = self.desc(max(line_width, 0), k, variant)
         d.convention = convention
@@ -274,6 +276,8 @@ class Engine:
         self._check(self.lib.dk_count_format(self.h, ctypes.c_void_p(ptr), n, fmt, ctypes.byref(d),
                                              ctypes.byref(t), ctypes.byref(w)), "dk_count_format")
         try:
+            if not copy:
+                return (int(t.n), int(t.n_kmers)), int(w.value)
             return self.table_result(t), int(w.value)
         finally:
             self.free_table(t)
