@@ -1343,7 +1343,9 @@ int Engine::count_locked(const char* text, uint64_t nbytes, bool text_on_device,
   out_sink = nullptr;
   out_groups = 1;
   const bool chunked_up = chunks.n > 1;
-  if (chunked_up && rc != DK_OK) cudaStreamSynchronize(s_in);  // no copy left in flight
+  // no chunk copy may still read the caller's buffer when the call returns
+  // (a count that ends early, e.g. lines shorter than k, never waited for them)
+  if (chunked_up) cudaStreamSynchronize(s_in);
   chunks.n = 0;
   stats.upload_chunks = chunked_up ? (uint64_t)kMaxChunks : 0;
   if (h_tb && (rc != DK_OK || !streaming || streamed != dt.n)) {

@@ -383,3 +383,22 @@ def test_failed_chunked_count_leaves_the_context_usable():
         finally:
             pin.free()
         check(e, small, 150, 31, dk.VARIANT_HASH)
+
+
+def test_chunked_upload_with_lines_shorter_than_k(engine):
+    """A 64 MB page-locked read set whose lines are shorter than k has no
+    k-mers; the call returns an empty table after its chunked upload ends,
+    and the context counts the next reads exactly."""
+    W = 20
+    n_lines = (70 << 20) // (W + 1)
+    text = np.full((n_lines, W + 1), ord("A"), np.uint8)
+    text[:, W] = ord("\n")
+    pin = dk.PinnedBuffer(text.size)
+    try:
+        pin.array[:] = text.reshape(-1)
+        r = engine.count(pin.array, W, 31)
+        assert r.n_kmers == 0 and r.kmers.size == 0
+    finally:
+        pin.free()
+    small = _reads_68mb(85)[: 5_000 * 151]
+    check(engine, small, 150, 31)
