@@ -1467,7 +1467,12 @@ int dk_destroy(dk_ctx* ctx) {
 }
 
 const char* dk_last_error_string(dk_ctx* ctx) {
-  return ctx ? ctx->eng.last_error.c_str() : "null context";
+  if (!ctx) return "null context";
+  // a copy per calling thread: another thread's count may replace the text
+  thread_local std::string copy;
+  std::lock_guard<std::mutex> g(ctx->eng.err_mu);
+  copy = ctx->eng.last_error;
+  return copy.c_str();
 }
 
 int dk_count(dk_ctx* ctx, const char* text, uint64_t nbytes, const dk_input_desc* desc,
@@ -1517,6 +1522,7 @@ int dk_autotune_reset(dk_ctx* ctx) {
 
 int dk_last_stats(dk_ctx* ctx, dk_stats* out) {
   if (!ctx || !out) return DK_ERR_INVALID_ARG;
+  std::lock_guard<std::mutex> g(ctx->eng.mu);  // a count on another thread writes them
   *out = ctx->eng.stats;
   return DK_OK;
 }

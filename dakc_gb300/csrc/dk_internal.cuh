@@ -77,6 +77,8 @@ constexpr int kCountThreads = 512;       // ... except the count (one buffer of 
                                          // CTA's lines do not depend on its tile size
 constexpr int kLineMaxW = 256;           // longer lines use the warp-per-line kernels
 constexpr int kLineChunk = 16;           // positions per line in one chunked-scatter chunk
+                                         // (twice this where shared memory still fits
+                                         // two CTAs per SM)
 
 struct ExtractArgs {
   const uint8_t* text;  // device text (the line kernels take any alignment)

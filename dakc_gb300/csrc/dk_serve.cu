@@ -47,6 +47,9 @@ struct Request {
   uint64_t kmers = 0;  // upper bound: lines * (line_width - k + 1)
   Clock::time_point t_submit, t_start, t_end;
   int status = DK_ERR_PENDING;
+  // cancelled while its batch runs: it stays pending (its text is still
+  // read) until the batch ends, then becomes DK_ERR_CANCELLED
+  bool cancel = false;
   dk_table table{};
   int worker = -1;
   int batch_jobs = 0;
@@ -126,9 +129,10 @@ struct Server {
           auto& r = batch[i];
           r->t_end = now;
           r->batch_jobs = (int)batch.size();
-          if (r->status == DK_ERR_CANCELLED) {
+          if (r->cancel) {
             if (rc == DK_OK) me.eng->release_table(outs[i].handle);
-            continue;  // stays CANCELLED; dk_poll reports it
+            r->status = DK_ERR_CANCELLED;  // dk_poll reports it; the text is free
+            continue;
           }
           r->status = rc;
           if (rc == DK_OK) {
@@ -152,6 +156,7 @@ namespace dk {
 Server* server_of(dk_ctx* ctx);
 void set_server(dk_ctx* ctx, Server* s);
 Engine* engine_of(dk_ctx* ctx);
+int serve_release(Server* s, uint64_t handle);
 }  // namespace dk
 
 extern "C" {
@@ -220,7 +225,11 @@ static int take_result(Server* s, uint64_t ticket, dk_table* out, dk_job_info* i
   auto r = it->second;
   if (r->status == DK_ERR_PENDING) return DK_ERR_PENDING;
   const int st = r->status;
-  if (out) *out = r->table;
+  if (out) {
+    *out = r->table;
+  } else if (st == DK_OK && r->table.handle) {
+    dk::serve_release(s, r->table.handle);  // no one takes the table: free it now
+  }
   if (info) {
     info->queued_us = dk::us_since(r->t_submit, r->t_start);
     info->run_us = dk::us_since(r->t_start, r->t_end);
@@ -267,7 +276,7 @@ int dk_cancel(dk_ctx* ctx, uint64_t ticket) {
       return DK_OK;
     }
   if (r->status == DK_ERR_PENDING) {  // running: its table is dropped when the batch ends
-    r->status = DK_ERR_CANCELLED;
+    r->cancel = true;
     return DK_OK;
   }
   return DK_ERR_INVALID_ARG;  // already finished: take it with dk_poll and free it
@@ -276,7 +285,12 @@ int dk_cancel(dk_ctx* ctx, uint64_t ticket) {
 int dk_serve_stop(dk_ctx* ctx) {
   Server* s = ctx ? dk::server_of(ctx) : nullptr;
   if (!s) return DK_ERR_INVALID_ARG;
-  s->stop.store(true);
+  {
+    // under the lock: a worker between its wait predicate and its sleep
+    // would otherwise miss the notification and never wake
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->stop.store(true);
+  }
   s->cv_work.notify_all();
   for (auto& w : s->workers)
     if (w.th.joinable()) w.th.join();

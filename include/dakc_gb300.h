@@ -276,13 +276,16 @@ typedef struct {
 } dk_job_info;
 
 int dk_serve_start(dk_ctx* ctx, int workers, int max_batch_jobs);
-/* text is borrowed until the job completes (or is cancelled and polled) */
+/* text is borrowed until dk_poll / dk_wait returns anything but
+ * DK_ERR_PENDING or DK_ERR_TIMEOUT for the job */
 int dk_submit(dk_ctx* ctx, const char* text, uint64_t nbytes, const dk_input_desc* desc,
               uint64_t* ticket);
 /* DK_ERR_PENDING while queued or running; otherwise the job's status, with
- * its table in *out (release with dk_table_free) */
+ * its table in *out (release with dk_table_free; out NULL releases it) */
 int dk_poll(dk_ctx* ctx, uint64_t ticket, dk_table* out, dk_job_info* info);
 int dk_wait(dk_ctx* ctx, uint64_t ticket, int timeout_ms, dk_table* out, dk_job_info* info);
+/* a queued job is dropped at once; a running one stays DK_ERR_PENDING (its
+ * text still read) until its batch ends, then polls as DK_ERR_CANCELLED */
 int dk_cancel(dk_ctx* ctx, uint64_t ticket);
 int dk_serve_stop(dk_ctx* ctx);  /* finishes queued jobs, joins the workers */
 

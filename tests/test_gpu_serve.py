@@ -62,6 +62,36 @@ def test_poll_cancel_and_timeout():
         eng.serve_stop()
 
 
+def test_cancelled_running_job_stays_pending_until_its_batch_ends():
+    """A job cancelled while its batch runs keeps its text borrowed: it polls
+    DK_ERR_PENDING (never a result) until the batch ends, then
+    DK_ERR_CANCELLED; the worker then serves the next job normally."""
+    big = synth.random_lines(5, 100_000, 250)     # ~25 MB, some ms of work
+    small = texts(3, 13)
+    with dk.Engine(0) as eng:
+        eng.serve_start(workers=1, max_batch_jobs=4)
+        tk = eng.submit(big, 250, 31)
+        time.sleep(0.02)                           # usually running by now
+        assert eng.cancel(tk) in (dk.DK_OK, dk.DK_ERR_INVALID_ARG)
+        rc = eng.lib.dk_wait(eng.h, tk, 120_000, None, None)
+        assert rc in (dk.DK_ERR_CANCELLED, dk.DK_OK)
+        big[:] = 0                                 # the text is no longer read
+        for t in small:
+            res, _ = eng.wait(eng.submit(t, 250, 31), 120_000)
+            keys, counts, nk = pyoracle.count(t, 250, 31)
+            assert res.n_kmers == nk and np.array_equal(res.kmers, keys)
+            assert np.array_equal(res.counts, counts)
+        eng.serve_stop()
+
+
+def test_serve_stop_right_after_start_returns():
+    """dk_serve_stop with idle workers (none has slept yet) joins them."""
+    with dk.Engine(0) as eng:
+        for _ in range(20):
+            eng.serve_start(workers=4, max_batch_jobs=4)
+            eng.serve_stop()
+
+
 def test_admission_rejects_oversized_job():
     big = synth.random_lines(1, 200_000, 250)   # ~50 MB of reads, ~44M k-mers
     with dk.Engine(0, mem_budget=256 << 20) as eng:
