@@ -441,13 +441,13 @@ __global__ void __launch_bounds__(kCountThreads) k_l1_lines_count(ExtractArgs a,
     if (line_prologue(a, l, l1, line, &jb, counters, s_jobs)) {
       LineRoll r;
       r.reset();
-      for (int p0 = 0; p0 < W && !r.stopped; p0 += 4) {
-        uint32_t c4[4];
+      for (int p0 = 0; p0 < W && !r.stopped; p0 += 8) {  // 8 independent loads per group
+        uint32_t c8[8];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) c4[u] = p0 + u < W ? lut[line[p0 + u]] : 0xF0u;
+        for (int u = 0; u < 8; ++u) c8[u] = p0 + u < W ? lut[line[p0 + u]] : 0xF0u;
 #pragma unroll
-        for (int u = 0; u < 4; ++u)
-          if (r.template step<PAK>(c4[u], p0 + u, W, k, a.kmask)) {
+        for (int u = 0; u < 8; ++u)
+          if (r.template step<PAK>(c8[u], p0 + u, W, k, a.kmask)) {
             atomicAdd(&cnt[a.njobs ? jb(r.key) : (uint32_t)(r.key >> a.shift1)], 1u);
             ++mine;
           }
