@@ -227,14 +227,20 @@ def pct(xs, p):
 def run_batched(eng, texts, variant):
     """jobs/s of one dk_count_batch over all sets vs one dk_count per set,
     both timed around the C calls (tables are released, not copied out);
-    per-set tables of the two forms are compared on a subset."""
+    per-set tables of the two forms are compared on a subset.  Each form is
+    timed `reps` times after a warm-up and its median kept: the host copies
+    of one call vary with the host's memory traffic."""
     import dakc_gb300 as dk
+    reps = 3
     desc = dk.Engine.desc(250, 31, variant, dk.RESIDENT_HOST)
     keep = [dk._buf_ptr(t) for t in texts]
     eng.count_batch_nocopy(texts, 250, 31, variant)  # warm-up: pools reach steady state
-    t0 = time.perf_counter()
-    nk, nd = eng.count_batch_nocopy(texts, 250, 31, variant)
-    t_batch = time.perf_counter() - t0
+    t_runs = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        nk, nd = eng.count_batch_nocopy(texts, 250, 31, variant)
+        t_runs.append(time.perf_counter() - t0)
+    t_batch = float(np.median(t_runs))
     st = eng.stats()
 
     def one(ptr, n):
@@ -243,26 +249,31 @@ def run_batched(eng, texts, variant):
 
     for ptr, n, _ in keep:
         one(ptr, n)  # warm-up
-    lat = []
-    t0 = time.perf_counter()
-    for ptr, n, _ in keep:
-        a = time.perf_counter()
-        one(ptr, n)
-        lat.append(time.perf_counter() - a)
-    t_plain = time.perf_counter() - t0
+    lat, p_runs = [], []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        for ptr, n, _ in keep:
+            a = time.perf_counter()
+            one(ptr, n)
+            lat.append(time.perf_counter() - a)
+        p_runs.append(time.perf_counter() - t0)
+    t_plain = float(np.median(p_runs))
     sub = texts[:16]
     got = eng.count_batch(sub, 250, 31, variant)
     exact = all(np.array_equal(g.kmers, p.kmers) and np.array_equal(g.counts, p.counts)
                 for g, p in zip(got, (eng.count(t, 250, 31, variant) for t in sub)))
     return {"jobs": len(texts), "k_mers": nk, "distinct": nd, "exact_vs_plain_subset": bool(exact),
             "batched": {"jobs_per_s": len(texts) / t_batch, "kmers_per_s": nk / t_batch,
-                        "seconds": t_batch, "waves": st["n_waves"], "ms_device": st["ms_device"],
+                        "seconds": t_batch, "seconds_all": [round(x, 5) for x in t_runs],
+                        "waves": st["n_waves"], "ms_device": st["ms_device"],
                         "ms_h2d": st["ms_h2d"], "ms_d2h": st["ms_d2h"],
                         "kernel_launches": st["kernel_launches"],
                         "kernels_ms": {KERNEL_NAMES[i]: round(float(st["ms_kernel"][i]), 3)
                                        for i in range(8)}},
             "one_job_per_launch": {"jobs_per_s": len(texts) / t_plain, "kmers_per_s": nk / t_plain,
-                                   "seconds": t_plain, "p50_ms": 1e3 * pct(lat, 50),
+                                   "seconds": t_plain,
+                                   "seconds_all": [round(x, 5) for x in p_runs],
+                                   "p50_ms": 1e3 * pct(lat, 50),
                                    "p99_ms": 1e3 * pct(lat, 99)},
             "speedup_jobs_per_s": t_plain / t_batch}
 
