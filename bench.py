@@ -417,7 +417,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-autotune", action="store_true",
                     help="count with the automatic parameters instead of the autotuned ones")
-    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--mode", default="count", choices=["count", "batch", "serve", "formats"],
                     help="count: the headline line; batch / serve: batched and served forms")
     ap.add_argument("--jobs", type=int, default=256, help="read sets for batch / serve modes")
@@ -562,7 +562,8 @@ def main():
         pin = dk.PinnedBuffer(nbytes)
         pin.array[:] = rs.text
         hdesc = dk.Engine.desc(rs.line_width, rs.k, variant, dk.RESIDENT_HOST)
-        for _ in range(2):  # the first call pins the host table pool, the second settles it
+        # the first call pins the host table pool; the others settle it
+        for _ in range(3):
             eng.free_table(eng.count_raw(pin.ptr, nbytes, hdesc))
         walls = []
         for _ in range(args.e2e_steps):
