@@ -254,29 +254,39 @@ int Engine::table_filter(const dk_table* t, uint32_t min_count, dk_table* out) {
   }
   TableBuf* tb = nullptr;
   DK_TRY(acquire_table(std::max<uint64_t>(total, 1), t->on_device != 0, &tb));
-  if (total) {
-    k_filter_write<<<(uint32_t)chunks, kOpsThreads, 0, stream>>>(
-        t->kmers, t->counts, n, min_count, kept, (uint64_t*)tb->k, (uint32_t*)tb->c);
-    DK_CUDA(cudaGetLastError());
+  // the kept entries and their occurrences; on failure the new table goes
+  // back to its pool and *out stays empty
+  auto fill = [&]() -> int {
+    if (total) {
+      k_filter_write<<<(uint32_t)chunks, kOpsThreads, 0, stream>>>(
+          t->kmers, t->counts, n, min_count, kept, (uint64_t*)tb->k, (uint32_t*)tb->c);
+      DK_CUDA(cudaGetLastError());
+    }
+    DK_CUDA(cudaStreamSynchronize(stream));
+    if (total) {
+      // occurrences of the kept k-mers = the sum of their counts
+      DK_TRY(Arena::ensure(this, aux, (chunks + 2) * 8 + 8));
+      uint64_t* sum = (uint64_t*)aux.p + chunks + 1;
+      DK_CUDA(cudaMemsetAsync(sum, 0, 8, stream));
+      k_sum_counts<<<grid_for(total, sm_count), kOpsThreads, 0, stream>>>(
+          (const uint32_t*)tb->c, total, (unsigned long long*)sum);
+      DK_CUDA(cudaGetLastError());
+      DK_TRY(sync_read(sum, 8, &out->n_kmers));
+    }
+    return DK_OK;
+  };
+  const int rc = fill();
+  if (rc != DK_OK) {
+    release_table(tb->id);
+    std::memset(out, 0, sizeof(*out));
+    return rc;
   }
-  DK_CUDA(cudaStreamSynchronize(stream));
   out->kmers = (uint64_t*)tb->k;
   out->counts = (uint32_t*)tb->c;
   out->n = total;
-  out->n_kmers = 0;  // occurrences of the kept k-mers: filled below
   out->on_device = t->on_device;
   out->variant_used = t->variant_used;
   out->handle = tb->id;
-  if (total) {
-    // occurrences of the kept k-mers = the sum of their counts
-    DK_TRY(Arena::ensure(this, aux, (chunks + 2) * 8 + 8));
-    uint64_t* sum = (uint64_t*)aux.p + chunks + 1;
-    DK_CUDA(cudaMemsetAsync(sum, 0, 8, stream));
-    k_sum_counts<<<grid_for(total, sm_count), kOpsThreads, 0, stream>>>(
-        (const uint32_t*)tb->c, total, (unsigned long long*)sum);
-    DK_CUDA(cudaGetLastError());
-    DK_TRY(sync_read(sum, 8, &out->n_kmers));
-  }
   return DK_OK;
 }
 
