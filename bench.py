@@ -565,19 +565,23 @@ def main():
         # the first call pins the host table pool; the others settle it
         for _ in range(3):
             eng.free_table(eng.count_raw(pin.ptr, nbytes, hdesc))
-        walls = []
+        walls, parts = [], []
         for _ in range(args.e2e_steps):
             t0 = time.perf_counter()
             t = eng.count_raw(pin.ptr, nbytes, hdesc)
             walls.append(time.perf_counter() - t0)
             n_out = int(t.n)
             eng.free_table(t)
-        st = eng.stats()
+            st = eng.stats()
+            # per call: device time, upload, and the download left after the device
+            parts.append([round(st["ms_device"], 2), round(st["ms_h2d"], 2),
+                          round(st["ms_d2h"], 2)])
         w = float(np.mean(walls))
         e2e = {"value": nk / w, "unit": UNIT, "h2d_bytes_per_step": nbytes,
                "d2h_bytes_per_step": n_out * 12, "ms_per_step": w * 1000.0,
                "ms_h2d": st["ms_h2d"], "ms_d2h": st["ms_d2h"],
-               "walls_ms": [round(x * 1000.0, 2) for x in walls]}
+               "walls_ms": [round(x * 1000.0, 2) for x in walls],
+               "device_h2d_d2h_ms": parts}
         pin.free()
 
     forms = None
