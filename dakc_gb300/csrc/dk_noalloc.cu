@@ -8,25 +8,20 @@
 // and forbids other libraries from reserving more.  dk_count and
 // dk_count_device allocate their work buffers (key partitions, staging) in
 // the engine context, so such callers cannot use them.  This entry point
-// needs no context: the caller passes device input and output buffers, and
-// the only scratch (the unsorted k-mers and the run-length head positions)
-// lives in one fixed array below that the library reserves at load time.
+// needs no context and no scratch: the caller passes device input and output
+// buffers.  The unsorted k-mers wait in the caller's k-mer array (it holds at
+// least the k-mer bound) until they are sorted into shared memory, and the
+// run-length head positions stay in shared memory.
 //
 // Limits and sharing rules:
 //   * at most kNoAllocMaxKmers (12,288) k-mer occurrences per call, judged by
 //     the upper bound lines * (line_width - k + 1); larger inputs are
 //     rejected with DK_ERR_ADMISSION before anything is launched;
-//   * the scratch array (147,712 bytes) is held on every GPU that loads the
-//     library until the process exits;
-//   * every call uses the same array and leaves its contents behind; nothing
-//     in it needs to start at zero (each word a call reads was written
-//     earlier in that same call), but two calls whose kernels overlap on the
-//     GPU -- on different streams, or from different host threads -- race
-//     on it and give wrong tables.  Serialise them on one stream;
+//   * calls share no device memory: calls on different streams or host
+//     threads may overlap, each with its own output buffers;
 //   * the first call on a device (with that device current) does a one-time
-//     set-up: it looks up the array's device address with
-//     cudaGetSymbolAddress and raises the kernel's shared-memory limit.
-//     Make that first call before any stream capture on that device.
+//     set-up: it raises the kernel's shared-memory limit.  Make that first
+//     call before any stream capture on that device.
 //
 // The kernel is a single-CTA variant of the engine's bin count: it extracts
 // the k-mers of every line (the same warp-per-line extraction), counting-sorts
@@ -46,26 +41,26 @@ using namespace dev;
 
 constexpr int kNoAllocMaxKmers = 12288;
 constexpr int kNoAllocThreads = 512;
-// scratch layout, in 8-byte words: [0, max) k-mers, then max/2 words holding
-// max uint32 head positions, then 32 spare words
-constexpr int kNoAllocWords = kNoAllocMaxKmers + kNoAllocMaxKmers / 2 + 32;
-
-static __device__ __align__(256) unsigned long long g_noalloc_scratch[kNoAllocWords];
+// dynamic shared memory: the sorted k-mers, then the run heads (uint32)
+constexpr size_t kNoAllocSmem = (size_t)kNoAllocMaxKmers * 12;
 
 template <int C>
 __global__ void __launch_bounds__(kNoAllocThreads)
     k_count_small_static(const uint8_t* __restrict__ text, uint64_t n_lines, int W, int k,
-                         unsigned long long* __restrict__ scratch, uint64_t* __restrict__ out_k,
-                         uint32_t* __restrict__ out_c, uint64_t* __restrict__ summary) {
-  extern __shared__ unsigned long long skeys[];  // kNoAllocMaxKmers
+                         uint64_t* out_k, uint32_t* __restrict__ out_c,
+                         uint64_t* __restrict__ summary) {
+  extern __shared__ unsigned long long skeys[];  // kNoAllocMaxKmers, then the heads
   __shared__ uint32_t hist[1u << 12];
   __shared__ unsigned long long tmp[32];
   __shared__ uint8_t lut[256];
   __shared__ uint16_t long_list[512];
   __shared__ uint32_t s_n, n_long;
   __shared__ unsigned long long s_first_nul;
-  unsigned long long* keys = scratch;
-  uint32_t* heads = reinterpret_cast<uint32_t*>(scratch + kNoAllocMaxKmers);
+  // the raw k-mers wait in the caller's table (it holds at least the k-mer
+  // bound) until they are sorted into shared memory; the table is written
+  // only after that
+  unsigned long long* keys = reinterpret_cast<unsigned long long*>(out_k);
+  uint32_t* heads = reinterpret_cast<uint32_t*>(skeys + kNoAllocMaxKmers);
   if (threadIdx.x == 0) {
     s_n = 0;
     n_long = 0;
@@ -150,13 +145,13 @@ __global__ void __launch_bounds__(kNoAllocThreads)
   for (uint32_t i = lo; i < hi; ++i)
     if (i == 0 || skeys[i] != skeys[i - 1]) {
       out_k[r] = skeys[i];
-      __stcg(heads + r, i);
+      heads[r] = i;
       ++r;
     }
   __syncthreads();
   for (uint32_t q = threadIdx.x; q < total; q += blockDim.x) {
-    const uint32_t end = (q + 1 < total) ? __ldcg(heads + q + 1) : n;
-    out_c[q] = end - __ldcg(heads + q);
+    const uint32_t end = (q + 1 < total) ? heads[q + 1] : n;
+    out_c[q] = end - heads[q];
   }
   if (threadIdx.x == 0) {
     summary[0] = total;
@@ -167,7 +162,6 @@ __global__ void __launch_bounds__(kNoAllocThreads)
 
 struct DeviceSetup {
   bool ready = false;
-  unsigned long long* scratch = nullptr;
 };
 constexpr int kMaxDevices = 128;
 std::mutex g_setup_mu;
@@ -176,19 +170,14 @@ DeviceSetup g_setup[kMaxDevices];
 template <int C>
 cudaError_t prepare_kernel() {
   return cudaFuncSetAttribute(k_count_small_static<C>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              kNoAllocMaxKmers * 8);
+                              (int)kNoAllocSmem);
 }
 
 // one-time, per-device set-up (the device must be current)
-int setup_device(int dev, unsigned long long** scratch) {
+int setup_device(int dev) {
   std::lock_guard<std::mutex> g(g_setup_mu);
   DeviceSetup& s = g_setup[dev];
   if (!s.ready) {
-    void* p = nullptr;
-    if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) {
-      cudaGetLastError();
-      return DK_ERR_CUDA;
-    }
     cudaError_t e = cudaSuccess;
     for (cudaError_t x : {prepare_kernel<1>(), prepare_kernel<2>(), prepare_kernel<4>(),
                           prepare_kernel<5>(), prepare_kernel<8>(), prepare_kernel<16>(),
@@ -198,10 +187,8 @@ int setup_device(int dev, unsigned long long** scratch) {
       cudaGetLastError();
       return DK_ERR_CUDA;
     }
-    s.scratch = static_cast<unsigned long long*>(p);
     s.ready = true;
   }
-  *scratch = s.scratch;
   return DK_OK;
 }
 
@@ -231,20 +218,19 @@ extern "C" int dk_count_small_noalloc(const char* d_text, uint64_t nbytes, int l
     cudaGetLastError();
     return DK_ERR_NO_DEVICE;
   }
-  unsigned long long* scratch = nullptr;
-  const int rc = setup_device(dev, &scratch);
+  const int rc = setup_device(dev);
   if (rc != DK_OK) return rc;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   const uint8_t* t = reinterpret_cast<const uint8_t*>(d_text);
-  const size_t smem = (size_t)kNoAllocMaxKmers * 8;
+  const size_t smem = kNoAllocSmem;
   const int c = (line_width + 31) / 32;
-  if (c <= 1) k_count_small_static<1><<<1, kNoAllocThreads, smem, s>>>(t, lines, line_width, k, scratch, d_kmers, d_counts, d_summary);
-  else if (c <= 2) k_count_small_static<2><<<1, kNoAllocThreads, smem, s>>>(t, lines, line_width, k, scratch, d_kmers, d_counts, d_summary);
-  else if (c <= 4) k_count_small_static<4><<<1, kNoAllocThreads, smem, s>>>(t, lines, line_width, k, scratch, d_kmers, d_counts, d_summary);
-  else if (c <= 5) k_count_small_static<5><<<1, kNoAllocThreads, smem, s>>>(t, lines, line_width, k, scratch, d_kmers, d_counts, d_summary);
-  else if (c <= 8) k_count_small_static<8><<<1, kNoAllocThreads, smem, s>>>(t, lines, line_width, k, scratch, d_kmers, d_counts, d_summary);
-  else if (c <= 16) k_count_small_static<16><<<1, kNoAllocThreads, smem, s>>>(t, lines, line_width, k, scratch, d_kmers, d_counts, d_summary);
-  else k_count_small_static<32><<<1, kNoAllocThreads, smem, s>>>(t, lines, line_width, k, scratch, d_kmers, d_counts, d_summary);
+  if (c <= 1) k_count_small_static<1><<<1, kNoAllocThreads, smem, s>>>(t, lines, line_width, k, d_kmers, d_counts, d_summary);
+  else if (c <= 2) k_count_small_static<2><<<1, kNoAllocThreads, smem, s>>>(t, lines, line_width, k, d_kmers, d_counts, d_summary);
+  else if (c <= 4) k_count_small_static<4><<<1, kNoAllocThreads, smem, s>>>(t, lines, line_width, k, d_kmers, d_counts, d_summary);
+  else if (c <= 5) k_count_small_static<5><<<1, kNoAllocThreads, smem, s>>>(t, lines, line_width, k, d_kmers, d_counts, d_summary);
+  else if (c <= 8) k_count_small_static<8><<<1, kNoAllocThreads, smem, s>>>(t, lines, line_width, k, d_kmers, d_counts, d_summary);
+  else if (c <= 16) k_count_small_static<16><<<1, kNoAllocThreads, smem, s>>>(t, lines, line_width, k, d_kmers, d_counts, d_summary);
+  else k_count_small_static<32><<<1, kNoAllocThreads, smem, s>>>(t, lines, line_width, k, d_kmers, d_counts, d_summary);
   if (cudaGetLastError() != cudaSuccess) return DK_ERR_CUDA;
   return DK_OK;
 }

@@ -302,18 +302,16 @@ int dk_serve_stop(dk_ctx* ctx);  /* finishes queued jobs, joins the workers */
  * memory, at least `capacity` entries) and d_summary (device memory, 3
  * uint64: distinct k-mers, k-mer occurrences, status 0 = ok).  The call is
  * asynchronous on `stream` (a cudaStream_t, NULL for the default stream) on
- * the current device and allocates nothing: its only scratch is one fixed
- * array of 147,712 bytes that the library reserves on every GPU that loads
- * it, until the process exits.
+ * the current device and allocates nothing; it has no scratch memory either
+ * (the unsorted k-mers wait in d_kmers, the rest stays in shared memory).
  *   - Inputs whose k-mer upper bound, lines * (line_width - k + 1), exceeds
  *     12,288 are rejected with DK_ERR_ADMISSION before any launch;
  *     capacity must be at least that bound (else DK_ERR_INVALID_ARG).
- *   - Every call shares the scratch array and leaves its contents behind;
- *     calls whose kernels overlap on the GPU (different streams or threads)
- *     race on it: serialise them on one stream.
- *   - The first call on a device does a one-time set-up (it looks up the
- *     array's device address and sets the kernel's shared-memory limit);
- *     make that first call before any stream capture on that device.
+ *   - Calls share no device memory: calls on different streams or threads
+ *     may overlap, each with its own buffers.
+ *   - The first call on a device does a one-time set-up (it sets the
+ *     kernel's shared-memory limit); make that first call before any stream
+ *     capture on that device.
  * Results equal dk_count's table for the same reads. */
 int dk_count_small_noalloc(const char* d_text, uint64_t nbytes, int line_width, int k,
                            uint64_t* d_kmers, uint32_t* d_counts, uint64_t capacity,

@@ -2,10 +2,11 @@
 
 It serves callers that cannot allocate device memory when they need a
 count (allocator callbacks, latency-bound serving loops, programs that own all
-device memory through their own pool).  Its only scratch is a fixed array in
-the library, shared by every call, so this file checks that two calls in a
-row -- the second on a smaller input, over the first call's leftovers --
-each give exactly dk_count's table, and that oversized inputs are rejected.
+device memory through their own pool).  It has no scratch memory: the
+unsorted k-mers wait in the caller's k-mer array.  This file checks that two
+calls in a row -- the second on a smaller input -- each give exactly
+dk_count's table, that two calls on different streams with their own buffers
+may overlap, and that oversized inputs are rejected.
 The file is named to be collected last; it also passes alone in a fresh
 process.
 """
@@ -76,3 +77,35 @@ def test_noalloc_rejects_oversized_input(lib):
     text = synth.random_lines(3, lines, W)
     rc, _ = _noalloc(lib, text, W, k)
     assert rc == dk.DK_ERR_ADMISSION
+
+
+def test_noalloc_calls_on_two_streams_overlap(lib, engine):
+    """Two calls launched back to back on two streams, each with its own
+    buffers, may run at the same time: each table equals dk_count's."""
+    import torch
+    g = synth.genome_uniform(51, 5000)
+    W, k = 150, 31
+    texts = [synth.reads(52 + i, g, 90, 100, W, W, rc_frac=0.5, err_rate=0.02) for i in range(2)]
+    runs = []
+    for text in texts:
+        d_text = torch.from_numpy(np.concatenate([text, np.zeros(64, np.uint8)])).cuda()
+        lines = (text.size + 1) // (W + 1)
+        cap = max(1, lines * (W - k + 1))
+        runs.append((text, d_text, cap, torch.empty(cap, dtype=torch.int64, device="cuda"),
+                     torch.empty(cap, dtype=torch.int32, device="cuda"),
+                     torch.full((3,), -1, dtype=torch.int64, device="cuda"), torch.cuda.Stream()))
+    torch.cuda.synchronize()
+    for text, d_text, cap, out_k, out_c, summ, st in runs:
+        rc = lib.dk_count_small_noalloc(
+            ctypes.c_void_p(d_text.data_ptr()), ctypes.c_uint64(text.size), W, k,
+            ctypes.c_void_p(out_k.data_ptr()), ctypes.c_void_p(out_c.data_ptr()),
+            ctypes.c_uint64(cap), ctypes.c_void_p(summ.data_ptr()), ctypes.c_void_p(st.cuda_stream))
+        assert rc == dk.DK_OK
+    torch.cuda.synchronize()
+    for text, d_text, cap, out_k, out_c, summ, st in runs:
+        s = summ.cpu().numpy()
+        nd = int(s[0])
+        ref = engine.count(text, W, k, dk.VARIANT_SORT)
+        assert int(s[2]) == 0 and int(s[1]) == ref.n_kmers
+        assert np.array_equal(out_k[:nd].cpu().numpy().view(np.uint64), ref.kmers)
+        assert np.array_equal(out_c[:nd].cpu().numpy().view(np.uint32), ref.counts)
