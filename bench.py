@@ -170,7 +170,8 @@ def make_workload(name: str, scale: float):
 
 
 def cpu_sample(rs, cap_reads: int):
-    n = min(rs.n_lines, cap_reads)
+    """The reads the CPU counts: all of them (cap_reads <= 0), else the first cap_reads."""
+    n = rs.n_lines if cap_reads <= 0 else min(rs.n_lines, cap_reads)
     return rs.text[: n * (rs.line_width + 1)], n
 
 
@@ -184,10 +185,24 @@ def run_cpu(rs, cap_reads: int, steps: int, warmup: int, threads: int):
         if i >= warmup:
             times.append(secs)
     t = float(np.mean(times))
+    what = "all" if n == rs.n_lines else f"first {n:,} of"
     return {"value": nk / t, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"first {n:,} of {rs.n_lines:,} reads ({nk:,} k-mers), {threads} PEs as "
+            "sample": f"{what} {rs.n_lines:,} reads ({nk:,} k-mers), {threads} PEs as "
                       f"threads, phase 1 + phase 2 as DAKC times them, mean of {steps}",
-            "seconds": t}
+            "seconds": t, "seconds_all": [round(x, 4) for x in times],
+            "same_config": n == rs.n_lines, "reads": n}
+
+
+def cpu_reads_for(rs, requested: int, runs: int, budget_s: float = 300.0,
+                  kmers_per_s: float = 4.0e8) -> int:
+    """Reads per CPU step: the whole workload (the same configuration as the
+    GPU arm) unless `runs` passes over it would take longer than `budget_s`
+    at a conservative `kmers_per_s`; then the largest prefix that fits."""
+    if requested > 0:
+        return requested
+    per_read = max(1, rs.line_width - rs.k + 1)
+    fit = int(budget_s * kmers_per_s / max(1, runs) / per_read)
+    return 0 if fit >= rs.n_lines else max(1, fit)
 
 
 def job_pool(n: int, seed: int = 4):
@@ -412,8 +427,11 @@ def main():
     ap.add_argument("--variant", default="auto", choices=["auto", "sort", "hash"])
     ap.add_argument("--l1-bits", type=int, default=0, help="level-1 partition bits (0 = auto)")
     ap.add_argument("--bin-target", type=int, default=0, help="keys per bin (0 = auto)")
-    ap.add_argument("--cpu-reads", type=int, default=4_000_000,
-                    help="reads in the CPU baseline's bounded sample")
+    ap.add_argument("--cpu-reads", type=int, default=0,
+                    help="reads per CPU step (0 = all reads of the workload, the GPU arm's "
+                         "configuration, unless that would not finish within about 5 minutes)")
+    ap.add_argument("--cpu-steps", type=int, default=3,
+                    help="timed runs of the CPU baseline leg in the engine's line")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-autotune", action="store_true",
                     help="count with the automatic parameters instead of the autotuned ones")
@@ -461,14 +479,16 @@ def main():
             return 0
         rs, cfg = make_workload(args.workload, args.scale)
         threads = os.cpu_count() or 1
-        cb = run_cpu(rs, args.cpu_reads, args.steps, args.warmup, threads)
+        reads = cpu_reads_for(rs, args.cpu_reads, args.steps + args.warmup)
+        cb = run_cpu(rs, reads, args.steps, args.warmup, threads)
         line = {"metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": args.gpus,
                 "steps": args.steps, "warmup": args.warmup,
                 "ms_per_step": cb["seconds"] * 1000.0, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic",
-                "config": dict(cfg, sample_reads=min(rs.n_lines, args.cpu_reads)),
+                "config": dict(cfg, sample_reads=cb["reads"], same_config=cb["same_config"]),
                 "impl": "reference",
-                "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
+                "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample",
+                                                    "same_config", "seconds_all")},
                 "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0,
                         "d2h_bytes_per_step": 0}}
         print(json.dumps(line), flush=True)
@@ -486,7 +506,8 @@ def main():
     # CPU baseline first (rank 0, N=1 only), before the GPU is busy
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        cpu = run_cpu(rs, args.cpu_reads, 1, 0, os.cpu_count() or 1)
+        cpu = run_cpu(rs, cpu_reads_for(rs, args.cpu_reads, args.cpu_steps), args.cpu_steps, 0,
+                      os.cpu_count() or 1)
 
     eng = dk.Engine(local)
     d_text = torch.empty(nbytes + 64, dtype=torch.uint8, device=f"cuda:{local}")
@@ -579,6 +600,8 @@ def main():
         w = float(np.mean(walls))
         e2e = {"value": nk / w, "unit": UNIT, "h2d_bytes_per_step": nbytes,
                "d2h_bytes_per_step": n_out * 12, "ms_per_step": w * 1000.0,
+               "ms_median": float(np.median(walls)) * 1000.0,
+               "value_median": nk / float(np.median(walls)),
                "ms_h2d": st["ms_h2d"], "ms_d2h": st["ms_d2h"],
                "walls_ms": [round(x * 1000.0, 2) for x in walls],
                "device_h2d_d2h_ms": parts}
@@ -622,7 +645,8 @@ def main():
             "wall_ms_per_step": (w1 - w0) * 1000.0 / args.steps,
             "clocks": clk,
             "e2e": e2e,
-            "cpu_baseline": ({k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")}
+            "cpu_baseline": ({k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample",
+                                                  "same_config", "seconds_all")}
                              if cpu else None),
             "forms": forms,
         }

@@ -17,9 +17,13 @@
  *   dakc/src/kcounter/kcounter.cpp:385-414       sort + run-length (HITTER=0)
  *   dakc/src/fqreader/fqreader.cpp:43-52         per-PE line split
  *
- * Two entry points:
+ * Three entry points:
  *   dko_count       single-threaded: extract -> LSD radix sort -> RLE.  The
  *                   plain checker.
+ *   dko_count_mt    the same table on T host threads for inputs of billions of
+ *                   k-mers: the key space is cut into ranges by its top bits,
+ *                   and each range is sorted and run-length reduced on its own
+ *                   (the ranges' tables, in range order, are the sorted table).
  *   dko_dakc_port   DAKC's two phases on P host threads: phase 1 parses each
  *                   PE's line range and routes every k-mer to
  *                   MurmurHash64A(kmer) % P; phase 2 sorts and run-length
@@ -39,6 +43,7 @@
 #include <string.h>
 #include <pthread.h>
 #include <time.h>
+#include <unistd.h>
 
 #include "dk_oracle.h"
 
@@ -329,4 +334,147 @@ int dko_dakc_port(const char* text, uint64_t nbytes, int line_width, int k, int 
   pthread_barrier_destroy(&bar);
   free(args); free(th); free(send); free(send_n); free(tab_k); free(tab_c); free(tab_n);
   return overflow ? DKO_ERR_OVERFLOW : 0;
+}
+
+/* ------------------------------------------------ range-parallel checker */
+/* dko_count's table on T threads.  Thread t extracts the k-mers of its share
+ * of the lines and histograms them by range (the top B key bits); the keys are
+ * then scattered into one array grouped by range; each range is radix sorted
+ * on its free bits and run-length reduced in place (kcounter.cpp:385-414's
+ * sort + run-length per range); the ranges' tables are concatenated in range
+ * order.  Independent of the engine's partition and hashing. */
+typedef struct {
+  const char* text; int W, k, T, B; uint64_t lines;
+  uint64_t** local; uint64_t* local_n;   /* [T] extracted keys */
+  uint64_t* hist;                         /* [T * R] keys per (thread, range) */
+  uint64_t* rbase;                        /* [R + 1] range starts */
+  uint64_t* rdist;                        /* [R] distinct keys per range */
+  uint64_t* all; uint64_t* tmp;           /* [n] grouped keys, scratch */
+  uint64_t* out_k; uint32_t* out_c;       /* [distinct] */
+  uint64_t* dbase;                        /* [R + 1] output starts */
+  uint64_t next_range;                    /* work counter (phase C) */
+  pthread_mutex_t mu;
+  pthread_barrier_t bar;
+  int overflow;
+  int fail;
+} mt_shared;
+
+typedef struct { mt_shared* s; int t; } mt_arg;
+
+static int mt_take_range(mt_shared* s) {
+  pthread_mutex_lock(&s->mu);
+  const uint64_t r = s->next_range++;
+  pthread_mutex_unlock(&s->mu);
+  return (int)r;
+}
+
+static void* mt_worker(void* vp) {
+  mt_arg* a = (mt_arg*)vp;
+  mt_shared* s = a->s;
+  const int t = a->t, T = s->T, R = 1 << s->B, sh = 2 * s->k - s->B;
+  /* A: extract and histogram this thread's lines */
+  const uint64_t l0 = s->lines * (uint64_t)t / (uint64_t)T;
+  const uint64_t l1 = s->lines * (uint64_t)(t + 1) / (uint64_t)T;
+  const uint64_t n = dko_extract_lines(s->text, s->W, s->k, l0, l1, NULL);
+  uint64_t* mine = (uint64_t*)malloc(sizeof(uint64_t) * (n ? n : 1));
+  if (!mine) s->fail = 1;
+  else dko_extract_lines(s->text, s->W, s->k, l0, l1, mine);
+  s->local[t] = mine; s->local_n[t] = mine ? n : 0;
+  uint64_t* h = s->hist + (size_t)t * R;
+  for (uint64_t i = 0; i < s->local_n[t]; ++i) h[mine[i] >> sh]++;
+  pthread_barrier_wait(&s->bar);
+  if (t == 0) {  /* range starts, and each thread's cursor per range */
+    uint64_t run = 0;
+    for (int r = 0; r < R; ++r) {
+      s->rbase[r] = run;
+      for (int u = 0; u < T; ++u) {
+        const uint64_t c = s->hist[(size_t)u * R + r];
+        s->hist[(size_t)u * R + r] = run;
+        run += c;
+      }
+    }
+    s->rbase[R] = run;
+    s->all = (uint64_t*)malloc(sizeof(uint64_t) * (run ? run : 1));
+    s->tmp = (uint64_t*)malloc(sizeof(uint64_t) * (run ? run : 1));
+    if (!s->all || !s->tmp) s->fail = 1;
+  }
+  pthread_barrier_wait(&s->bar);
+  /* B: scatter into the grouped array */
+  if (!s->fail)
+    for (uint64_t i = 0; i < s->local_n[t]; ++i) s->all[h[mine[i] >> sh]++] = mine[i];
+  free(mine);
+  s->local[t] = NULL;
+  pthread_barrier_wait(&s->bar);
+  /* C: sort and run-length reduce each range in place (distinct keys at the
+   * range's start in all[], counts at its start in tmp[] viewed as u32) */
+  for (int r; !s->fail && (r = mt_take_range(s)) < R;) {
+    const uint64_t b = s->rbase[r], m = s->rbase[r + 1] - b;
+    radix_sort_u64(s->all + b, s->tmp + b, m, sh);
+    int ovf = 0;
+    s->rdist[r] = rle(s->all + b, m, s->all + b, (uint32_t*)(s->tmp + b), &ovf);
+    if (ovf) s->overflow = 1;
+  }
+  pthread_barrier_wait(&s->bar);
+  if (t == 0 && !s->fail) {
+    uint64_t run = 0;
+    for (int r = 0; r < R; ++r) { s->dbase[r] = run; run += s->rdist[r]; }
+    s->dbase[R] = run;
+    s->out_k = (uint64_t*)malloc(sizeof(uint64_t) * (run ? run : 1));
+    s->out_c = (uint32_t*)malloc(sizeof(uint32_t) * (run ? run : 1));
+    if (!s->out_k || !s->out_c) s->fail = 1;
+  }
+  pthread_barrier_wait(&s->bar);
+  /* D: concatenate the ranges' tables (ranges split evenly over threads) */
+  if (!s->fail)
+    for (int r = t; r < R; r += T) {
+      const uint64_t b = s->rbase[r], d = s->rdist[r], o = s->dbase[r];
+      memcpy(s->out_k + o, s->all + b, sizeof(uint64_t) * d);
+      memcpy(s->out_c + o, (const uint32_t*)(s->tmp + b), sizeof(uint32_t) * d);
+    }
+  return NULL;
+}
+
+int dko_count_mt(const char* text, uint64_t nbytes, int line_width, int k, int threads,
+                 dko_table* out) {
+  memset(out, 0, sizeof(*out));
+  int64_t lines;
+  int rc = check_args(text, nbytes, line_width, k, &lines);
+  if (rc) return rc;
+  int T = threads;
+  if (T < 1) T = (int)sysconf(_SC_NPROCESSORS_ONLN);
+  if (T < 1) T = 1;
+  mt_shared s;
+  memset(&s, 0, sizeof(s));
+  s.text = text; s.W = line_width; s.k = k; s.T = T; s.lines = (uint64_t)lines;
+  s.B = 2 * k < 12 ? 2 * k : 12;
+  const int R = 1 << s.B;
+  s.local = (uint64_t**)calloc((size_t)T, sizeof(uint64_t*));
+  s.local_n = (uint64_t*)calloc((size_t)T, sizeof(uint64_t));
+  s.hist = (uint64_t*)calloc((size_t)T * R, sizeof(uint64_t));
+  s.rbase = (uint64_t*)calloc((size_t)R + 1, sizeof(uint64_t));
+  s.rdist = (uint64_t*)calloc((size_t)R, sizeof(uint64_t));
+  s.dbase = (uint64_t*)calloc((size_t)R + 1, sizeof(uint64_t));
+  pthread_mutex_init(&s.mu, NULL);
+  pthread_barrier_init(&s.bar, NULL, (unsigned)T);
+  pthread_t* th = (pthread_t*)calloc((size_t)T, sizeof(pthread_t));
+  mt_arg* args = (mt_arg*)calloc((size_t)T, sizeof(mt_arg));
+  for (int t = 0; t < T; ++t) {
+    args[t].s = &s; args[t].t = t;
+    pthread_create(&th[t], NULL, mt_worker, &args[t]);
+  }
+  for (int t = 0; t < T; ++t) pthread_join(th[t], NULL);
+  if (s.fail) {
+    free(s.out_k); free(s.out_c);
+    rc = DKO_ERR_ARG;
+  } else {
+    out->kmers = s.out_k; out->counts = s.out_c; out->n = s.dbase[R];
+    out->n_kmers = s.rbase[R];
+    rc = s.overflow ? DKO_ERR_OVERFLOW : 0;
+  }
+  free(s.all); free(s.tmp);
+  pthread_barrier_destroy(&s.bar);
+  pthread_mutex_destroy(&s.mu);
+  free(s.local); free(s.local_n); free(s.hist); free(s.rbase); free(s.rdist); free(s.dbase);
+  free(th); free(args);
+  return rc;
 }

@@ -23,6 +23,8 @@ uint64_t dko_extract_lines(const char* text, int line_width, int k, uint64_t l0,
                            uint64_t* out);
 uint64_t dko_murmur64a(uint64_t key, uint64_t seed);
 int dko_count(const char* text, uint64_t nbytes, int line_width, int k, dko_table* out);
+int dko_count_mt(const char* text, uint64_t nbytes, int line_width, int k, int threads,
+                 dko_table* out);
 int dko_dakc_port(const char* text, uint64_t nbytes, int line_width, int k, int pes, int merge,
                   dko_table* out, double* seconds);
 void dko_free(dko_table* t);

@@ -6,6 +6,9 @@ never calls it.
 
 * ``count``      -- dk_oracle.c's single-threaded restatement (extract, LSD
                     radix sort, run-length), the parity checker.
+* ``count_mt``   -- the same table on T host threads (key ranges sorted and
+                    run-length reduced independently), the checker for inputs
+                    of billions of k-mers.
 * ``dakc_port``  -- DAKC's two phases on P host threads (owner hash
                     MurmurHash64A % P, per-owner sort + run-length), timed as
                     the CPU baseline.
@@ -51,6 +54,7 @@ def _load():
         lib = ctypes.CDLL(LIB)
         vp, u64, i32 = ctypes.c_void_p, ctypes.c_uint64, ctypes.c_int
         lib.dko_count.argtypes = [vp, u64, i32, i32, ctypes.POINTER(_Table)]
+        lib.dko_count_mt.argtypes = [vp, u64, i32, i32, i32, ctypes.POINTER(_Table)]
         lib.dko_dakc_port.argtypes = [vp, u64, i32, i32, i32, i32, ctypes.POINTER(_Table),
                                       ctypes.POINTER(ctypes.c_double)]
         lib.dko_free.argtypes = [ctypes.POINTER(_Table)]
@@ -93,6 +97,23 @@ def count(text, line_width: int, k: int):
     try:
         if rc == -1:
             raise OracleError("invalid arguments")
+        out = _take(t)
+        if rc == -2:
+            raise OracleError("count overflows 32 bits")
+        return out
+    finally:
+        lib.dko_free(ctypes.byref(t))
+
+
+def count_mt(text, line_width: int, k: int, threads: int = 0):
+    """(keys, counts, n_kmers) of ``count`` on `threads` host threads (0 = all)."""
+    buf = _as_bytes(text)
+    lib = _load()
+    t = _Table()
+    rc = lib.dko_count_mt(buf.ctypes.data, buf.size, line_width, k, threads, ctypes.byref(t))
+    try:
+        if rc == -1:
+            raise OracleError("invalid arguments or out of host memory")
         out = _take(t)
         if rc == -2:
             raise OracleError("count overflows 32 bits")

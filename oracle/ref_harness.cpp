@@ -23,6 +23,7 @@
 #include <cstdint>
 #include <string>
 #include <vector>
+#include <algorithm>
 #include <unistd.h>
 #include <sys/wait.h>
 
@@ -59,6 +60,8 @@ static int run_pe(const std::vector<char>& file, int pe, int P, const std::strin
       if (i > 0 && h[i].kmer <= h[i - 1].kmer) break;
       rows.emplace_back(h[i].kmer, h[i].count);
     }
+    // the PE's table is the union of its light and heavy tables (each sorted)
+    std::sort(rows.begin(), rows.end());
 #endif
   }
   std::free(chunk);

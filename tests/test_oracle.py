@@ -53,14 +53,81 @@ def test_port_matches_reference_fixture(path):
         assert gn == nk and np.array_equal(gk, keys) and np.array_equal(gc, counts)
 
 
+@pytest.mark.parametrize("path", FIXTURES, ids=[os.path.basename(p)[:-4] for p in FIXTURES])
+def test_count_mt_matches_reference_fixture(path):
+    """The range-parallel checker (used at config size) reproduces every
+    reference table, for several thread counts."""
+    text, W, k, keys, counts, nk = load(path)
+    for threads in (1, 3, 8):
+        gk, gc, gn = pyoracle.count_mt(text, W, k, threads)
+        assert gn == nk and np.array_equal(gk, keys) and np.array_equal(gc, counts)
+
+
+def test_count_mt_equals_count_random():
+    text = synth.random_lines(12, 4000, 100, b"ACGTACGTACGTN")
+    for k in (1, 5, 6, 7, 13, 31, 32):
+        ref = pyoracle.count(text, 100, k)
+        got = pyoracle.count_mt(text, 100, k, 5)
+        assert got[2] == ref[2] and np.array_equal(got[0], ref[0]) and np.array_equal(got[1], ref[1])
+    assert pyoracle.count_mt(b"", 10, 4)[2] == 0
+
+
 def test_plain_1m_digest():
     with open(os.path.join(GOLDEN, "index.json")) as f:
         ent = json.load(f)["cases"]["plain_1m"]
     rs = synth.plain_1m()
     assert hashlib.sha256(rs.text.tobytes()).hexdigest() == ent["text_sha256"]
-    keys, counts, nk = pyoracle.count(rs.text, 150, 31)
-    assert nk == ent["n_kmers"] and keys.size == ent["n_distinct"]
-    assert hashlib.sha256(keys.tobytes() + counts.tobytes()).hexdigest() == ent["table_sha256"]
+    for keys, counts, nk in (pyoracle.count(rs.text, 150, 31), pyoracle.count_mt(rs.text, 150, 31)):
+        assert nk == ent["n_kmers"] and keys.size == ent["n_distinct"]
+        assert hashlib.sha256(keys.tobytes() + counts.tobytes()).hexdigest() == ent["table_sha256"]
+
+
+def _with_one_more_zero(keys, counts):
+    """The table plus one occurrence of k-mer 0."""
+    keys = [int(x) for x in keys]
+    counts = [int(x) for x in counts]
+    if keys and keys[0] == 0:
+        counts[0] += 1
+    else:
+        keys.insert(0, 0)
+        counts.insert(0, 1)
+    return keys, counts
+
+
+def test_hitter1_record():
+    """The reference built with HITTER=1 (the header default,
+    common.hpp:42-44) gives the HITTER=0 table on every golden input but one.
+    In edge_w20_k1 every k-mer of the PE reaches it as a heavy (k-mer, count)
+    pair, so its light vector is empty; phase 2 still starts its run-length
+    pass at element 0 of that vector (kcounter.cpp:334, 368-377) and counts one
+    occurrence of k-mer 0.  The engine follows the HITTER=0 table."""
+    with open(os.path.join(GOLDEN, "hitter1.json")) as f:
+        rec = json.load(f)["cases"]
+    assert set(rec) == {os.path.basename(p)[:-4] for p in FIXTURES}
+    differing = []
+    for name, runs in rec.items():
+        text, W, k, keys, counts, nk = load(os.path.join(GOLDEN, name + ".npz"))
+        for p, ent in runs.items():
+            if ent["equals_hitter0"]:
+                assert ent["table_sha256"] == hashlib.sha256(keys.tobytes() + counts.tobytes()).hexdigest()
+                assert ent["n_kmers"] == nk
+            else:
+                differing.append(name)
+                assert (ent["keys"], ent["counts"]) == _with_one_more_zero(keys, counts)
+                assert ent["n_kmers"] == nk + 1
+    assert differing == ["edge_w20_k1"]
+
+
+@pytest.mark.skipif(not os.path.isdir(pyoracle.REFERENCE_TREE), reason="reference tree absent")
+@pytest.mark.parametrize("name", ["reads_w150_k31", "skew_w150_k31", "edge_w20_k1"])
+def test_hitter1_live(name):
+    text, W, k, keys, counts, nk = load(os.path.join(GOLDEN, name + ".npz"))
+    with open(os.path.join(GOLDEN, "hitter1.json")) as f:
+        runs = json.load(f)["cases"][name]
+    for p, ent in runs.items():
+        (hk, hc, hn), _ = pyoracle.ref_table(text, W, k, pes=int(p), hitter=1)
+        assert hashlib.sha256(hk.tobytes() + hc.tobytes()).hexdigest() == ent["table_sha256"]
+        assert hn == ent["n_kmers"]
 
 
 def test_known_answers():
