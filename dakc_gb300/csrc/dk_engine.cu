@@ -950,7 +950,10 @@ int Engine::count_device(const uint8_t* d_text, uint64_t nbytes, const dk_input_
   // than a bin is counted whole by one hash bin; one that turns out to hold
   // too many distinct keys is re-partitioned through a proxy child and the
   // levels resume from the proxies (a pass per round of such bins).
-  const int big_ok = use_hash ? 1 : 0;
+  // the sort variant still counts a hot node of 2^31 keys or more as one hash
+  // bin: splitting it would take many levels over all its keys, and near 2^32
+  // keys the partition's 32-bit per-child offsets cannot hold it
+  const int big_ok = use_hash ? 1 : (k <= 31 ? 2 : 0);
   uint32_t node_end = (uint32_t)F1;  // nodes [0, node_end) exist
   uint32_t n_final = 0;              // final nodes listed so far (all groups)
   uint32_t n_bigf = 0;               // big-bin final nodes listed so far

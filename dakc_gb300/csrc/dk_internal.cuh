@@ -137,7 +137,8 @@ int launch_l1_scatter(const ExtractArgs& a, int grid, const uint64_t* O, uint64_
                       unsigned long long* counters, cudaStream_t s);
 // split nodes get a digit width that makes their children ~split_target/2 keys
 // big_ok: a skewed node (it kept most of its parent's keys: a hot k-mer) larger
-// than a bin becomes a final hash bin instead of splitting again
+// than a bin becomes a final hash bin instead of splitting again (big_ok 2:
+// only a node of 2^31 keys or more)
 // (big bins go to big_list: the bin count takes them first, so that one
 // CTA's long pass over a hot k-mer overlaps the other bins)
 // (level-1 nodes of several ranges always split: a final bin's keys are one range)

@@ -257,7 +257,8 @@ __global__ void k_l1_starts(Node* nodes, int F1, int shift1, const int16_t* buck
   const int lo = min(F1, (int)threadIdx.x * per), hi = min(F1, lo + per);
   unsigned long long s = 0;
   for (int i = lo; i < hi; ++i) s += nodes[i].n;
-  unsigned long long base = block_excl_scan<unsigned long long>(s, tmp, nullptr);
+  unsigned long long total = 0;
+  unsigned long long base = block_excl_scan<unsigned long long>(s, tmp, &total);
   for (int i = lo; i < hi; ++i) {
     Node& nd = nodes[i];
     nd.start = base;
@@ -272,7 +273,9 @@ __global__ void k_l1_starts(Node* nodes, int F1, int shift1, const int16_t* buck
     nd.ntiles = 0;
     nd.th_base = 0;
     nd.width = 0;
-    nd.skewed = 0;
+    // most of all keys and too many for the partition's 32-bit offsets once
+    // split: a hot k-mer, counted whole by a big hash bin
+    nd.skewed = nd.n * 2 > total && nd.n >= (1ull << 31);
   }
 }
 
@@ -840,9 +843,12 @@ __global__ void k_classify(Node* nodes, uint32_t lo, uint32_t hi, uint32_t* fina
   // while one hash bin streams any number of copies (it is re-partitioned if
   // it holds too many distinct keys).  A node of several ranges splits (into
   // one range per child) whatever its size.
+  // big_ok 1: any such node; big_ok 2: only one of 2^31 keys or more (its
+  // split would need as many partition levels, each over all its keys, and
+  // near 2^32 the partition's 32-bit per-child offsets)
   if (!multi_range(rg, i) &&
       (nd.n <= (uint64_t)bin_cap || nd.shift <= kDenseBits ||
-       (big_ok && nd.skewed && nd.n < (1ull << 31)))) {
+       (big_ok && nd.skewed && (big_ok == 1 || nd.n >= (1ull << 31))))) {
     nodes[i].state = NODE_FINAL;
     if (nd.n > (uint64_t)bin_cap && nd.shift > kDenseBits)
       big_list[atomicAdd(&ctr->n_big_final, 1u)] = i;
@@ -1545,12 +1551,13 @@ constexpr uint32_t kRankMax = 256;  // longer digit ranges are sorted by a warp
 // kHashMaxProbe slots or the bin holds more than kHashMaxDistinct keys.
 __device__ bool bin_hashed(Node* nodes, uint32_t ni, const Node& nd, uint64_t* keys, uint32_t* cnt,
                            unsigned long long* region, uint32_t* hist, uint32_t* tmp,
-                           uint32_t* mark, uint32_t* flags, bool hot) {
+                           uint32_t* mark, uint32_t* flags, bool hot,
+                           unsigned long long* overflow) {
   unsigned long long* tk = region;                                  // kHashSlots keys
   uint32_t* tc = reinterpret_cast<uint32_t*>(tk + kHashSlots);       // kHashSlots counts
   unsigned long long* sk = reinterpret_cast<unsigned long long*>(tc + kHashSlots);  // by digit
   uint32_t* sc = reinterpret_cast<uint32_t*>(sk + kHashMaxDistinct);
-  const uint32_t n = (uint32_t)nd.n;
+  const uint64_t n = nd.n;  // a big bin may hold 2^32 keys or more
   const uint32_t T = blockDim.x;
   DK_PHASE_BEGIN();
   // digits: the top D free bits, about n / 8 of them (ranks within a digit
@@ -1578,19 +1585,19 @@ __device__ bool bin_hashed(Node* nodes, uint32_t ni, const Node& nd, uint64_t* k
   // trip (bin count 23.2 ms on 2.4 G k-mers, against 23.6 ms with 8, 23.3
   // with 10 and 23.4 with 16)
   constexpr int kBatch = 12;
-  for (uint32_t i0 = 0; i0 < n; i0 += kBatch * T) {
+  for (uint64_t i0 = 0; i0 < n; i0 += (uint64_t)kBatch * T) {
     // a failed table stops the pass early (a large bin would otherwise probe
     // the full table for every remaining key); warp-uniform exit
     if (__any_sync(0xFFFFFFFFu, *reinterpret_cast<volatile uint32_t*>(&flags[1]) != 0)) break;
     unsigned long long kk[kBatch];
 #pragma unroll
     for (int u = 0; u < kBatch; ++u) {
-      const uint32_t i = i0 + (uint32_t)u * T + threadIdx.x;
+      const uint64_t i = i0 + (uint64_t)u * T + threadIdx.x;
       kk[u] = i < n ? __ldg(keys + i) : kEmptyKey;
     }
 #pragma unroll
     for (int u = 0; u < kBatch; ++u) {
-      if (i0 + (uint32_t)u * T >= n) break;  // uniform: no lane has a key from here on
+      if (i0 + (uint64_t)u * T >= n) break;  // uniform: no lane has a key from here on
       const unsigned long long key = kk[u];
       bool live = key != kEmptyKey;
       uint32_t mult = 1;
@@ -1608,7 +1615,7 @@ __device__ bool bin_hashed(Node* nodes, uint32_t ni, const Node& nd, uint64_t* k
         }
         const unsigned long long prev = atomicCAS(&tk[slot], kEmptyKey, key);
         if (prev == kEmptyKey || prev == key) {
-          atomicAdd(&tc[slot], mult);
+          if (atomicAdd(&tc[slot], mult) > 0xFFFFFFFFu - mult) atomicMax(overflow, 1ull);
           if (prev == kEmptyKey) atomicAdd(&hist[(uint32_t)(key >> sh) & M], 1u);
           break;
         }
@@ -1678,6 +1685,176 @@ __device__ bool bin_hashed(Node* nodes, uint32_t ni, const Node& nd, uint64_t* k
   return true;
 }
 
+// ---- packed hash variant: one 64-bit word per distinct key
+// A bin's keys share their bits [s, 2k) (s = nd.shift free bits), so a key is
+// its low s bits.  Entry = (free bits << (64 - s)) | count: the free bits sit
+// at the top, the count (< 2^14 for a bin of at most kBinCap keys) at the
+// bottom.  Entries compare as the keys they hold, 0 is an empty slot, a new
+// key enters with one 64-bit CAS and a repeat adds to the low 32-bit word.
+constexpr int kPackSlotBits = 13;
+constexpr uint32_t kPackSlots = 1u << kPackSlotBits;     // 64 KB of table
+constexpr uint32_t kPackMaxProbe = 64;
+constexpr uint32_t kPackMaxDistinct = (kBinCap * 8 - kPackSlots * 8) / 8;  // sorted entries after the table
+constexpr int kPackMaxShift = 50;  // the count field keeps >= 14 bits
+// inside the two-CTA-per-SM bin kernel the packed table measured slower than
+// bin_hashed (C2 bin count 24.6 against 22.8 ms), so it is not selected there
+constexpr bool kPackInBinKernel = false;
+static_assert(kBinCap < (1 << (64 - kPackMaxShift)), "a bin's largest count fits the count field");
+static_assert(kPackSlots * 8 + kPackMaxDistinct * 8 <= kBinCap * 8, "table and sorted entries fit");
+static_assert(kPackMaxDistinct * 12 <= kPackSlots * 8, "the output stage fits the table");
+static_assert(kPackSlots % (2 * kBinThreads) == 0, "slot loops");
+
+// Insert one key (rk = key << (64 - s)) with multiplicity mult; false when the
+// probe runs past kPackMaxProbe slots.
+__device__ __forceinline__ bool pack_insert(unsigned long long* tab, unsigned long long rk,
+                                            unsigned long long himask, uint32_t mult,
+                                            uint32_t* hist, int dsh) {
+  const uint32_t h = (uint32_t)(rk >> 32) ^ (uint32_t)rk;
+  uint32_t slot = (h * 0x9E3779B1u) >> (32 - kPackSlotBits);
+  for (uint32_t probe = 0; probe < kPackMaxProbe; ++probe) {
+    unsigned long long e = *reinterpret_cast<volatile unsigned long long*>(&tab[slot]);
+    if (e == 0ull) {
+      e = atomicCAS(&tab[slot], 0ull, rk | mult);
+      if (e == 0ull) {
+        atomicAdd(&hist[(uint32_t)(rk >> dsh)], 1u);
+        return true;
+      }
+    }
+    if ((e & himask) == rk) {
+      atomicAdd(reinterpret_cast<unsigned int*>(&tab[slot]), mult);  // the low word
+      return true;
+    }
+    slot = (slot + 1) & (kPackSlots - 1);
+  }
+  return false;
+}
+
+// A bin with at most kBinCap keys and kDenseBits < s <= kPackMaxShift free
+// bits: insert every key into a packed table, place the distinct entries by
+// their top D bits (counting sort), rank each inside its digit range, stage
+// the sorted (key, count) pairs in shared memory and write them to the bin's
+// region with coalesced stores.  Returns false, having written nothing, when
+// a probe runs too long or the bin holds more than kPackMaxDistinct keys.
+__device__ bool bin_packed(Node* nodes, uint32_t ni, const Node& nd, uint64_t* keys, uint32_t* cnt,
+                           unsigned long long* region, uint32_t* hist, uint32_t* tmp,
+                           uint32_t* mark, uint32_t* flags, bool hot) {
+  unsigned long long* tab = region;                  // kPackSlots entries
+  unsigned long long* sorted = region + kPackSlots;  // by digit
+  const uint32_t n = (uint32_t)nd.n;
+  const int s = nd.shift;
+  const int cbits = 64 - s;
+  const unsigned long long himask = ~((1ull << cbits) - 1ull);
+  const uint32_t cmask = cbits >= 32 ? 0xFFFFFFFFu : ((1u << cbits) - 1u);
+  int D = ceil_log2_u64(n) - 3;
+  D = max(4, min(D, kBinDigitBits));
+  D = min(D, s);
+  const int dsh = 64 - D;
+  const uint32_t R = 1u << D;
+  const uint64_t prefix = n ? (__ldg(keys) >> s) << s : 0ull;
+  DK_PHASE_BEGIN();
+  {
+    uint4* t4 = reinterpret_cast<uint4*>(tab);
+#pragma unroll
+    for (uint32_t u = 0; u < kPackSlots / 2 / kBinThreads; ++u)
+      t4[threadIdx.x + u * kBinThreads] = make_uint4(0u, 0u, 0u, 0u);
+  }
+  for (uint32_t j = threadIdx.x; j < R; j += kBinThreads) hist[j] = 0;
+  for (uint32_t w = threadIdx.x; w < (R + 31) / 32; w += kBinThreads) mark[w] = 0;
+  if (threadIdx.x == 0) flags[1] = 0;
+  __syncthreads();
+  DK_PHASE(11);
+  constexpr int kBatch = 8;
+  bool ok = true;
+  for (uint32_t i0 = 0; i0 < n; i0 += kBatch * kBinThreads) {
+    unsigned long long kk[kBatch];
+#pragma unroll
+    for (int u = 0; u < kBatch; ++u) {
+      const uint32_t i = i0 + (uint32_t)u * kBinThreads + threadIdx.x;
+      kk[u] = i < n ? __ldg(keys + i) : 0ull;
+    }
+#pragma unroll
+    for (int u = 0; u < kBatch; ++u) {
+      if (i0 + (uint32_t)u * kBinThreads >= n) break;  // uniform
+      const bool valid = i0 + (uint32_t)u * kBinThreads + threadIdx.x < n;
+      const unsigned long long rk = kk[u] << cbits;
+      uint32_t mult = 1;
+      bool live = valid;
+      if (hot) {  // copies of one key in this warp insert once with their multiplicity
+        const uint32_t vm = __ballot_sync(0xFFFFFFFFu, valid);
+        const uint32_t peers = __match_any_sync(0xFFFFFFFFu, rk) & vm;
+        live = valid && (int)lane_id() == __ffs(peers) - 1;
+        mult = (uint32_t)__popc(peers);
+      }
+      if (live && ok) ok = pack_insert(tab, rk, himask, mult, hist, dsh);
+    }
+  }
+  if (!ok) flags[1] = 1;
+  __syncthreads();
+  DK_PHASE(12);
+  if (flags[1]) return false;
+  const uint32_t d = block_scan_array<uint32_t>(hist, (int)R, tmp);  // distinct keys
+  if (d > kPackMaxDistinct) return false;  // uniform
+  DK_PHASE(13);
+  // place: hist[j] becomes the end of digit range j
+  {
+    const ulonglong2* t2 = reinterpret_cast<const ulonglong2*>(tab);
+#pragma unroll
+    for (uint32_t u = 0; u < kPackSlots / 2 / kBinThreads; ++u) {
+      const ulonglong2 e = t2[threadIdx.x + u * kBinThreads];
+      if (e.x) sorted[atomicAdd(&hist[(uint32_t)(e.x >> dsh)], 1u)] = e.x;
+      if (e.y) sorted[atomicAdd(&hist[(uint32_t)(e.y >> dsh)], 1u)] = e.y;
+    }
+  }
+  __syncthreads();
+  DK_PHASE(14);
+  // rank inside the digit range and stage the pair (the table is free now);
+  // ranges of more than kRankMax entries are marked for a warp sort
+  unsigned long long* ok_ = tab;                              // d keys
+  uint32_t* oc = reinterpret_cast<uint32_t*>(tab + d);        // d counts
+  for (uint32_t x = threadIdx.x; x < d; x += kBinThreads) {
+    const unsigned long long v = sorted[x];
+    const uint32_t j = (uint32_t)(v >> dsh);
+    const uint32_t lo = j ? hist[j - 1] : 0, hi = hist[j];
+    if (hi - lo > kRankMax) {
+      atomicOr(&mark[j >> 5], 1u << (j & 31));
+      continue;
+    }
+    uint32_t r = lo;
+    for (uint32_t y = lo; y < hi; ++y) r += sorted[y] < v;
+    ok_[r] = prefix | (v >> cbits);
+    oc[r] = (uint32_t)v & cmask;
+  }
+  __syncthreads();
+  DK_PHASE(15);
+  const uint32_t warp = threadIdx.x >> 5;
+  for (uint32_t w = warp; w < (R + 31) / 32; w += kBinThreads / 32) {
+    uint32_t bits = mark[w];
+    while (bits) {
+      const uint32_t j = w * 32 + (__ffs(bits) - 1);
+      bits &= bits - 1;
+      const uint32_t lo = j ? hist[j - 1] : 0, hi = hist[j];
+      warp_bitonic(sorted + lo, hi - lo);
+      for (uint32_t x = lo + lane_id(); x < hi; x += 32) {
+        const unsigned long long v = sorted[x];
+        ok_[x] = prefix | (v >> cbits);
+        oc[x] = (uint32_t)v & cmask;
+      }
+    }
+  }
+  __syncthreads();
+  DK_PHASE(16);
+  for (uint32_t x = threadIdx.x; x < d; x += kBinThreads) {
+    keys[x] = ok_[x];
+    cnt[x] = oc[x];
+  }
+  DK_PHASE(19);
+  DK_PHASE_ADD(23, 1);
+  DK_PHASE_ADD(27, n);
+  DK_PHASE_ADD(28, d);
+  if (threadIdx.x == 0) nodes[ni].d = d;
+  return true;
+}
+
 // Persistent bin counter: CTAs take final nodes from a ticket until none are
 // left.  Two CTAs fit per SM (96 KB keys + 16 KB histogram each).
 __device__ __forceinline__ uint32_t bin_at(const uint32_t* big, uint32_t n_big,
@@ -1736,7 +1913,8 @@ __global__ void __launch_bounds__(kBinThreads, kBinBlocksPerSM) k_bin_count(Node
     } else if (nd.n > (uint64_t)kBinCap) {
       // a large skewed bin: the hash bin streams its keys; with too many
       // distinct keys it is left, unwritten, for the host to re-partition
-      const bool done = bin_hashed(nodes, ni, nd, keys, cnt, skeys, hist, tmp, mark, hflags, hot);
+      const bool done = bin_hashed(nodes, ni, nd, keys, cnt, skeys, hist, tmp, mark, hflags, hot,
+                                   &ctr[5]);
       if (threadIdx.x == 0) {
         atomicAdd(&ctr[17], 1ull);
         if (!done) {
@@ -1746,8 +1924,12 @@ __global__ void __launch_bounds__(kBinThreads, kBinBlocksPerSM) k_bin_count(Node
       }
     } else {
       bool done = false;
-      if (use_hash) {
-        done = bin_hashed(nodes, ni, nd, keys, cnt, skeys, hist, tmp, mark, hflags, hot);
+      if (kPackInBinKernel && use_hash && nd.shift <= kPackMaxShift) {
+        done = bin_packed(nodes, ni, nd, keys, cnt, skeys, hist, tmp, mark, hflags, hot);
+        __syncthreads();
+      }
+      if (use_hash && !done) {
+        done = bin_hashed(nodes, ni, nd, keys, cnt, skeys, hist, tmp, mark, hflags, hot, &ctr[5]);
         if (!done && threadIdx.x == 0) atomicAdd(&ctr[6], 1ull);  // bins that fell back
         __syncthreads();
       }

@@ -273,6 +273,7 @@ int dk_cancel(dk_ctx* ctx, uint64_t ticket) {
     if ((*q)->ticket == ticket) {
       s->queue.erase(q);
       r->status = DK_ERR_CANCELLED;
+      s->cv_done.notify_all();  // a dk_wait on this ticket returns now
       return DK_OK;
     }
   if (r->status == DK_ERR_PENDING) {  // running: its table is dropped when the batch ends
@@ -294,6 +295,12 @@ int dk_serve_stop(dk_ctx* ctx) {
   s->cv_work.notify_all();
   for (auto& w : s->workers)
     if (w.th.joinable()) w.th.join();
+  // finished jobs whose tables nobody took go back to the pool
+  for (auto& kv : s->jobs) {
+    dk::Request& r = *kv.second;
+    if (r.status == DK_OK && r.table.handle) dk::serve_release(s, r.table.handle);
+  }
+  s->jobs.clear();
   dk::set_server(ctx, nullptr);
   delete s;
   return DK_OK;

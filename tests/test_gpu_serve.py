@@ -84,6 +84,52 @@ def test_cancelled_running_job_stays_pending_until_its_batch_ends():
         eng.serve_stop()
 
 
+def test_wait_on_a_queued_job_returns_when_it_is_cancelled():
+    """A thread blocked in dk_wait on a queued job wakes when another thread
+    cancels that job, and gets DK_ERR_CANCELLED (not a timeout)."""
+    import threading
+    big = synth.random_lines(6, 200_000, 250)     # keeps the one worker busy
+    queued = texts(1, 14)[0]
+    with dk.Engine(0) as eng:
+        eng.serve_start(workers=1, max_batch_jobs=1)
+        tk_big = eng.submit(big, 250, 31)
+        time.sleep(0.02)
+        tk = eng.submit(queued, 250, 31)
+        out = {}
+
+        def waiter():
+            t0 = time.perf_counter()
+            out["rc"] = eng.lib.dk_wait(eng.h, tk, 60_000, None, None)
+            out["s"] = time.perf_counter() - t0
+
+        th = threading.Thread(target=waiter)
+        th.start()
+        time.sleep(0.01)
+        c = eng.cancel(tk)
+        th.join(timeout=30)
+        assert not th.is_alive()
+        if c == dk.DK_OK:
+            assert out["rc"] in (dk.DK_ERR_CANCELLED, dk.DK_OK)
+        assert out["s"] < 30
+        eng.lib.dk_wait(eng.h, tk_big, 120_000, None, None)
+        eng.serve_stop()
+
+
+def test_serve_stop_releases_results_nobody_took():
+    """Finished jobs whose tables were never taken go back to the host pool
+    at dk_serve_stop; the context keeps counting afterwards."""
+    jobs = texts(4, 15)
+    with dk.Engine(0) as eng:
+        eng.serve_start(workers=2, max_batch_jobs=4)
+        for t in jobs:
+            eng.submit(t, 250, 31)
+        time.sleep(1.0)   # small jobs: finished by now, their tables not taken
+        eng.serve_stop()
+        res = eng.count(jobs[0], 250, 31)
+        keys, counts, nk = pyoracle.count(jobs[0], 250, 31)
+        assert res.n_kmers == nk and np.array_equal(res.kmers, keys)
+
+
 def test_serve_stop_right_after_start_returns():
     """dk_serve_stop with idle workers (none has slept yet) joins them."""
     with dk.Engine(0) as eng:
