@@ -102,7 +102,8 @@ class Stats(ctypes.Structure):
                 ("n_partitioned", ctypes.c_uint64), ("n_waves", ctypes.c_uint64),
                 ("n_bins_resorted", ctypes.c_uint64), ("n_bins_big", ctypes.c_uint64),
                 ("n_bins_retried", ctypes.c_uint64), ("n_groups", ctypes.c_uint64),
-                ("table_streamed", ctypes.c_uint64), ("upload_chunks", ctypes.c_uint64)]
+                ("table_streamed", ctypes.c_uint64), ("upload_chunks", ctypes.c_uint64),
+                ("n_bins_packed", ctypes.c_uint64), ("n_bins_fallback", ctypes.c_uint64)]
 
     KERNEL_NAMES = ["extract_count", "extract_scatter", "partition_hist", "partition_scatter",
                     "bin_count", "compact", "hash_insert", "other"]

@@ -165,7 +165,7 @@ Engine::~Engine() {
   for (cudaStream_t st : {stream, s_in, s_out})
     if (st) cudaStreamSynchronize(st);
   for (DevBuf* b : {&text, &text2, &keysA, &keysB, &cnt, &H, &O, &nodes, &tiles, &TH, &finals, &bigs, &rng, &ctrs,
-                    &aux})
+                    &aux, &fbl})
     Arena::release(this, *b);
   for (auto& t : tables) {  // device tables (host tables live in the shared pool)
     cudaFree(t.k);
@@ -1009,10 +1009,18 @@ int Engine::count_device(const uint8_t* d_text, uint64_t nbytes, const dk_input_
         // this pass's levels are done: count its final nodes
         if (grp == 0 && fin_lo == fin_g) DK_CUDA(cudaEventRecord(ev_stage[3], stream));
         DK_CUDA(cudaMemsetAsync(c64 + 4, 0, 8, stream));  // bin ticket
+        uint32_t* fb = nullptr;
+        if (use_hash && n_final > fin_lo) {
+          // the packed kernel's ticket and fallback count (its totals, [21] and
+          // [22], run over the whole count)
+          DK_TRY(Arena::ensure(this, fbl, (size_t)(n_final - fin_lo) * 4));
+          DK_CUDA(cudaMemsetAsync(c64 + 19, 0, 16, stream));
+          fb = (uint32_t*)fbl.p;
+        }
         TIMED(4, launch_bin_count((Node*)nodes.p, (uint32_t*)bigs.p + big_lo, n_bigf - big_lo,
                                   (uint32_t*)finals.p + fin_lo, n_final - fin_lo,
                                   (uint64_t*)keysA.p, (uint64_t*)keysB.p, (uint32_t*)cnt.p,
-                                  use_hash ? 1 : 0, c64, sm_count, stream));
+                                  use_hash ? 1 : 0, c64, sm_count, stream, fb));
         DK_CUDA(cudaEventRecord(ev_stage[4], stream));
         if (!big_ok || n_bigf == big_lo) break;  // only big bins can ask for a retry
         uint64_t retry = 0;
@@ -1089,10 +1097,12 @@ int Engine::count_device(const uint8_t* d_text, uint64_t nbytes, const dk_input_
   }
   stats.n_bins = n_final + n_bigf - (uint32_t)stats.n_bins_retried;
   stats.n_groups = group_at.size() - 1;
-  uint64_t tail[16];
-  DK_TRY(sync_read(c64 + 2, 128, tail));
+  uint64_t tail[21];
+  DK_TRY(sync_read(c64 + 2, sizeof(tail), tail));
   stats.n_bins_resorted = tail[4];
   stats.n_bins_big = tail[15];
+  stats.n_bins_packed = tail[19];
+  stats.n_bins_fallback = tail[20];
   const uint64_t n_distinct = tail[0];
   if (tail[1]) {
     set_error("a bounded device wait (TMA copy) timed out");

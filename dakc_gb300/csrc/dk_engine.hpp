@@ -117,6 +117,7 @@ struct Engine {
 
   // device arenas
   DevBuf text, text2, keysA, keysB, cnt, H, O, nodes, tiles, TH, finals, bigs, rng, ctrs;
+  DevBuf fbl;  // final nodes the packed bin kernel leaves to the general one
   size_t node_cap_needed = 0;
   uint64_t* out_k = nullptr;
   uint32_t* out_c = nullptr;

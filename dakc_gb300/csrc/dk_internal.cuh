@@ -170,10 +170,13 @@ int launch_tile_scatter(const Node* nodes, const Tile* tiles, uint32_t n_tiles, 
 // [17] = big skewed bins counted (all zeroed by the caller); use_hash selects
 // the hash-first bin count
 // bins: big_list[0, n_big) first, then final_list[0, n_final)
+// with use_hash and fb_list (room for n_final entries), the final list goes
+// through the packed-table kernel first (ctr[19] its ticket, ctr[20] the bins
+// it leaves in fb_list, ctr[21] the bins it counts; all zeroed by the caller)
 int launch_bin_count(Node* nodes, const uint32_t* big_list, uint32_t n_big,
                      const uint32_t* final_list, uint32_t n_final, uint64_t* A, uint64_t* B,
                      uint32_t* C, int use_hash, unsigned long long* ctr, int sm_count,
-                     cudaStream_t s);
+                     cudaStream_t s, uint32_t* fb_list = nullptr);
 int launch_aggregate(Node* nodes, uint32_t node_lo, uint32_t node_hi, cudaStream_t s);
 // level-1 nodes [b0, b1) follow the *total_d distinct keys before them
 int launch_l1_offsets(Node* nodes, uint32_t b0, uint32_t b1, unsigned long long* total_d,

@@ -1685,24 +1685,30 @@ __device__ bool bin_hashed(Node* nodes, uint32_t ni, const Node& nd, uint64_t* k
   return true;
 }
 
-// ---- packed hash variant: one 64-bit word per distinct key
+// ---- packed hash bins: one 64-bit word per distinct key
 // A bin's keys share their bits [s, 2k) (s = nd.shift free bits), so a key is
 // its low s bits.  Entry = (free bits << (64 - s)) | count: the free bits sit
 // at the top, the count (< 2^14 for a bin of at most kBinCap keys) at the
 // bottom.  Entries compare as the keys they hold, 0 is an empty slot, a new
 // key enters with one 64-bit CAS and a repeat adds to the low 32-bit word.
-constexpr int kPackSlotBits = 13;
-constexpr uint32_t kPackSlots = 1u << kPackSlotBits;     // 64 KB of table
+// Normal bins are counted this way by their own kernel (k_bin_packed), whose
+// small shared-memory footprint fits three 512-thread CTAs per SM: a bin's
+// work is a chain of dependent shared-memory steps, so throughput follows the
+// number of bins in flight (3 CTAs: 14.7 ms per 2.4 G keys of C2-shaped bins,
+// 2 CTAs with twice the table: 18.8 ms).  Bins it cannot take go to a list
+// that k_bin_count handles after it.
+constexpr int kPackSlotBits = 12;
+constexpr uint32_t kPackSlots = 1u << kPackSlotBits;  // 32 KB of table
+constexpr uint32_t kPackMaxDistinct = 2048;            // sorted entries (16 KB)
+constexpr int kPackDigitBits = 10;                     // counting-sort digits (4 KB)
 constexpr uint32_t kPackMaxProbe = 64;
-constexpr uint32_t kPackMaxDistinct = (kBinCap * 8 - kPackSlots * 8) / 8;  // sorted entries after the table
 constexpr int kPackMaxShift = 50;  // the count field keeps >= 14 bits
-// inside the two-CTA-per-SM bin kernel the packed table measured slower than
-// bin_hashed (C2 bin count 24.6 against 22.8 ms), so it is not selected there
-constexpr bool kPackInBinKernel = false;
+constexpr int kPackThreads = 512;
+constexpr int kPackBlocksPerSM = 3;
+constexpr size_t kPackSmem = kPackSlots * 8 + kPackMaxDistinct * 8 + (4u << kPackDigitBits);
 static_assert(kBinCap < (1 << (64 - kPackMaxShift)), "a bin's largest count fits the count field");
-static_assert(kPackSlots * 8 + kPackMaxDistinct * 8 <= kBinCap * 8, "table and sorted entries fit");
 static_assert(kPackMaxDistinct * 12 <= kPackSlots * 8, "the output stage fits the table");
-static_assert(kPackSlots % (2 * kBinThreads) == 0, "slot loops");
+static_assert(kPackSlots % (2 * kPackThreads) == 0, "slot loops");
 
 // Insert one key (rk = key << (64 - s)) with multiplicity mult; false when the
 // probe runs past kPackMaxProbe slots.
@@ -1729,24 +1735,26 @@ __device__ __forceinline__ bool pack_insert(unsigned long long* tab, unsigned lo
   return false;
 }
 
-// A bin with at most kBinCap keys and kDenseBits < s <= kPackMaxShift free
-// bits: insert every key into a packed table, place the distinct entries by
+// One bin with at most kBinCap keys and kDenseBits < s <= kPackMaxShift free
+// bits: insert every key into the packed table, place the distinct entries by
 // their top D bits (counting sort), rank each inside its digit range, stage
-// the sorted (key, count) pairs in shared memory and write them to the bin's
-// region with coalesced stores.  Returns false, having written nothing, when
-// a probe runs too long or the bin holds more than kPackMaxDistinct keys.
+// the sorted (key, count) pairs in the freed table and write them to the
+// bin's region with coalesced stores.  Returns false, having written nothing,
+// when a probe runs too long or the bin holds more than kPackMaxDistinct keys.
 __device__ bool bin_packed(Node* nodes, uint32_t ni, const Node& nd, uint64_t* keys, uint32_t* cnt,
-                           unsigned long long* region, uint32_t* hist, uint32_t* tmp,
-                           uint32_t* mark, uint32_t* flags, bool hot) {
-  unsigned long long* tab = region;                  // kPackSlots entries
-  unsigned long long* sorted = region + kPackSlots;  // by digit
+                           unsigned long long* region, uint32_t* tmp, uint32_t* mark,
+                           uint32_t* flags, bool hot) {
+  constexpr uint32_t T = kPackThreads;
+  unsigned long long* tab = region;                                          // kPackSlots
+  unsigned long long* sorted = region + kPackSlots;                          // by digit
+  uint32_t* hist = reinterpret_cast<uint32_t*>(sorted + kPackMaxDistinct);   // 2^D
   const uint32_t n = (uint32_t)nd.n;
   const int s = nd.shift;
   const int cbits = 64 - s;
   const unsigned long long himask = ~((1ull << cbits) - 1ull);
   const uint32_t cmask = cbits >= 32 ? 0xFFFFFFFFu : ((1u << cbits) - 1u);
   int D = ceil_log2_u64(n) - 3;
-  D = max(4, min(D, kBinDigitBits));
+  D = max(4, min(D, kPackDigitBits));
   D = min(D, s);
   const int dsh = 64 - D;
   const uint32_t R = 1u << D;
@@ -1755,27 +1763,27 @@ __device__ bool bin_packed(Node* nodes, uint32_t ni, const Node& nd, uint64_t* k
   {
     uint4* t4 = reinterpret_cast<uint4*>(tab);
 #pragma unroll
-    for (uint32_t u = 0; u < kPackSlots / 2 / kBinThreads; ++u)
-      t4[threadIdx.x + u * kBinThreads] = make_uint4(0u, 0u, 0u, 0u);
+    for (uint32_t u = 0; u < kPackSlots / 2 / T; ++u)
+      t4[threadIdx.x + u * T] = make_uint4(0u, 0u, 0u, 0u);
   }
-  for (uint32_t j = threadIdx.x; j < R; j += kBinThreads) hist[j] = 0;
-  for (uint32_t w = threadIdx.x; w < (R + 31) / 32; w += kBinThreads) mark[w] = 0;
+  for (uint32_t j = threadIdx.x; j < R; j += T) hist[j] = 0;
+  for (uint32_t w = threadIdx.x; w < (R + 31) / 32; w += T) mark[w] = 0;
   if (threadIdx.x == 0) flags[1] = 0;
   __syncthreads();
   DK_PHASE(11);
   constexpr int kBatch = 8;
   bool ok = true;
-  for (uint32_t i0 = 0; i0 < n; i0 += kBatch * kBinThreads) {
+  for (uint32_t i0 = 0; i0 < n; i0 += kBatch * T) {
     unsigned long long kk[kBatch];
 #pragma unroll
     for (int u = 0; u < kBatch; ++u) {
-      const uint32_t i = i0 + (uint32_t)u * kBinThreads + threadIdx.x;
+      const uint32_t i = i0 + (uint32_t)u * T + threadIdx.x;
       kk[u] = i < n ? __ldg(keys + i) : 0ull;
     }
 #pragma unroll
     for (int u = 0; u < kBatch; ++u) {
-      if (i0 + (uint32_t)u * kBinThreads >= n) break;  // uniform
-      const bool valid = i0 + (uint32_t)u * kBinThreads + threadIdx.x < n;
+      if (i0 + (uint32_t)u * T >= n) break;  // uniform
+      const bool valid = i0 + (uint32_t)u * T + threadIdx.x < n;
       const unsigned long long rk = kk[u] << cbits;
       uint32_t mult = 1;
       bool live = valid;
@@ -1799,8 +1807,8 @@ __device__ bool bin_packed(Node* nodes, uint32_t ni, const Node& nd, uint64_t* k
   {
     const ulonglong2* t2 = reinterpret_cast<const ulonglong2*>(tab);
 #pragma unroll
-    for (uint32_t u = 0; u < kPackSlots / 2 / kBinThreads; ++u) {
-      const ulonglong2 e = t2[threadIdx.x + u * kBinThreads];
+    for (uint32_t u = 0; u < kPackSlots / 2 / T; ++u) {
+      const ulonglong2 e = t2[threadIdx.x + u * T];
       if (e.x) sorted[atomicAdd(&hist[(uint32_t)(e.x >> dsh)], 1u)] = e.x;
       if (e.y) sorted[atomicAdd(&hist[(uint32_t)(e.y >> dsh)], 1u)] = e.y;
     }
@@ -1809,9 +1817,9 @@ __device__ bool bin_packed(Node* nodes, uint32_t ni, const Node& nd, uint64_t* k
   DK_PHASE(14);
   // rank inside the digit range and stage the pair (the table is free now);
   // ranges of more than kRankMax entries are marked for a warp sort
-  unsigned long long* ok_ = tab;                              // d keys
-  uint32_t* oc = reinterpret_cast<uint32_t*>(tab + d);        // d counts
-  for (uint32_t x = threadIdx.x; x < d; x += kBinThreads) {
+  unsigned long long* ok_ = tab;                          // d keys
+  uint32_t* oc = reinterpret_cast<uint32_t*>(tab + d);    // d counts
+  for (uint32_t x = threadIdx.x; x < d; x += T) {
     const unsigned long long v = sorted[x];
     const uint32_t j = (uint32_t)(v >> dsh);
     const uint32_t lo = j ? hist[j - 1] : 0, hi = hist[j];
@@ -1827,7 +1835,7 @@ __device__ bool bin_packed(Node* nodes, uint32_t ni, const Node& nd, uint64_t* k
   __syncthreads();
   DK_PHASE(15);
   const uint32_t warp = threadIdx.x >> 5;
-  for (uint32_t w = warp; w < (R + 31) / 32; w += kBinThreads / 32) {
+  for (uint32_t w = warp; w < (R + 31) / 32; w += T / 32) {
     uint32_t bits = mark[w];
     while (bits) {
       const uint32_t j = w * 32 + (__ffs(bits) - 1);
@@ -1843,7 +1851,7 @@ __device__ bool bin_packed(Node* nodes, uint32_t ni, const Node& nd, uint64_t* k
   }
   __syncthreads();
   DK_PHASE(16);
-  for (uint32_t x = threadIdx.x; x < d; x += kBinThreads) {
+  for (uint32_t x = threadIdx.x; x < d; x += T) {
     keys[x] = ok_[x];
     cnt[x] = oc[x];
   }
@@ -1853,6 +1861,63 @@ __device__ bool bin_packed(Node* nodes, uint32_t ni, const Node& nd, uint64_t* k
   DK_PHASE_ADD(28, d);
   if (threadIdx.x == 0) nodes[ni].d = d;
   return true;
+}
+
+// Persistent packed-bin counter over the final list: CTAs take bins by
+// ticket (ctr[19]) and pull the next bin's keys into L2 while counting one.
+// Bins it does not count -- dense ones (at most kDenseBits free bits), ones
+// with more than kPackMaxShift free bits, and ones the packed table cannot
+// hold -- are appended to fb_list (ctr[20] entries) for k_bin_count; ctr[21]
+// counts the bins it finished and ctr[22] the ones it left, over all passes.
+__global__ void __launch_bounds__(kPackThreads, kPackBlocksPerSM)
+    k_bin_packed(Node* nodes, const uint32_t* __restrict__ finals, uint32_t n_bins, uint64_t* A,
+                 uint64_t* B, uint32_t* C, unsigned long long* ctr, uint32_t* fb_list) {
+  extern __shared__ __align__(16) unsigned long long region[];
+  __shared__ uint32_t tmp[64];
+  __shared__ uint32_t mark[(1u << kPackDigitBits) / 32];
+  __shared__ uint32_t s_bin;
+  __shared__ uint32_t flags[2];
+  __shared__ bool s_hot;
+  unsigned int* ticket = reinterpret_cast<unsigned int*>(&ctr[19]);
+  if (threadIdx.x == 0) s_bin = atomicAdd(ticket, 1u);
+  __syncthreads();
+  for (;;) {
+    const uint32_t b = s_bin;
+    if (b >= n_bins) break;
+    const uint32_t ni = finals[b];
+    const Node nd = nodes[ni];
+    uint64_t* keys = (nd.buf ? B : A) + nd.start;
+    uint32_t* cnt = C + nd.start;
+    __syncthreads();  // every thread has read s_bin
+    if (threadIdx.x == 32) {
+      const uint32_t nb = atomicAdd(ticket, 1u);
+      s_bin = nb;
+      if (nb < n_bins) {
+        const Node& nx = nodes[finals[nb]];
+        prefetch_l2_range((nx.buf ? B : A) + nx.start, nx.n * 8);
+      }
+    }
+    const bool eligible = nd.shift > kDenseBits && nd.shift <= kPackMaxShift &&
+                          nd.n <= (uint64_t)kBinCap;
+    if (eligible && threadIdx.x < 32) {  // hot bin: a 32-key sample repeats a key >= 4 times
+      const uint64_t smp = nd.n ? __ldg(keys + (nd.n * threadIdx.x) / 32) : 0ull;
+      const uint32_t peers = __match_any_sync(0xFFFFFFFFu, smp);
+      const uint32_t dup = __reduce_max_sync(0xFFFFFFFFu, (uint32_t)__popc(peers));
+      if (threadIdx.x == 0) s_hot = dup >= 4;
+    }
+    __syncthreads();
+    bool done = false;
+    if (eligible) done = bin_packed(nodes, ni, nd, keys, cnt, region, tmp, mark, flags, s_hot);
+    if (threadIdx.x == 0) {
+      if (done) {
+        atomicAdd(&ctr[21], 1ull);
+      } else {
+        fb_list[atomicAdd(reinterpret_cast<unsigned int*>(&ctr[20]), 1u)] = ni;
+        atomicAdd(&ctr[22], 1ull);
+      }
+    }
+    __syncthreads();
+  }
 }
 
 // Persistent bin counter: CTAs take final nodes from a ticket until none are
@@ -1869,7 +1934,8 @@ __global__ void __launch_bounds__(kBinThreads, kBinBlocksPerSM) k_bin_count(Node
                                                               uint32_t n_bins, uint64_t* A,
                                                               uint64_t* B, uint32_t* C,
                                                               unsigned long long* ctr,
-                                                              int use_hash) {
+                                                              int use_hash,
+                                                              const unsigned int* n_finals_dev) {
   extern __shared__ __align__(16) unsigned long long skeys[];  // kBinCap keys / 4096 u64 counts
   __shared__ uint32_t hist[1u << kBinDigitBits];
   __shared__ uint32_t tmp[64];
@@ -1878,6 +1944,9 @@ __global__ void __launch_bounds__(kBinThreads, kBinBlocksPerSM) k_bin_count(Node
   __shared__ uint32_t s_bin, n_defer;
   __shared__ uint32_t hflags[2];
   __shared__ bool s_hot;
+  // with n_finals_dev the final list's length is only known on the device
+  // (the packed bins' fallback list)
+  if (n_finals_dev) n_bins = n_big + *n_finals_dev;
   if (threadIdx.x == 0) s_bin = atomicAdd(reinterpret_cast<unsigned int*>(&ctr[4]), 1u);
   __syncthreads();
   for (;;) {
@@ -1924,11 +1993,7 @@ __global__ void __launch_bounds__(kBinThreads, kBinBlocksPerSM) k_bin_count(Node
       }
     } else {
       bool done = false;
-      if (kPackInBinKernel && use_hash && nd.shift <= kPackMaxShift) {
-        done = bin_packed(nodes, ni, nd, keys, cnt, skeys, hist, tmp, mark, hflags, hot);
-        __syncthreads();
-      }
-      if (use_hash && !done) {
+      if (use_hash) {
         done = bin_hashed(nodes, ni, nd, keys, cnt, skeys, hist, tmp, mark, hflags, hot, &ctr[5]);
         if (!done && threadIdx.x == 0) atomicAdd(&ctr[6], 1ull);  // bins that fell back
         __syncthreads();
@@ -2301,14 +2366,31 @@ int bin_count_smem_bytes(int) { return kBinCap * 8; }
 int launch_bin_count(Node* nodes, const uint32_t* big_list, uint32_t n_big,
                      const uint32_t* final_list, uint32_t n_final, uint64_t* A, uint64_t* B,
                      uint32_t* C, int use_hash, unsigned long long* ctr, int sm_count,
-                     cudaStream_t s) {
+                     cudaStream_t s, uint32_t* fb_list) {
   const uint32_t n_bins = n_big + n_final;
   if (!n_bins) return 0;
   allow_max_smem(k_bin_count);
+  if (!use_hash || !fb_list) {
+    const uint32_t grid = std::min<uint32_t>(n_bins, (uint32_t)(kBinBlocksPerSM * sm_count));
+    k_bin_count<<<grid, kBinThreads, kBinCap * 8, s>>>(nodes, big_list, n_big, final_list, n_bins,
+                                                       A, B, C, ctr, use_hash, nullptr);
+    return 1;
+  }
+  // hash variant: the packed kernel takes the final list; what it leaves
+  // (fb_list) follows the big bins through k_bin_count
+  int launches = 0;
+  if (n_final) {
+    allow_max_smem(k_bin_packed);
+    const uint32_t grid = std::min<uint32_t>(n_final, (uint32_t)(kPackBlocksPerSM * sm_count));
+    k_bin_packed<<<grid, kPackThreads, kPackSmem, s>>>(nodes, final_list, n_final, A, B, C, ctr,
+                                                       fb_list);
+    ++launches;
+  }
   const uint32_t grid = std::min<uint32_t>(n_bins, (uint32_t)(kBinBlocksPerSM * sm_count));
-  k_bin_count<<<grid, kBinThreads, kBinCap * 8, s>>>(nodes, big_list, n_big, final_list, n_bins,
-                                                     A, B, C, ctr, use_hash);
-  return 1;
+  k_bin_count<<<grid, kBinThreads, kBinCap * 8, s>>>(nodes, big_list, n_big, fb_list, 0, A, B, C,
+                                                     ctr, use_hash,
+                                                     reinterpret_cast<const unsigned int*>(&ctr[20]));
+  return launches + 1;
 }
 
 int launch_aggregate(Node* nodes, uint32_t lo, uint32_t hi, cudaStream_t s) {

@@ -144,6 +144,10 @@ typedef struct {
                                while the count ran; 0: after it               */
   uint64_t upload_chunks;   /* chunks the reads were uploaded in, each counted as
                                it landed (0: one upload before the count)     */
+  uint64_t n_bins_packed;   /* hash variant: bins counted in a packed table (one
+                               64-bit word per distinct k-mer)                 */
+  uint64_t n_bins_fallback; /* of the final bins, those the packed table could not
+                               hold (counted by the general bin kernel)        */
 } dk_stats;
 
 /* One read set of a batch (dk_count_batch). */

@@ -75,6 +75,14 @@ def _assert_same(got, ref):
 
 
 @pytest.fixture(scope="module")
+def engine():
+    """A context of its own: its arenas (tens of GB at these sizes) are freed
+    when the module ends instead of staying with the session's context."""
+    with dk.Engine(0) as eng:
+        yield eng
+
+
+@pytest.fixture(scope="module")
 def large():
     rs = synth.large_100m()
     ref = pyoracle.count_mt(rs.text, rs.line_width, rs.k)

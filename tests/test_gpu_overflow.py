@@ -37,6 +37,7 @@ def test_one_kmer_around_2_32_times(variant):
     import torch
     below = (1 << 32) // (W - K + 1) - 4_000    # 4,294,487,040 occurrences
     above = below + 10_000                      # 4,295,687,040 > 2^32
+    torch.cuda.empty_cache()
     with dk.Engine(0) as eng:
         d_text, nbytes = _device_lines_of_a(below)
         t = eng.count_raw(d_text.data_ptr(), nbytes,
