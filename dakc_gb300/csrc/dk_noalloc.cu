@@ -8,20 +8,24 @@
 // and forbids other libraries from reserving more.  dk_count and
 // dk_count_device allocate their work buffers (key partitions, staging) in
 // the engine context, so such callers cannot use them.  This entry point
-// needs no context and no scratch: the caller passes device input and output
-// buffers.  The unsorted k-mers wait in the caller's k-mer array (it holds at
-// least the k-mer bound) until they are sorted into shared memory, and the
-// run-length head positions stay in shared memory.
+// needs no context: the caller passes device input and output buffers, and
+// the kernel's scratch (the unsorted k-mers, before they are sorted into
+// shared memory) is one fixed array in this file, g_noalloc_keys, that the
+// library holds on every device that loads it, until the process exits.
 //
 // Limits and sharing rules:
 //   * at most kNoAllocMaxKmers (12,288) k-mer occurrences per call, judged by
 //     the upper bound lines * (line_width - k + 1); larger inputs are
 //     rejected with DK_ERR_ADMISSION before anything is launched;
-//   * calls share no device memory: calls on different streams or host
-//     threads may overlap, each with its own output buffers;
+//   * every call on a device uses the same scratch array, which keeps the
+//     last call's contents; each call writes every entry it reads, so nothing
+//     needs clearing, but calls that overlap on the GPU (different streams or
+//     host threads with no ordering between them) race on it: order them;
 //   * the first call on a device (with that device current) does a one-time
-//     set-up: it raises the kernel's shared-memory limit.  Make that first
-//     call before any stream capture on that device.
+//     set-up: it looks up the scratch array's device address with
+//     cudaGetSymbolAddress and raises the kernel's shared-memory limit.  Make
+//     that first call before any stream capture on that device.  A device
+//     reset (cudaDeviceReset) invalidates that set-up: use a new process.
 //
 // The kernel is a single-CTA variant of the engine's bin count: it extracts
 // the k-mers of every line (the same warp-per-line extraction), counting-sorts
@@ -44,11 +48,15 @@ constexpr int kNoAllocThreads = 512;
 // dynamic shared memory: the sorted k-mers, then the run heads (uint32)
 constexpr size_t kNoAllocSmem = (size_t)kNoAllocMaxKmers * 12;
 
+// The scratch: the unsorted k-mers of one call (98,304 bytes per device).
+// Host code reaches it only through the address cudaGetSymbolAddress gives.
+static __device__ __align__(256) unsigned long long g_noalloc_keys[kNoAllocMaxKmers];
+
 template <int C>
 __global__ void __launch_bounds__(kNoAllocThreads)
     k_count_small_static(const uint8_t* __restrict__ text, uint64_t n_lines, int W, int k,
-                         uint64_t* out_k, uint32_t* __restrict__ out_c,
-                         uint64_t* __restrict__ summary) {
+                         unsigned long long* __restrict__ keys, uint64_t* __restrict__ out_k,
+                         uint32_t* __restrict__ out_c, uint64_t* __restrict__ summary) {
   extern __shared__ unsigned long long skeys[];  // kNoAllocMaxKmers, then the heads
   __shared__ uint32_t hist[1u << 12];
   __shared__ unsigned long long tmp[32];
@@ -56,10 +64,8 @@ __global__ void __launch_bounds__(kNoAllocThreads)
   __shared__ uint16_t long_list[512];
   __shared__ uint32_t s_n, n_long;
   __shared__ unsigned long long s_first_nul;
-  // the raw k-mers wait in the caller's table (it holds at least the k-mer
-  // bound) until they are sorted into shared memory; the table is written
-  // only after that
-  unsigned long long* keys = reinterpret_cast<unsigned long long*>(out_k);
+  // the raw k-mers wait in the scratch array (keys) until they are sorted
+  // into shared memory
   uint32_t* heads = reinterpret_cast<uint32_t*>(skeys + kNoAllocMaxKmers);
   if (threadIdx.x == 0) {
     s_n = 0;
@@ -162,6 +168,7 @@ __global__ void __launch_bounds__(kNoAllocThreads)
 
 struct DeviceSetup {
   bool ready = false;
+  unsigned long long* scratch = nullptr;  // device address of g_noalloc_keys
 };
 constexpr int kMaxDevices = 128;
 std::mutex g_setup_mu;
@@ -173,11 +180,18 @@ cudaError_t prepare_kernel() {
                               (int)kNoAllocSmem);
 }
 
-// one-time, per-device set-up (the device must be current)
-int setup_device(int dev) {
+// one-time, per-device set-up (the device must be current): the scratch
+// array's device address and the kernel's shared-memory limit
+int setup_device(int dev, unsigned long long** scratch) {
   std::lock_guard<std::mutex> g(g_setup_mu);
   DeviceSetup& s = g_setup[dev];
   if (!s.ready) {
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_noalloc_keys) != cudaSuccess || !p) {
+      cudaGetLastError();
+      return DK_ERR_CUDA;
+    }
+    s.scratch = static_cast<unsigned long long*>(p);
     cudaError_t e = cudaSuccess;
     for (cudaError_t x : {prepare_kernel<1>(), prepare_kernel<2>(), prepare_kernel<4>(),
                           prepare_kernel<5>(), prepare_kernel<8>(), prepare_kernel<16>(),
@@ -189,6 +203,7 @@ int setup_device(int dev) {
     }
     s.ready = true;
   }
+  *scratch = s.scratch;
   return DK_OK;
 }
 
@@ -218,19 +233,20 @@ extern "C" int dk_count_small_noalloc(const char* d_text, uint64_t nbytes, int l
     cudaGetLastError();
     return DK_ERR_NO_DEVICE;
   }
-  const int rc = setup_device(dev);
+  unsigned long long* scratch = nullptr;
+  const int rc = setup_device(dev, &scratch);
   if (rc != DK_OK) return rc;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   const uint8_t* t = reinterpret_cast<const uint8_t*>(d_text);
   const size_t smem = kNoAllocSmem;
   const int c = (line_width + 31) / 32;
-  if (c <= 1) k_count_small_static<1><<<1, kNoAllocThreads, smem, s>>>(t, lines, line_width, k, d_kmers, d_counts, d_summary);
-  else if (c <= 2) k_count_small_static<2><<<1, kNoAllocThreads, smem, s>>>(t, lines, line_width, k, d_kmers, d_counts, d_summary);
-  else if (c <= 4) k_count_small_static<4><<<1, kNoAllocThreads, smem, s>>>(t, lines, line_width, k, d_kmers, d_counts, d_summary);
-  else if (c <= 5) k_count_small_static<5><<<1, kNoAllocThreads, smem, s>>>(t, lines, line_width, k, d_kmers, d_counts, d_summary);
-  else if (c <= 8) k_count_small_static<8><<<1, kNoAllocThreads, smem, s>>>(t, lines, line_width, k, d_kmers, d_counts, d_summary);
-  else if (c <= 16) k_count_small_static<16><<<1, kNoAllocThreads, smem, s>>>(t, lines, line_width, k, d_kmers, d_counts, d_summary);
-  else k_count_small_static<32><<<1, kNoAllocThreads, smem, s>>>(t, lines, line_width, k, d_kmers, d_counts, d_summary);
+  if (c <= 1) k_count_small_static<1><<<1, kNoAllocThreads, smem, s>>>(t, lines, line_width, k, scratch, d_kmers, d_counts, d_summary);
+  else if (c <= 2) k_count_small_static<2><<<1, kNoAllocThreads, smem, s>>>(t, lines, line_width, k, scratch, d_kmers, d_counts, d_summary);
+  else if (c <= 4) k_count_small_static<4><<<1, kNoAllocThreads, smem, s>>>(t, lines, line_width, k, scratch, d_kmers, d_counts, d_summary);
+  else if (c <= 5) k_count_small_static<5><<<1, kNoAllocThreads, smem, s>>>(t, lines, line_width, k, scratch, d_kmers, d_counts, d_summary);
+  else if (c <= 8) k_count_small_static<8><<<1, kNoAllocThreads, smem, s>>>(t, lines, line_width, k, scratch, d_kmers, d_counts, d_summary);
+  else if (c <= 16) k_count_small_static<16><<<1, kNoAllocThreads, smem, s>>>(t, lines, line_width, k, scratch, d_kmers, d_counts, d_summary);
+  else k_count_small_static<32><<<1, kNoAllocThreads, smem, s>>>(t, lines, line_width, k, scratch, d_kmers, d_counts, d_summary);
   if (cudaGetLastError() != cudaSuccess) return DK_ERR_CUDA;
   return DK_OK;
 }

@@ -306,16 +306,19 @@ int dk_serve_stop(dk_ctx* ctx);  /* finishes queued jobs, joins the workers */
  * memory, at least `capacity` entries) and d_summary (device memory, 3
  * uint64: distinct k-mers, k-mer occurrences, status 0 = ok).  The call is
  * asynchronous on `stream` (a cudaStream_t, NULL for the default stream) on
- * the current device and allocates nothing; it has no scratch memory either
- * (the unsorted k-mers wait in d_kmers, the rest stays in shared memory).
+ * the current device and allocates nothing: its scratch is one fixed array
+ * of 12,288 uint64 (96 KB) inside the library, which every device that
+ * loads the library holds until the process exits.
  *   - Inputs whose k-mer upper bound, lines * (line_width - k + 1), exceeds
  *     12,288 are rejected with DK_ERR_ADMISSION before any launch;
  *     capacity must be at least that bound (else DK_ERR_INVALID_ARG).
- *   - Calls share no device memory: calls on different streams or threads
- *     may overlap, each with its own buffers.
- *   - The first call on a device does a one-time set-up (it sets the
+ *   - Every call on a device shares that scratch array (it keeps the last
+ *     call's contents; each call writes all it reads).  Calls that overlap
+ *     on the GPU race on it: issue them on one stream, or order them.
+ *   - The first call on a device does a one-time set-up with that device
+ *     current (it looks up the scratch array's device address and sets the
  *     kernel's shared-memory limit); make that first call before any stream
- *     capture on that device.
+ *     capture on that device.  After a device reset, use a new process.
  * Results equal dk_count's table for the same reads. */
 int dk_count_small_noalloc(const char* d_text, uint64_t nbytes, int line_width, int k,
                            uint64_t* d_kmers, uint32_t* d_counts, uint64_t capacity,

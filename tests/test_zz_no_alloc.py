@@ -1,12 +1,13 @@
 """dk_count_small_noalloc: the count that allocates nothing.
 
-It serves callers that cannot allocate device memory when they need a
-count (allocator callbacks, latency-bound serving loops, programs that own all
-device memory through their own pool).  It has no scratch memory: the
-unsorted k-mers wait in the caller's k-mer array.  This file checks that two
-calls in a row -- the second on a smaller input -- each give exactly
-dk_count's table, that two calls on different streams with their own buffers
-may overlap, and that oversized inputs are rejected.
+It serves callers that cannot allocate device memory when they need a count
+(allocator callbacks, latency-bound serving loops, programs that own all
+device memory through their own pool).  Its scratch is one fixed array inside
+the library, shared by every call on a device.  This file checks, through the
+C ABI, that two calls in a row -- the second on a smaller input, over the
+first call's leftovers in that array -- each give exactly dk_count's table,
+that several calls queued back to back on one stream do too, and that
+oversized inputs are rejected.
 The file is named to be collected last; it also passes alone in a fresh
 process.
 """
@@ -79,13 +80,16 @@ def test_noalloc_rejects_oversized_input(lib):
     assert rc == dk.DK_ERR_ADMISSION
 
 
-def test_noalloc_calls_on_two_streams_overlap(lib, engine):
-    """Two calls launched back to back on two streams, each with its own
-    buffers, may run at the same time: each table equals dk_count's."""
+def test_noalloc_calls_back_to_back_on_one_stream(lib, engine):
+    """Calls queued on one stream run one after the other, each over the
+    previous call's leftovers in the shared scratch array: every table equals
+    dk_count's."""
     import torch
     g = synth.genome_uniform(51, 5000)
     W, k = 150, 31
-    texts = [synth.reads(52 + i, g, 90, 100, W, W, rc_frac=0.5, err_rate=0.02) for i in range(2)]
+    texts = [synth.reads(52 + i, g, 90 - 20 * i, 100, W, W, rc_frac=0.5, err_rate=0.02)
+             for i in range(3)]
+    stream = torch.cuda.current_stream().cuda_stream
     runs = []
     for text in texts:
         d_text = torch.from_numpy(np.concatenate([text, np.zeros(64, np.uint8)])).cuda()
@@ -93,16 +97,16 @@ def test_noalloc_calls_on_two_streams_overlap(lib, engine):
         cap = max(1, lines * (W - k + 1))
         runs.append((text, d_text, cap, torch.empty(cap, dtype=torch.int64, device="cuda"),
                      torch.empty(cap, dtype=torch.int32, device="cuda"),
-                     torch.full((3,), -1, dtype=torch.int64, device="cuda"), torch.cuda.Stream()))
+                     torch.full((3,), -1, dtype=torch.int64, device="cuda")))
     torch.cuda.synchronize()
-    for text, d_text, cap, out_k, out_c, summ, st in runs:
+    for text, d_text, cap, out_k, out_c, summ in runs:
         rc = lib.dk_count_small_noalloc(
             ctypes.c_void_p(d_text.data_ptr()), ctypes.c_uint64(text.size), W, k,
             ctypes.c_void_p(out_k.data_ptr()), ctypes.c_void_p(out_c.data_ptr()),
-            ctypes.c_uint64(cap), ctypes.c_void_p(summ.data_ptr()), ctypes.c_void_p(st.cuda_stream))
+            ctypes.c_uint64(cap), ctypes.c_void_p(summ.data_ptr()), ctypes.c_void_p(stream))
         assert rc == dk.DK_OK
     torch.cuda.synchronize()
-    for text, d_text, cap, out_k, out_c, summ, st in runs:
+    for text, d_text, cap, out_k, out_c, summ in runs:
         s = summ.cpu().numpy()
         nd = int(s[0])
         ref = engine.count(text, W, k, dk.VARIANT_SORT)
