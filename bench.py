@@ -240,30 +240,56 @@ def pct(xs, p):
     return float(np.percentile(np.asarray(xs, dtype=np.float64), p)) if len(xs) else None
 
 
-def run_batched(eng, texts, variant):
-    """jobs/s of one dk_count_batch over all sets vs one dk_count per set,
-    both timed around the C calls (tables are released, not copied out);
-    per-set tables of the two forms are compared on a subset.  Each form is
-    timed `reps` times after a warm-up and its median kept: the host copies
-    of one call vary with the host's memory traffic."""
+def run_batched(eng, texts, variant, residency=None, call_jobs=0, reps=3):
+    """jobs/s of dk_count_batch over all sets vs one dk_count per set, both
+    timed around the C calls with the same table residency (tables are
+    released, not copied out).  call_jobs > 0 cuts the batched arm into
+    consecutive calls of that many sets, each call's tables released before
+    the next (a full 4,096-set batch holds more table than host memory)."""
     import dakc_gb300 as dk
-    reps = 3
-    desc = dk.Engine.desc(250, 31, variant, dk.RESIDENT_HOST)
+    residency = dk.RESIDENT_HOST if residency is None else residency
+    desc = dk.Engine.desc(250, 31, variant, residency)
     keep = [dk._buf_ptr(t) for t in texts]
-    eng.count_batch_nocopy(texts, 250, 31, variant)  # warm-up: pools reach steady state
-    t_runs = []
+    step = call_jobs if call_jobs > 0 else len(texts)
+    calls = [texts[i:i + step] for i in range(0, len(texts), step)]
+
+    def batched():
+        nk = nd = 0
+        for c in calls:
+            a, b = eng.count_batch_nocopy(c, 250, 31, variant, residency)
+            nk += a
+            nd += b
+        return nk, nd
+
+    eng.count_batch_nocopy(calls[0], 250, 31, variant, residency)  # warm-up: pools settle
+    t_runs, waves, ms_dev, ms_h2d, ms_d2h, launches = [], 0, 0.0, 0.0, 0.0, 0
+    kms = np.zeros(8)
     for _ in range(reps):
         t0 = time.perf_counter()
-        nk, nd = eng.count_batch_nocopy(texts, 250, 31, variant)
+        nk = nd = 0
+        waves = 0
+        ms_dev = ms_h2d = ms_d2h = 0.0
+        launches = 0
+        kms[:] = 0
+        for c in calls:
+            a, b = eng.count_batch_nocopy(c, 250, 31, variant, residency)
+            nk += a
+            nd += b
+            st = eng.stats()
+            waves += st["n_waves"]
+            ms_dev += st["ms_device"]
+            ms_h2d += st["ms_h2d"]
+            ms_d2h += st["ms_d2h"]
+            launches += st["kernel_launches"]
+            kms += np.asarray(st["ms_kernel"])
         t_runs.append(time.perf_counter() - t0)
     t_batch = float(np.median(t_runs))
-    st = eng.stats()
 
     def one(ptr, n):
         t = eng.count_raw(ptr, n, desc)
         eng.free_table(t)
 
-    for ptr, n, _ in keep:
+    for ptr, n, _ in keep[: min(len(keep), 64)]:
         one(ptr, n)  # warm-up
     lat, p_runs = [], []
     for _ in range(reps):
@@ -279,13 +305,12 @@ def run_batched(eng, texts, variant):
     exact = all(np.array_equal(g.kmers, p.kmers) and np.array_equal(g.counts, p.counts)
                 for g, p in zip(got, (eng.count(t, 250, 31, variant) for t in sub)))
     return {"jobs": len(texts), "k_mers": nk, "distinct": nd, "exact_vs_plain_subset": bool(exact),
+            "residency": "device" if residency == dk.RESIDENT_DEVICE else "host",
             "batched": {"jobs_per_s": len(texts) / t_batch, "kmers_per_s": nk / t_batch,
                         "seconds": t_batch, "seconds_all": [round(x, 5) for x in t_runs],
-                        "waves": st["n_waves"], "ms_device": st["ms_device"],
-                        "ms_h2d": st["ms_h2d"], "ms_d2h": st["ms_d2h"],
-                        "kernel_launches": st["kernel_launches"],
-                        "kernels_ms": {KERNEL_NAMES[i]: round(float(st["ms_kernel"][i]), 3)
-                                       for i in range(8)}},
+                        "calls": len(calls), "waves": waves, "ms_device": ms_dev,
+                        "ms_h2d": ms_h2d, "ms_d2h": ms_d2h, "kernel_launches": launches,
+                        "kernels_ms": {KERNEL_NAMES[i]: round(float(kms[i]), 3) for i in range(8)}},
             "one_job_per_launch": {"jobs_per_s": len(texts) / t_plain, "kmers_per_s": nk / t_plain,
                                    "seconds": t_plain,
                                    "seconds_all": [round(x, 5) for x in p_runs],
@@ -294,12 +319,17 @@ def run_batched(eng, texts, variant):
             "speedup_jobs_per_s": t_plain / t_batch}
 
 
-def run_served(texts, rate, n_jobs, variant, workers, max_batch, seed=5):
+def run_served(texts, rate, n_jobs, variant, workers, max_batch, seed=5, residency=None,
+               mem_budget=0):
     """Open-loop Poisson arrivals at `rate` jobs/s; sizes drawn from the pool.
     The same arrival stream runs once untimed first, so that every worker's
-    device arenas and table pools are at their steady-state sizes."""
+    device arenas and table pools are at their steady-state sizes.  Tables
+    stay where `residency` puts them and are released, not copied out;
+    mem_budget (bytes, 0 = 80% of free memory) is the context's admission
+    budget, split between the workers."""
     import dakc_gb300 as dk
     from dakc_gb300 import synth
+    residency = dk.RESIDENT_HOST if residency is None else residency
     gaps = synth.exponential(seed, n_jobs, rate)
     pick = np.random.Generator(np.random.PCG64(seed)).integers(0, len(texts), n_jobs)
 
@@ -312,16 +342,16 @@ def run_served(texts, rate, n_jobs, variant, workers, max_batch, seed=5):
             now = time.perf_counter()
             if due > now:
                 time.sleep(due - now)
-            tickets.append(eng.submit(texts[pick[i]], 250, 31, variant))
+            tickets.append(eng.submit(texts[pick[i]], 250, 31, variant, residency))
         lat, nk, batches = [], 0, []
         for tk in tickets:
-            _, n_kmers, info = eng.wait_nocopy(tk, 600_000)  # host tables released, not copied
+            _, n_kmers, info = eng.wait_nocopy(tk, 600_000)  # tables released, not copied
             lat.append((info["queued_us"] + info["run_us"]) / 1e3)
             nk += n_kmers
             batches.append(info["batch_jobs"])
         return time.perf_counter() - t0, lat, nk, batches
 
-    with dk.Engine(0) as eng:
+    with dk.Engine(0, mem_budget=mem_budget) as eng:
         eng.serve_start(workers=workers, max_batch_jobs=max_batch)
         stream(eng)  # warm-up pass
         span, lat, nk, batches = stream(eng)
@@ -329,7 +359,9 @@ def run_served(texts, rate, n_jobs, variant, workers, max_batch, seed=5):
     return {"rate": rate, "jobs": n_jobs, "jobs_per_s": n_jobs / span, "kmers_per_s": nk / span,
             "p50_ms": pct(lat, 50), "p99_ms": pct(lat, 99), "p999_ms": pct(lat, 99.9),
             "mean_batch_jobs": float(np.mean(batches)), "workers": workers,
-            "max_batch": max_batch}
+            "max_batch": max_batch,
+            "residency": "device" if residency == dk.RESIDENT_DEVICE else "host",
+            "mem_budget_gb": round(mem_budget / 1e9, 1) if mem_budget else None}
 
 
 def run_formats(steps: int):
@@ -445,6 +477,14 @@ def main():
                     help="batch / serve read sets in pageable memory (staged through pinned slots)")
     ap.add_argument("--no-forms", action="store_true",
                     help="skip the batched / served summaries in the headline line")
+    ap.add_argument("--residency", default="device", choices=["device", "host"],
+                    help="where batch / serve tables stay (both arms alike)")
+    ap.add_argument("--call-jobs", type=int, default=0,
+                    help="batch mode: sets per dk_count_batch call (0 = all in one call)")
+    ap.add_argument("--reps", type=int, default=3, help="batch mode: timed repetitions")
+    ap.add_argument("--workers", type=int, default=2, help="serve mode: workers in both arms")
+    ap.add_argument("--mem-budget-gb", type=float, default=150.0,
+                    help="serve mode: the context's device-memory admission budget")
     args = ap.parse_args()
     rank, world, local = dist_env()
 
@@ -460,16 +500,20 @@ def main():
         pinned = None
         if not args.pageable_jobs:  # reads arrive in page-locked buffers (the engine's ingest)
             pinned, texts = pin_texts(texts)
+        res = dk.RESIDENT_DEVICE if args.residency == "device" else dk.RESIDENT_HOST
         if args.mode == "batch":
             with dk.Engine(local) as eng:
-                out = run_batched(eng, texts, variant)
+                out = run_batched(eng, texts, variant, res, args.call_jobs, args.reps)
             out.update(mode="batch", workload="batch_jobs (first %d of 4,096 sets)" % len(texts),
                        reads_in="pageable" if pinned is None else "pinned (dk_host_alloc)")
             print(json.dumps(out), flush=True)
         else:
+            budget = int(args.mem_budget_gb * 1e9)
             for r in [float(x) for x in args.rates.split(",")]:
-                cb = run_served(texts, r, args.serve_jobs, variant, workers=2, max_batch=1024)
-                one = run_served(texts, r, args.serve_jobs, variant, workers=1, max_batch=1)
+                cb = run_served(texts, r, args.serve_jobs, variant, args.workers, 1024,
+                                residency=res, mem_budget=budget)
+                one = run_served(texts, r, args.serve_jobs, variant, args.workers, 1,
+                                 residency=res, mem_budget=budget)
                 print(json.dumps({"mode": "serve", "continuous_batching": cb,
                                   "one_job_per_launch": one}), flush=True)
         return 0
@@ -610,11 +654,18 @@ def main():
     forms = None
     if rank == 0 and world == 1 and not args.no_forms:
         pinned_forms, texts = pin_texts(job_pool(64))
-        forms = {"batched": run_batched(eng, texts, variant),
-                 "served": {"continuous_batching": run_served(texts, 2000.0, 64, variant, 2, 1024),
-                            "one_job_per_launch": run_served(texts, 2000.0, 64, variant, 1, 1)},
-                 "note": "first 64 sets of the 4,096-set batched workload; served: Poisson "
-                         "2,000 jobs/s (the top offered rate; --mode serve sweeps 10-2,000)"}
+        budget = int(args.mem_budget_gb * 1e9)
+        forms = {"batched": run_batched(eng, texts, variant, dk.RESIDENT_DEVICE),
+                 "served": {"continuous_batching": run_served(texts, 2000.0, 64, variant, 2, 1024,
+                                                              residency=dk.RESIDENT_DEVICE,
+                                                              mem_budget=budget),
+                            "one_job_per_launch": run_served(texts, 2000.0, 64, variant, 2, 1,
+                                                             residency=dk.RESIDENT_DEVICE,
+                                                             mem_budget=budget)},
+                 "note": "first 64 sets of the 4,096-set batched workload, tables left on the "
+                         "device in both arms; served: Poisson 2,000 jobs/s (the top offered "
+                         "rate; --mode serve sweeps 10-2,000), 2 workers in both arms, "
+                         f"{args.mem_budget_gb:g} GB admission budget"}
 
     if rank == 0:
         line = {
@@ -642,6 +693,7 @@ def main():
             "kernels_ms_per_step": {KERNEL_NAMES[i]: float(kms[i]) for i in range(8)},
             "n_kmers": nk, "n_distinct": nd, "partition_levels": sts[0]["partition_levels"],
             "n_bins": sts[0]["n_bins"], "n_bins_resorted": sts[0]["n_bins_resorted"],
+            "n_bins_packed": sts[0]["n_bins_packed"], "n_bins_fallback": sts[0]["n_bins_fallback"],
             "wall_ms_per_step": (w1 - w0) * 1000.0 / args.steps,
             "clocks": clk,
             "e2e": e2e,

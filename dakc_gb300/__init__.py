@@ -126,10 +126,12 @@ _lib = None
 
 
 def load_library(path: str = LIB_PATH):
-    """Load the engine library (build it first if it is absent and nvcc exists)."""
+    """Load the engine library (build it first if it is absent and nvcc exists).
+    DAKC_GB300_LIB, when set, names another build of the library to load."""
     global _lib
     if _lib is not None:
         return _lib
+    path = os.environ.get("DAKC_GB300_LIB", path)
     if not os.path.exists(path):
         from . import build as _b
         _b.build_engine()
@@ -341,7 +343,8 @@ class Engine:
             self.free_table(t)
             del keep
 
-    def count_batch_nocopy(self, texts, line_width: int, k: int, variant: int = VARIANT_AUTO):
+    def count_batch_nocopy(self, texts, line_width: int, k: int, variant: int = VARIANT_AUTO,
+                           residency: int = RESIDENT_HOST):
         """dk_count_batch without copying the tables out; returns (n_kmers, n_distinct)."""
         keep = [_buf_ptr(t) for t in texts]
         jobs = (Job * max(1, len(texts)))()
@@ -349,7 +352,7 @@ class Engine:
             jobs[j].text = ptr
             jobs[j].nbytes = n
         outs = (Table * max(1, len(texts)))()
-        d = self.desc(line_width, k, variant)
+        d = self.desc(line_width, k, variant, residency)
         self._check(self.lib.dk_count_batch(self.h, jobs, len(texts), ctypes.byref(d), outs),
                     "dk_count_batch")
         nk = sum(int(outs[j].n_kmers) for j in range(len(texts)))
@@ -359,16 +362,17 @@ class Engine:
                 self.free_table(outs[j])
         return nk, nd
 
-    def count_batch_raw(self, texts, line_width: int, k: int, variant: int = VARIANT_AUTO):
+    def count_batch_raw(self, texts, line_width: int, k: int, variant: int = VARIANT_AUTO,
+                        residency: int = RESIDENT_HOST):
         """dk_count_batch returning the raw dk_table structs (still owned by the
-        engine: copy with table_result, release with free_table)."""
+        engine: copy host tables with table_result, release with free_table)."""
         keep = [_buf_ptr(t) for t in texts]
         jobs = (Job * max(1, len(texts)))()
         for j, (ptr, n, _) in enumerate(keep):
             jobs[j].text = ptr
             jobs[j].nbytes = n
         outs = (Table * max(1, len(texts)))()
-        d = self.desc(line_width, k, variant)
+        d = self.desc(line_width, k, variant, residency)
         self._check(self.lib.dk_count_batch(self.h, jobs, len(texts), ctypes.byref(d), outs),
                     "dk_count_batch")
         return [outs[j] for j in range(len(texts))]
@@ -422,10 +426,11 @@ class Engine:
         self._check(self.lib.dk_serve_stop(self.h), "dk_serve_stop")
         self._inflight = {}
 
-    def submit(self, text, line_width: int, k: int, variant: int = VARIANT_AUTO) -> int:
+    def submit(self, text, line_width: int, k: int, variant: int = VARIANT_AUTO,
+               residency: int = RESIDENT_HOST) -> int:
         ptr, n, keep = _buf_ptr(text)
         t = ctypes.c_uint64(0)
-        d = self.desc(line_width, k, variant)
+        d = self.desc(line_width, k, variant, residency)
         self._check(self.lib.dk_submit(self.h, ctypes.c_void_p(ptr), n, ctypes.byref(d),
                                        ctypes.byref(t)), "dk_submit")
         self._inflight[t.value] = keep  # the text is borrowed until the job completes
@@ -461,6 +466,19 @@ class Engine:
         if rc == DK_ERR_TIMEOUT:
             raise DkError(rc, "dk_wait timed out")
         return self._take(ticket, rc, t, info)
+
+    def wait_raw(self, ticket: int, timeout_ms: int = 60_000):
+        """dk_wait returning the raw dk_table (host or device resident; release
+        it with free_table) and the job info; None while pending."""
+        t, info = Table(), JobInfo()
+        rc = self.lib.dk_wait(self.h, ticket, timeout_ms, ctypes.byref(t), ctypes.byref(info))
+        if rc == DK_ERR_TIMEOUT:
+            raise DkError(rc, "dk_wait timed out")
+        if rc == DK_ERR_PENDING:
+            return None
+        self._inflight.pop(ticket, None)
+        self._check(rc, "served job")
+        return t, {f: getattr(info, f) for f, _ in info._fields_}
 
     def wait_nocopy(self, ticket: int, timeout_ms: int = 60_000):
         """Like wait(), but the table is released without being copied out:

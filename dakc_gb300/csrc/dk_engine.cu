@@ -377,10 +377,14 @@ int Engine::count_batch(const dk_job* jobs, int njobs, const dk_input_desc* desc
   for (int j = 0; j < njobs; ++j) std::memset(&outs[j], 0, sizeof(dk_table));
   if (desc->k < 1 || desc->k > 32 || desc->line_width < 1 || desc->line_width > 1024 ||
       !convention_ok(*desc) || desc->variant < DK_VARIANT_AUTO ||
-      desc->variant > DK_VARIANT_HASH || desc->residency != DK_RESIDENT_HOST) {
-    set_error("invalid input descriptor (batch results are host-resident)");
+      desc->variant > DK_VARIANT_HASH ||
+      (desc->residency != DK_RESIDENT_HOST && desc->residency != DK_RESIDENT_DEVICE)) {
+    set_error("invalid input descriptor");
     return DK_ERR_INVALID_ARG;
   }
+  // device residency: each wave's device table is handed out as it is (its
+  // jobs' tables are runs of it), nothing is copied back
+  const bool on_dev = desc->residency == DK_RESIDENT_DEVICE;
   const int W = desc->line_width, k = desc->k;
   const uint64_t stride = (uint64_t)W + 1;
   const uint64_t per_line = W >= k ? (uint64_t)(W - k + 1) : 0;
@@ -546,26 +550,34 @@ int Engine::count_batch(const dk_job* jobs, int njobs, const dk_input_desc* desc
       stats_batch.n_bins += stats.n_bins;
       stats_batch.n_partitioned += stats.n_partitioned;
       stats_batch.n_bins_resorted += stats.n_bins_resorted;
+      stats_batch.n_bins_packed += stats.n_bins_packed;
+      stats_batch.n_bins_fallback += stats.n_bins_fallback;
       stats_batch.partition_levels = std::max(stats_batch.partition_levels, stats.partition_levels);
       stats_batch.variant_used = stats.variant_used;
-      // the wave's table goes back on s_out while the next wave runs
       TableBuf* h_tb = nullptr;
-      r = acquire_table(std::max<uint64_t>(dt.n, 1), false, &h_tb);
-      if (r != DK_OK) {
-        release_table(dev_tb[b]->id);
+      if (on_dev) {
+        // the jobs hold the wave's device table until each is freed
+        h_tb = dev_tb[b];
         dev_tb[b] = nullptr;
-        return r;
-      }
-      DK_CUDA(cudaEventRecord(ev_stage[7], stream));
-      DK_CUDA(cudaStreamWaitEvent(s_out, ev_stage[7], 0));
-      DK_CUDA(cudaEventRecord(ev_out0[b], s_out));
-      if (dt.n) {
-        DK_CUDA(cudaMemcpyAsync(h_tb->k, dev_tb[b]->k, dt.n * 8, cudaMemcpyDeviceToHost, s_out));
-        DK_CUDA(cudaMemcpyAsync(h_tb->c, dev_tb[b]->c, dt.n * 4, cudaMemcpyDeviceToHost, s_out));
-      }
-      DK_CUDA(cudaEventRecord(ev_out1[b], s_out));
-      out_pending[b] = true;
-      {
+        std::lock_guard<std::mutex> pg(pool_mu);
+        h_tb->refs = (uint32_t)nj;
+      } else {
+        // the wave's table goes back on s_out while the next wave runs
+        r = acquire_table(std::max<uint64_t>(dt.n, 1), false, &h_tb);
+        if (r != DK_OK) {
+          release_table(dev_tb[b]->id);
+          dev_tb[b] = nullptr;
+          return r;
+        }
+        DK_CUDA(cudaEventRecord(ev_stage[7], stream));
+        DK_CUDA(cudaStreamWaitEvent(s_out, ev_stage[7], 0));
+        DK_CUDA(cudaEventRecord(ev_out0[b], s_out));
+        if (dt.n) {
+          DK_CUDA(cudaMemcpyAsync(h_tb->k, dev_tb[b]->k, dt.n * 8, cudaMemcpyDeviceToHost, s_out));
+          DK_CUDA(cudaMemcpyAsync(h_tb->c, dev_tb[b]->c, dt.n * 4, cudaMemcpyDeviceToHost, s_out));
+        }
+        DK_CUDA(cudaEventRecord(ev_out1[b], s_out));
+        out_pending[b] = true;
         std::lock_guard<std::mutex> pg(hpool->mu);
         h_tb->refs = (uint32_t)nj;
       }
@@ -584,7 +596,7 @@ int Engine::count_batch(const dk_job* jobs, int njobs, const dk_input_desc* desc
         t.counts = (uint32_t*)h_tb->c + off;
         t.n = d;
         t.n_kmers = n;
-        t.on_device = 0;
+        t.on_device = on_dev ? 1 : 0;
         t.variant_used = stats.variant_used;
         t.handle = h_tb->id;
       }

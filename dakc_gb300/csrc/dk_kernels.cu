@@ -1692,11 +1692,12 @@ __device__ bool bin_hashed(Node* nodes, uint32_t ni, const Node& nd, uint64_t* k
 // bottom.  Entries compare as the keys they hold, 0 is an empty slot, a new
 // key enters with one 64-bit CAS and a repeat adds to the low 32-bit word.
 // Normal bins are counted this way by their own kernel (k_bin_packed), whose
-// small shared-memory footprint fits three 512-thread CTAs per SM: a bin's
-// work is a chain of dependent shared-memory steps, so throughput follows the
-// number of bins in flight (3 CTAs: 14.7 ms per 2.4 G keys of C2-shaped bins,
-// 2 CTAs with twice the table: 18.8 ms).  Bins it cannot take go to a list
-// that k_bin_count handles after it.
+// small shared-memory footprint (53 KB) and 30 registers fit four 512-thread
+// CTAs per SM: a bin's work is a chain of dependent shared-memory steps, so
+// more bins in flight is what pays (2.4 G keys of large_100m: 20.1 ms with 4
+// CTAs and 4 keys per thread per batch, 20.2 ms with 3 CTAs and 8 keys, 21.5
+// ms with 2 keys; the general kernel at 2 CTAs: 22.8 ms).  Bins it cannot
+// take go to a list that k_bin_count handles after it.
 constexpr int kPackSlotBits = 12;
 constexpr uint32_t kPackSlots = 1u << kPackSlotBits;  // 32 KB of table
 constexpr uint32_t kPackMaxDistinct = 2048;            // sorted entries (16 KB)
@@ -1704,7 +1705,11 @@ constexpr int kPackDigitBits = 10;                     // counting-sort digits (
 constexpr uint32_t kPackMaxProbe = 64;
 constexpr int kPackMaxShift = 50;  // the count field keeps >= 14 bits
 constexpr int kPackThreads = 512;
-constexpr int kPackBlocksPerSM = 3;
+constexpr int kPackBlocksPerSM = 4;
+#ifndef DK_PACK_BATCH
+#define DK_PACK_BATCH 4
+#endif
+constexpr int kPackBatch = DK_PACK_BATCH;  // keys a thread loads before inserting them
 constexpr size_t kPackSmem = kPackSlots * 8 + kPackMaxDistinct * 8 + (4u << kPackDigitBits);
 static_assert(kBinCap < (1 << (64 - kPackMaxShift)), "a bin's largest count fits the count field");
 static_assert(kPackMaxDistinct * 12 <= kPackSlots * 8, "the output stage fits the table");
@@ -1743,7 +1748,7 @@ __device__ __forceinline__ bool pack_insert(unsigned long long* tab, unsigned lo
 // when a probe runs too long or the bin holds more than kPackMaxDistinct keys.
 __device__ bool bin_packed(Node* nodes, uint32_t ni, const Node& nd, uint64_t* keys, uint32_t* cnt,
                            unsigned long long* region, uint32_t* tmp, uint32_t* mark,
-                           uint32_t* flags, bool hot) {
+                           uint32_t* flags) {
   constexpr uint32_t T = kPackThreads;
   unsigned long long* tab = region;                                          // kPackSlots
   unsigned long long* sorted = region + kPackSlots;                          // by digit
@@ -1771,8 +1776,11 @@ __device__ bool bin_packed(Node* nodes, uint32_t ni, const Node& nd, uint64_t* k
   if (threadIdx.x == 0) flags[1] = 0;
   __syncthreads();
   DK_PHASE(11);
-  constexpr int kBatch = 8;
+  constexpr int kBatch = kPackBatch;
   bool ok = true;
+  // a warp whose first 32 keys repeat one key four times or more holds a hot
+  // k-mer: its copies then insert once per warp with their multiplicity
+  bool hot = false;
   for (uint32_t i0 = 0; i0 < n; i0 += kBatch * T) {
     unsigned long long kk[kBatch];
 #pragma unroll
@@ -1787,6 +1795,10 @@ __device__ bool bin_packed(Node* nodes, uint32_t ni, const Node& nd, uint64_t* k
       const unsigned long long rk = kk[u] << cbits;
       uint32_t mult = 1;
       bool live = valid;
+      if (i0 == 0 && u == 0) {
+        const uint32_t peers = __match_any_sync(0xFFFFFFFFu, rk) & __ballot_sync(0xFFFFFFFFu, valid);
+        hot = __reduce_max_sync(0xFFFFFFFFu, valid ? (uint32_t)__popc(peers) : 0u) >= 4;
+      }
       if (hot) {  // copies of one key in this warp insert once with their multiplicity
         const uint32_t vm = __ballot_sync(0xFFFFFFFFu, valid);
         const uint32_t peers = __match_any_sync(0xFFFFFFFFu, rk) & vm;
@@ -1864,7 +1876,8 @@ __device__ bool bin_packed(Node* nodes, uint32_t ni, const Node& nd, uint64_t* k
 }
 
 // Persistent packed-bin counter over the final list: CTAs take bins by
-// ticket (ctr[19]) and pull the next bin's keys into L2 while counting one.
+// ticket (ctr[19]); while the CTA counts one bin, one thread takes the next
+// ticket, stages that bin's node in shared memory and pulls its keys into L2.
 // Bins it does not count -- dense ones (at most kDenseBits free bits), ones
 // with more than kPackMaxShift free bits, and ones the packed table cannot
 // hold -- are appended to fb_list (ctr[20] entries) for k_bin_count; ctr[21]
@@ -1875,39 +1888,37 @@ __global__ void __launch_bounds__(kPackThreads, kPackBlocksPerSM)
   extern __shared__ __align__(16) unsigned long long region[];
   __shared__ uint32_t tmp[64];
   __shared__ uint32_t mark[(1u << kPackDigitBits) / 32];
-  __shared__ uint32_t s_bin;
   __shared__ uint32_t flags[2];
-  __shared__ bool s_hot;
+  // the current and the next bin: ticket, node index and node, so that one
+  // thread fetches the next bin's node while the CTA counts the current one
+  __shared__ uint32_t s_b[2], s_ni[2];
+  __shared__ Node s_node[2];
   unsigned int* ticket = reinterpret_cast<unsigned int*>(&ctr[19]);
-  if (threadIdx.x == 0) s_bin = atomicAdd(ticket, 1u);
+  auto take = [&](int slot) {
+    const uint32_t nb = atomicAdd(ticket, 1u);
+    s_b[slot] = nb;
+    if (nb < n_bins) {
+      const uint32_t nn = finals[nb];
+      const Node nx = nodes[nn];
+      s_ni[slot] = nn;
+      s_node[slot] = nx;
+      prefetch_l2_range((nx.buf ? B : A) + nx.start, nx.n * 8);
+    }
+  };
+  if (threadIdx.x == 32) take(0);
   __syncthreads();
-  for (;;) {
-    const uint32_t b = s_bin;
+  for (int cur = 0;; cur ^= 1) {
+    const uint32_t b = s_b[cur];
     if (b >= n_bins) break;
-    const uint32_t ni = finals[b];
-    const Node nd = nodes[ni];
+    const uint32_t ni = s_ni[cur];
+    const Node nd = s_node[cur];
     uint64_t* keys = (nd.buf ? B : A) + nd.start;
     uint32_t* cnt = C + nd.start;
-    __syncthreads();  // every thread has read s_bin
-    if (threadIdx.x == 32) {
-      const uint32_t nb = atomicAdd(ticket, 1u);
-      s_bin = nb;
-      if (nb < n_bins) {
-        const Node& nx = nodes[finals[nb]];
-        prefetch_l2_range((nx.buf ? B : A) + nx.start, nx.n * 8);
-      }
-    }
+    if (threadIdx.x == 32) take(cur ^ 1);
     const bool eligible = nd.shift > kDenseBits && nd.shift <= kPackMaxShift &&
                           nd.n <= (uint64_t)kBinCap;
-    if (eligible && threadIdx.x < 32) {  // hot bin: a 32-key sample repeats a key >= 4 times
-      const uint64_t smp = nd.n ? __ldg(keys + (nd.n * threadIdx.x) / 32) : 0ull;
-      const uint32_t peers = __match_any_sync(0xFFFFFFFFu, smp);
-      const uint32_t dup = __reduce_max_sync(0xFFFFFFFFu, (uint32_t)__popc(peers));
-      if (threadIdx.x == 0) s_hot = dup >= 4;
-    }
-    __syncthreads();
     bool done = false;
-    if (eligible) done = bin_packed(nodes, ni, nd, keys, cnt, region, tmp, mark, flags, s_hot);
+    if (eligible) done = bin_packed(nodes, ni, nd, keys, cnt, region, tmp, mark, flags);
     if (threadIdx.x == 0) {
       if (done) {
         atomicAdd(&ctr[21], 1ull);

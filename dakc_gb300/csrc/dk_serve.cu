@@ -13,8 +13,10 @@
 //     and counts them with one dk_count_batch pipeline.  Jobs that arrive
 //     while other workers run are picked up by the next free worker, so their
 //     work overlaps on the device.
-//   * dk_poll / dk_wait return the job's host-resident table; dk_table_free
-//     releases it.  Waits are bounded by the caller's timeout.
+//   * dk_poll / dk_wait return the job's table -- host-resident, or left in
+//     device memory when the job's descriptor asks for device residency (then
+//     it stays valid until dk_serve_stop); dk_table_free releases it.  Waits
+//     are bounded by the caller's timeout.
 #include "dk_engine.hpp"
 #include "../../include/dakc_gb300.h"
 
@@ -101,7 +103,8 @@ struct Server {
              it != queue.end() && (int)batch.size() < max_batch && kmers < kBatchKmers;) {
           const auto& r = *it;
           const bool same = r->desc.line_width == d0.line_width && r->desc.k == d0.k &&
-                            r->desc.variant == d0.variant;
+                            r->desc.variant == d0.variant &&
+                            r->desc.residency == d0.residency;
           if (same && (batch.empty() || bytes + r->est <= (uint64_t)(0.7 * (double)me.budget))) {
             bytes += r->est;
             kmers += r->kmers;
@@ -117,8 +120,7 @@ struct Server {
       std::vector<dk_job> jv(batch.size());
       std::vector<dk_table> outs(batch.size());
       for (size_t i = 0; i < batch.size(); ++i) jv[i] = {batch[i]->text, batch[i]->nbytes};
-      dk_input_desc d = batch[0]->desc;
-      d.residency = DK_RESIDENT_HOST;
+      dk_input_desc d = batch[0]->desc;  // host or device tables, as the jobs asked
       const int rc = me.eng->count_batch(jv.data(), (int)jv.size(), &d, outs.data());
       {
         std::lock_guard<std::mutex> lk(mu);

@@ -183,9 +183,10 @@ int dk_last_stats(dk_ctx* ctx, dk_stats* out);
  * the reference would run one kmercounter per set (kcounter.hpp:84-99); here
  * every set is its own level-1 partition of one launch sequence, processed in
  * waves sized to the context's memory budget (up to 4,096 sets per wave).
- * outs[j] receives job j's sorted table (host-resident; tables of one wave
- * share one allocation, each must still be released with dk_table_free).
- * Per-job tables equal dk_count's on that job's text. */
+ * outs[j] receives job j's sorted table, host- or device-resident as
+ * desc->residency asks (tables of one wave share one allocation, each must
+ * still be released with dk_table_free; device-resident tables are never
+ * copied back).  Per-job tables equal dk_count's on that job's text. */
 int dk_count_batch(dk_ctx* ctx, const dk_job* jobs, int njobs, const dk_input_desc* desc,
                    dk_table* outs);
 
@@ -271,10 +272,12 @@ int dk_table_pairs(dk_ctx* ctx, const dk_table* t, void* out);
  * are admitted by an estimate of their device memory, queue, and are
  * coalesced into batched launches (dk_count_batch) by whichever worker frees
  * up first, so work of jobs that arrive while others run overlaps on the
- * device.  No counterpart in the reference (one kmercounter per run). */
+ * device.  A job's table is host-resident, or stays in device memory when
+ * its descriptor asks for DK_RESIDENT_DEVICE (valid until dk_serve_stop).
+ * No counterpart in the reference (one kmercounter per run). */
 typedef struct {
   double queued_us;  /* submit -> start of its batch                      */
-  double run_us;     /* start of its batch -> table ready on the host     */
+  double run_us;     /* start of its batch -> its table ready               */
   int batch_jobs;    /* jobs in the batch it ran in                       */
   int worker;
 } dk_job_info;

@@ -200,6 +200,43 @@ def ref_table(text, line_width: int, k: int, pes: int = 1, hitter: int = 0, time
         return read_table_file(out), p.stdout
 
 
+def pakman_binary(k: int, build: bool = True) -> str | None:
+    """Path of PakMan*'s k-mer counting built against the one-rank MPI
+    stand-in (oracle/_ref/pakman_ref_k<k>); None when unavailable."""
+    path = os.path.join(REF_DIR, f"pakman_ref_k{k}")
+    if os.path.exists(path):
+        return path
+    if not build or not os.path.isdir(os.path.join(REFERENCE_TREE, "pakman_star", "src")):
+        return None
+    subprocess.run(["make", "-s", "-C", HERE, "pakman", f"K={k}", f"REF={REFERENCE_TREE}"],
+                   check=True)
+    return path
+
+
+def pakman_ref_table(fasta, k: int, batch: int = 100_000_000, timeout: float = 600):
+    """Run PakMan*'s own k-mer counting (one rank) on a FASTA buffer; returns
+    (keys, counts) sorted by k-mer."""
+    exe = pakman_binary(k)
+    if exe is None:
+        raise OracleError("PakMan* binary unavailable (reference tree absent)")
+    buf = _as_bytes(fasta)
+    with tempfile.TemporaryDirectory() as d:
+        inp = os.path.join(d, "reads.fa")
+        out = os.path.join(d, "table.bin")
+        buf.tofile(inp)
+        p = subprocess.run([exe, inp, str(batch), out], capture_output=True, text=True,
+                           timeout=timeout)
+        if p.returncode != 0:
+            raise OracleError(f"PakMan* exited {p.returncode}: {p.stderr.strip()[:200]}")
+        with open(out, "rb") as f:
+            raw = f.read()
+    if raw[:4] != b"PKT1":
+        raise OracleError("bad table file")
+    n = int(np.frombuffer(raw, np.uint64, 1, 4)[0])
+    rec = np.frombuffer(raw, dtype=np.dtype([("k", "<u8"), ("c", "<u4")]), count=n, offset=12)
+    return rec["k"].copy(), rec["c"].copy()
+
+
 def pakman_histogram_cutoff(counts, num_buckets: int):
     """PakMan*'s count histogram and min-bucket cut-off, restated from
     pakman_star/src/kmer_histogram.cpp:72-130: hist[c] = distinct k-mers with

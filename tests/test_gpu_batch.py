@@ -116,3 +116,37 @@ def test_batch_tables_free_while_another_batch_runs():
     for j, r in enumerate(out["second"]):
         keys, counts, nk = expect[15 + j]
         assert r.n_kmers == nk and np.array_equal(r.kmers, keys), 15 + j
+
+
+@pytest.mark.parametrize("variant", [dk.VARIANT_SORT, dk.VARIANT_HASH])
+def test_batch_device_resident_tables(engine, variant):
+    """With device residency each job's table stays in device memory (no copy
+    back) and equals the oracle's; freeing them in any order releases the
+    wave's buffer only with its last job."""
+    import ctypes
+    import torch
+    texts = job_texts(24, seed=7)
+    outs = engine.count_batch_raw(texts, 250, 31, variant, dk.RESIDENT_DEVICE)
+    try:
+        for j, t in enumerate(texts):
+            keys, counts, nk = pyoracle.count(t, 250, 31)
+            o = outs[j]
+            assert o.on_device == 1 and int(o.n_kmers) == nk and int(o.n) == keys.size
+            n = int(o.n)
+            if n == 0:
+                continue
+            kp = ctypes.cast(o.kmers, ctypes.c_void_p).value
+            cp = ctypes.cast(o.counts, ctypes.c_void_p).value
+
+            class _A:
+                def __init__(self, p, typestr):
+                    self.__cuda_array_interface__ = {"shape": (n,), "typestr": typestr,
+                                                     "data": (p, False), "version": 3}
+            gk = torch.as_tensor(_A(kp, "<i8"), device="cuda").cpu().numpy().view(np.uint64)
+            gc = torch.as_tensor(_A(cp, "<i4"), device="cuda").cpu().numpy().view(np.uint32)
+            assert np.array_equal(gk, keys), j
+            assert np.array_equal(gc, counts), j
+    finally:
+        for o in reversed(outs):
+            if o.handle:
+                engine.free_table(o)

@@ -90,3 +90,30 @@ def test_format_edge_cases(engine):
         engine.count_format(b"ACGTACGTAC\n", dk.FORMAT_LINES, 3, dk.CONV_DAKC, line_width=5)
     with pytest.raises(dk.DkError):       # PakMan* lines are limited to 256 bytes
         engine.count_format(b">h\n" + b"A" * 300 + b"\n", dk.FORMAT_FASTA, 3, dk.CONV_PAKMAN)
+
+
+import glob  # noqa: E402
+import os  # noqa: E402
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+FORMAT_FIXTURES = sorted(glob.glob(os.path.join(GOLDEN, "formats", "formats_*.npz")))
+
+
+@pytest.mark.parametrize("path", FORMAT_FIXTURES, ids=[os.path.basename(p)[:-4] for p in FORMAT_FIXTURES])
+@pytest.mark.parametrize("k", [21, 31])
+def test_formats_match_reference_runs(engine, path, k):
+    """FASTQ through dk_count_format equals DAKC's table of fq2txtmaker.sh's
+    text, and the same reads as FASTA (fq2famaker.sh) under the PakMan*
+    convention equal PakMan*'s own table -- both produced by running the
+    reference's code (tests/golden/make_formats.py)."""
+    z = np.load(path)
+    r, width = engine.count_format(z["fastq"].tobytes(), dk.FORMAT_FASTQ, k, dk.CONV_DAKC)
+    assert width == int(z["W"])
+    assert r.n_kmers == int(z[f"dakc_nk_k{k}"])
+    assert np.array_equal(r.kmers, z[f"dakc_keys_k{k}"])
+    assert np.array_equal(r.counts, z[f"dakc_counts_k{k}"])
+    for variant in (dk.VARIANT_HASH, dk.VARIANT_SORT):
+        r, _ = engine.count_format(z["fa"].tobytes(), dk.FORMAT_FASTA, k, dk.CONV_PAKMAN,
+                                   variant=variant)
+        assert np.array_equal(r.kmers, z[f"pakman_keys_k{k}"]), variant
+        assert np.array_equal(r.counts, z[f"pakman_counts_k{k}"]), variant

@@ -170,3 +170,41 @@ def test_served_tables_share_the_context_pool_and_outlive_the_server():
             assert np.array_equal(np.ctypeslib.as_array(tab.kmers, shape=(n,)), keys), j
             assert np.array_equal(np.ctypeslib.as_array(tab.counts, shape=(n,)), counts), j
             eng.free_table(tab)
+
+
+def test_served_device_resident_tables():
+    """Jobs submitted with device residency get tables left in device memory
+    (no copy back), equal to the oracle's; host and device jobs mix."""
+    import ctypes
+    import torch
+    jobs = texts(10, 16)
+    with dk.Engine(0) as eng:
+        eng.serve_start(workers=2, max_batch_jobs=8)
+        tks = [(eng.submit(t, 250, 31, dk.VARIANT_AUTO,
+                           dk.RESIDENT_DEVICE if j % 3 else dk.RESIDENT_HOST), j)
+               for j, t in enumerate(jobs)]
+        for tk, j in tks:
+            t, info = eng.wait_raw(tk, 120_000)
+            try:
+                keys, counts, nk = pyoracle.count(jobs[j], 250, 31)
+                assert int(t.n_kmers) == nk and int(t.n) == keys.size
+                assert t.on_device == (1 if j % 3 else 0)
+                n = int(t.n)
+                if n and t.on_device:
+                    class _A:
+                        def __init__(self, p, typestr):
+                            self.__cuda_array_interface__ = {"shape": (n,), "typestr": typestr,
+                                                             "data": (p, False), "version": 3}
+                    kp = ctypes.cast(t.kmers, ctypes.c_void_p).value
+                    cp = ctypes.cast(t.counts, ctypes.c_void_p).value
+                    gk = torch.as_tensor(_A(kp, "<i8"), device="cuda").cpu().numpy().view(np.uint64)
+                    gc = torch.as_tensor(_A(cp, "<i4"), device="cuda").cpu().numpy().view(np.uint32)
+                elif n:
+                    gk = np.ctypeslib.as_array(t.kmers, shape=(n,)).copy()
+                    gc = np.ctypeslib.as_array(t.counts, shape=(n,)).copy()
+                else:
+                    gk, gc = np.zeros(0, np.uint64), np.zeros(0, np.uint32)
+                assert np.array_equal(gk, keys) and np.array_equal(gc, counts)
+            finally:
+                eng.free_table(t)
+        eng.serve_stop()

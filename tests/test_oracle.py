@@ -230,3 +230,27 @@ def test_pakman_kmers_known_answer():
     assert got.tolist() == [((0 << 2) | 7) & 15, ((7 << 2) | 1) & 15]
     assert pyoracle.format_lines(fa, "fasta") == [b"ACGTA", b"GG", b"TTT"]
     assert pyoracle.format_lines(b"x\n>a\nC\n", "fasta") == [b"C"]
+
+
+FORMAT_FIXTURES = sorted(glob.glob(os.path.join(GOLDEN, "formats", "formats_*.npz")))
+
+
+@pytest.mark.parametrize("path", FORMAT_FIXTURES, ids=[os.path.basename(p)[:-4] for p in FORMAT_FIXTURES])
+def test_format_restatements_match_reference_runs(path):
+    """The restatements behind the read-format rows reproduce what the
+    reference's own code produced on the same input: fq2txtmaker.sh's text
+    (run with bash/awk/sed), DAKC's table of that text, and PakMan*'s table of
+    fq2famaker.sh's FASTA (kmer_counting.cpp compiled unmodified, one rank)."""
+    z = np.load(path)
+    fq, txt, fa, W = z["fastq"].tobytes(), z["txt"].tobytes(), z["fa"].tobytes(), int(z["W"])
+    with open(os.path.join(GOLDEN, "formats", "formats.json")) as f:
+        ent = json.load(f)["cases"][os.path.basename(path)[:-4]]
+    assert hashlib.sha256(fq).hexdigest() == ent["fastq_sha256"]
+    got_txt, w = pyoracle.fq2txt(fq)
+    assert w == W and got_txt == txt
+    for k in (21, 31):
+        keys, counts, nk = pyoracle.count(np.frombuffer(txt, np.uint8), W, k)
+        assert nk == int(z[f"dakc_nk_k{k}"])
+        assert np.array_equal(keys, z[f"dakc_keys_k{k}"]) and np.array_equal(counts, z[f"dakc_counts_k{k}"])
+        pk, pc, _ = pyoracle.table_of(pyoracle.pakman_kmers(fa, k))
+        assert np.array_equal(pk, z[f"pakman_keys_k{k}"]) and np.array_equal(pc, z[f"pakman_counts_k{k}"])
