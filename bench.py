@@ -240,7 +240,7 @@ def pct(xs, p):
     return float(np.percentile(np.asarray(xs, dtype=np.float64), p)) if len(xs) else None
 
 
-def run_batched(eng, texts, variant, residency=None, call_jobs=0, reps=3):
+def run_batched(eng, texts, variant, residency=None, call_jobs=0, reps=3, bin_target=0):
     """jobs/s of dk_count_batch over all sets vs one dk_count per set, both
     timed around the C calls with the same table residency (tables are
     released, not copied out).  call_jobs > 0 cuts the batched arm into
@@ -248,7 +248,7 @@ def run_batched(eng, texts, variant, residency=None, call_jobs=0, reps=3):
     the next (a full 4,096-set batch holds more table than host memory)."""
     import dakc_gb300 as dk
     residency = dk.RESIDENT_HOST if residency is None else residency
-    desc = dk.Engine.desc(250, 31, variant, residency)
+    desc = dk.Engine.desc(250, 31, variant, residency, 0, bin_target)
     keep = [dk._buf_ptr(t) for t in texts]
     step = call_jobs if call_jobs > 0 else len(texts)
     calls = [texts[i:i + step] for i in range(0, len(texts), step)]
@@ -256,13 +256,14 @@ def run_batched(eng, texts, variant, residency=None, call_jobs=0, reps=3):
     def batched():
         nk = nd = 0
         for c in calls:
-            a, b = eng.count_batch_nocopy(c, 250, 31, variant, residency)
+            a, b = eng.count_batch_nocopy(c, 250, 31, variant, residency, bin_target)
             nk += a
             nd += b
         return nk, nd
 
-    eng.count_batch_nocopy(calls[0], 250, 31, variant, residency)  # warm-up: pools settle
+    eng.count_batch_nocopy(calls[0], 250, 31, variant, residency, bin_target)  # warm-up
     t_runs, waves, ms_dev, ms_h2d, ms_d2h, launches = [], 0, 0.0, 0.0, 0.0, 0
+    packed = fallback = 0
     kms = np.zeros(8)
     for _ in range(reps):
         t0 = time.perf_counter()
@@ -270,9 +271,10 @@ def run_batched(eng, texts, variant, residency=None, call_jobs=0, reps=3):
         waves = 0
         ms_dev = ms_h2d = ms_d2h = 0.0
         launches = 0
+        packed = fallback = 0
         kms[:] = 0
         for c in calls:
-            a, b = eng.count_batch_nocopy(c, 250, 31, variant, residency)
+            a, b = eng.count_batch_nocopy(c, 250, 31, variant, residency, bin_target)
             nk += a
             nd += b
             st = eng.stats()
@@ -281,6 +283,8 @@ def run_batched(eng, texts, variant, residency=None, call_jobs=0, reps=3):
             ms_h2d += st["ms_h2d"]
             ms_d2h += st["ms_d2h"]
             launches += st["kernel_launches"]
+            packed += st["n_bins_packed"]
+            fallback += st["n_bins_fallback"]
             kms += np.asarray(st["ms_kernel"])
         t_runs.append(time.perf_counter() - t0)
     t_batch = float(np.median(t_runs))
@@ -310,6 +314,7 @@ def run_batched(eng, texts, variant, residency=None, call_jobs=0, reps=3):
                         "seconds": t_batch, "seconds_all": [round(x, 5) for x in t_runs],
                         "calls": len(calls), "waves": waves, "ms_device": ms_dev,
                         "ms_h2d": ms_h2d, "ms_d2h": ms_d2h, "kernel_launches": launches,
+                        "n_bins_packed": packed, "n_bins_fallback": fallback,
                         "kernels_ms": {KERNEL_NAMES[i]: round(float(kms[i]), 3) for i in range(8)}},
             "one_job_per_launch": {"jobs_per_s": len(texts) / t_plain, "kmers_per_s": nk / t_plain,
                                    "seconds": t_plain,
@@ -503,7 +508,8 @@ def main():
         res = dk.RESIDENT_DEVICE if args.residency == "device" else dk.RESIDENT_HOST
         if args.mode == "batch":
             with dk.Engine(local) as eng:
-                out = run_batched(eng, texts, variant, res, args.call_jobs, args.reps)
+                out = run_batched(eng, texts, variant, res, args.call_jobs, args.reps,
+                                  args.bin_target)
             out.update(mode="batch", workload="batch_jobs (first %d of 4,096 sets)" % len(texts),
                        reads_in="pageable" if pinned is None else "pinned (dk_host_alloc)")
             print(json.dumps(out), flush=True)

@@ -344,7 +344,7 @@ class Engine:
             del keep
 
     def count_batch_nocopy(self, texts, line_width: int, k: int, variant: int = VARIANT_AUTO,
-                           residency: int = RESIDENT_HOST):
+                           residency: int = RESIDENT_HOST, bin_target: int = 0):
         """dk_count_batch without copying the tables out; returns (n_kmers, n_distinct)."""
         keep = [_buf_ptr(t) for t in texts]
         jobs = (Job * max(1, len(texts)))()
@@ -352,7 +352,7 @@ class Engine:
             jobs[j].text = ptr
             jobs[j].nbytes = n
         outs = (Table * max(1, len(texts)))()
-        d = self.desc(line_width, k, variant, residency)
+        d = self.desc(line_width, k, variant, residency, 0, bin_target)
         self._check(self.lib.dk_count_batch(self.h, jobs, len(texts), ctypes.byref(d), outs),
                     "dk_count_batch")
         nk = sum(int(outs[j].n_kmers) for j in range(len(texts)))

@@ -386,6 +386,13 @@ int Engine::count_batch(const dk_job* jobs, int njobs, const dk_input_desc* desc
   // jobs' tables are runs of it), nothing is copied back
   const bool on_dev = desc->residency == DK_RESIDENT_DEVICE;
   const int W = desc->line_width, k = desc->k;
+  // batched read sets are mostly small and of low coverage (most k-mers
+  // distinct), so their bins default to kBatchBinTarget keys: bins of the
+  // plain default would hold more distinct k-mers than the packed bin table
+  // (256 C4-shaped sets: bin count 39.7 ms at 6,000 keys, 30.3 at 4,500, 28.0
+  // at 3,000)
+  dk_input_desc bdesc = *desc;
+  if (bdesc.bin_target <= 0) bdesc.bin_target = kBatchBinTarget;
   const uint64_t stride = (uint64_t)W + 1;
   const uint64_t per_line = W >= k ? (uint64_t)(W - k + 1) : 0;
   std::vector<uint64_t> lines(njobs);
@@ -406,8 +413,7 @@ int Engine::count_batch(const dk_job* jobs, int njobs, const dk_input_desc* desc
   const uint64_t mem_cap = budget ? (uint64_t)(0.7 * (double)budget) : ~0ull;
   const uint64_t wave_cap = std::min(mem_cap, std::max<uint64_t>(total / 4, 256ull << 20));
   const int max_wave_jobs = l1_max_buckets(W, true);  // every job needs one bucket at least
-  const double target = (double)((desc->bin_target > 0) ? std::min(desc->bin_target, kBinCap / 2)
-                                                        : kBinCap / 2);
+  const double target = (double)std::min(bdesc.bin_target, kBinCap / 2);
   struct Wave {
     int j0 = 0, j1 = 0;
     JobSet js;
@@ -528,7 +534,7 @@ int Engine::count_batch(const dk_job* jobs, int njobs, const dk_input_desc* desc
       out_k = (uint64_t*)dev_tb[b]->k;
       out_c = (uint32_t*)dev_tb[b]->c;
       DeviceTable dt;
-      int r = count_device((const uint8_t*)tbuf[b]->p, wv.bytes, *desc, &dt, &js);
+      int r = count_device((const uint8_t*)tbuf[b]->p, wv.bytes, bdesc, &dt, &js);
       if (r != DK_OK) {
         release_table(dev_tb[b]->id);
         dev_tb[b] = nullptr;

@@ -64,8 +64,12 @@ static_assert(sizeof(LevelCounters) == 64, "LevelCounters is read back as 64 byt
 constexpr int kDigitBits = 8;           // typical partition fan-out (level-1 sizing)
 constexpr int kFanout = 1 << kDigitBits;
 constexpr int kMaxSplitBits = 12;       // widest per-node split (4096 children)
-constexpr int kTileKeys = 8192;         // keys per partition tile
+#ifndef DK_TILE_KEYS
+#define DK_TILE_KEYS 8192
+#endif
+constexpr int kTileKeys = DK_TILE_KEYS;  // keys per partition tile
 constexpr int kBinCap = 12000;          // keys a bin-count CTA sorts in shared memory
+constexpr int kBatchBinTarget = 3000;   // default bin size of dk_count_batch (and serving)
 constexpr int kDenseBits = 12;          // nodes with <= this many free bits are counted densely
 constexpr int kBinThreads = 512;
 constexpr int kBinBlocksPerSM = 2;      // resident bin-count CTAs per SM

@@ -1025,7 +1025,10 @@ constexpr int kTileThreads = 512;
 constexpr int kTileKeysPerThread = kTileKeys / kTileThreads;
 static_assert(kTileKeys <= 65536 && kTileKeysPerThread % 2 == 0, "ranks are packed as 16-bit pairs");
 
-__global__ void __launch_bounds__(kTileThreads, 2) k_tile_scatter(const Node* nodes,
+#ifndef DK_TILE_CTAS
+#define DK_TILE_CTAS 2
+#endif
+__global__ void __launch_bounds__(kTileThreads, DK_TILE_CTAS) k_tile_scatter(const Node* nodes,
                                                                   const Tile* tiles, uint64_t* A,
                                                                   uint64_t* B,
                                                                   const uint32_t* TH,
@@ -1688,56 +1691,71 @@ __device__ bool bin_hashed(Node* nodes, uint32_t ni, const Node& nd, uint64_t* k
 // ---- packed hash bins: one 64-bit word per distinct key
 // A bin's keys share their bits [s, 2k) (s = nd.shift free bits), so a key is
 // its low s bits.  Entry = (free bits << (64 - s)) | count: the free bits sit
-// at the top, the count (< 2^14 for a bin of at most kBinCap keys) at the
-// bottom.  Entries compare as the keys they hold, 0 is an empty slot, a new
-// key enters with one 64-bit CAS and a repeat adds to the low 32-bit word.
+// at the top, the count at the bottom.  Entries compare as the keys they
+// hold, 0 is an empty slot, a new key enters with one 64-bit CAS and a repeat
+// adds to the low 32-bit word.  With s <= 50 the count field (>= 14 bits)
+// holds any count of a bin of at most kBinCap keys; with more free bits (bins
+// of small read sets, which few levels split) the field is narrower, every
+// add checks it, and a bin whose count would not fit is left to k_bin_count.
 // Normal bins are counted this way by their own kernel (k_bin_packed), whose
 // small shared-memory footprint (53 KB) and 30 registers fit four 512-thread
 // CTAs per SM: a bin's work is a chain of dependent shared-memory steps, so
-// more bins in flight is what pays (2.4 G keys of large_100m: 20.1 ms with 4
-// CTAs and 4 keys per thread per batch, 20.2 ms with 3 CTAs and 8 keys, 21.5
-// ms with 2 keys; the general kernel at 2 CTAs: 22.8 ms).  Bins it cannot
+// bins in flight are what pays (2.4 G keys of large_100m: 20.1 ms with 4
+// CTAs, 21.9 ms with 3 CTAs of a 5,120-slot table, 21.5 ms with 2 keys per
+// thread per batch; the general kernel at 2 CTAs: 22.8 ms).  Bins it cannot
 // take go to a list that k_bin_count handles after it.
-constexpr int kPackSlotBits = 12;
-constexpr uint32_t kPackSlots = 1u << kPackSlotBits;  // 32 KB of table
-constexpr uint32_t kPackMaxDistinct = 2048;            // sorted entries (16 KB)
-constexpr int kPackDigitBits = 10;                     // counting-sort digits (4 KB)
+#ifndef DK_PACK_SLOTS
+#define DK_PACK_SLOTS 4096
+#define DK_PACK_MAXD 2048
+#define DK_PACK_CTAS 4
+#endif
+constexpr uint32_t kPackSlots = DK_PACK_SLOTS;        // table slots (32 KB)
+constexpr uint32_t kPackMaxDistinct = DK_PACK_MAXD;   // sorted entries (16 KB): load <= 0.5
+constexpr int kPackDigitBits = 10;                    // counting-sort digits (4 KB)
 constexpr uint32_t kPackMaxProbe = 64;
-constexpr int kPackMaxShift = 50;  // the count field keeps >= 14 bits
+constexpr int kPackWideShift = 50;  // up to here the count field holds >= 14 bits
+constexpr int kPackMaxShift = 62;   // beyond: at most 1 count bit, not worth a try
 constexpr int kPackThreads = 512;
-constexpr int kPackBlocksPerSM = 4;
+constexpr int kPackBlocksPerSM = DK_PACK_CTAS;
 #ifndef DK_PACK_BATCH
 #define DK_PACK_BATCH 4
 #endif
 constexpr int kPackBatch = DK_PACK_BATCH;  // keys a thread loads before inserting them
 constexpr size_t kPackSmem = kPackSlots * 8 + kPackMaxDistinct * 8 + (4u << kPackDigitBits);
-static_assert(kBinCap < (1 << (64 - kPackMaxShift)), "a bin's largest count fits the count field");
+static_assert(kBinCap < (1 << (64 - kPackWideShift)), "a bin's largest count fits a wide field");
 static_assert(kPackMaxDistinct * 12 <= kPackSlots * 8, "the output stage fits the table");
 static_assert(kPackSlots % (2 * kPackThreads) == 0, "slot loops");
 
-// Insert one key (rk = key << (64 - s)) with multiplicity mult; false when the
-// probe runs past kPackMaxProbe slots.
-__device__ __forceinline__ bool pack_insert(unsigned long long* tab, unsigned long long rk,
-                                            unsigned long long himask, uint32_t mult,
-                                            uint32_t* hist, int dsh) {
-  const uint32_t h = (uint32_t)(rk >> 32) ^ (uint32_t)rk;
-  uint32_t slot = (h * 0x9E3779B1u) >> (32 - kPackSlotBits);
+// Insert one key (rk = key << (64 - s)) with multiplicity mult: 2 when it is
+// new, 1 when it was there, 0 when the probe runs past kPackMaxProbe slots or
+// (cmax != 0: a narrow count field of at most cmax) its count would not fit.
+__device__ __forceinline__ int pack_insert(unsigned long long* tab, unsigned long long rk,
+                                           unsigned long long himask, uint32_t mult,
+                                           uint32_t* hist, int dsh, uint32_t cmax) {
+  if (cmax && mult > cmax) return 0;
+  const uint32_t h = ((uint32_t)(rk >> 32) ^ (uint32_t)rk) * 0x9E3779B1u;
+  uint32_t slot = __umulhi(h, kPackSlots);  // h scaled to [0, kPackSlots)
   for (uint32_t probe = 0; probe < kPackMaxProbe; ++probe) {
     unsigned long long e = *reinterpret_cast<volatile unsigned long long*>(&tab[slot]);
     if (e == 0ull) {
       e = atomicCAS(&tab[slot], 0ull, rk | mult);
       if (e == 0ull) {
         atomicAdd(&hist[(uint32_t)(rk >> dsh)], 1u);
-        return true;
+        return 2;
       }
     }
     if ((e & himask) == rk) {
-      atomicAdd(reinterpret_cast<unsigned int*>(&tab[slot]), mult);  // the low word
-      return true;
+      unsigned int* lo = reinterpret_cast<unsigned int*>(&tab[slot]);  // the low word
+      if (!cmax) {
+        atomicAdd(lo, mult);
+        return 1;
+      }
+      // a carry out of a narrow field corrupts the entry: the bin is dropped
+      return (atomicAdd(lo, mult) & cmax) + mult <= cmax ? 1 : 0;
     }
-    slot = (slot + 1) & (kPackSlots - 1);
+    slot = slot + 1 == kPackSlots ? 0 : slot + 1;
   }
-  return false;
+  return 0;
 }
 
 // One bin with at most kBinCap keys and kDenseBits < s <= kPackMaxShift free
@@ -1745,7 +1763,8 @@ __device__ __forceinline__ bool pack_insert(unsigned long long* tab, unsigned lo
 // their top D bits (counting sort), rank each inside its digit range, stage
 // the sorted (key, count) pairs in the freed table and write them to the
 // bin's region with coalesced stores.  Returns false, having written nothing,
-// when a probe runs too long or the bin holds more than kPackMaxDistinct keys.
+// when a probe runs too long, a count outgrows a narrow field or the bin
+// holds more than kPackMaxDistinct keys.
 __device__ bool bin_packed(Node* nodes, uint32_t ni, const Node& nd, uint64_t* keys, uint32_t* cnt,
                            unsigned long long* region, uint32_t* tmp, uint32_t* mark,
                            uint32_t* flags) {
@@ -1758,6 +1777,7 @@ __device__ bool bin_packed(Node* nodes, uint32_t ni, const Node& nd, uint64_t* k
   const int cbits = 64 - s;
   const unsigned long long himask = ~((1ull << cbits) - 1ull);
   const uint32_t cmask = cbits >= 32 ? 0xFFFFFFFFu : ((1u << cbits) - 1u);
+  const uint32_t cmax = s > kPackWideShift ? cmask : 0u;  // a narrow count field
   int D = ceil_log2_u64(n) - 3;
   D = max(4, min(D, kPackDigitBits));
   D = min(D, s);
@@ -1773,7 +1793,10 @@ __device__ bool bin_packed(Node* nodes, uint32_t ni, const Node& nd, uint64_t* k
   }
   for (uint32_t j = threadIdx.x; j < R; j += T) hist[j] = 0;
   for (uint32_t w = threadIdx.x; w < (R + 31) / 32; w += T) mark[w] = 0;
-  if (threadIdx.x == 0) flags[1] = 0;
+  if (threadIdx.x == 0) {
+    flags[0] = 0;  // distinct keys so far (updated once per warp and batch)
+    flags[1] = 0;  // the bin has failed
+  }
   __syncthreads();
   DK_PHASE(11);
   constexpr int kBatch = kPackBatch;
@@ -1782,6 +1805,10 @@ __device__ bool bin_packed(Node* nodes, uint32_t ni, const Node& nd, uint64_t* k
   // k-mer: its copies then insert once per warp with their multiplicity
   bool hot = false;
   for (uint32_t i0 = 0; i0 < n; i0 += kBatch * T) {
+    // a bin that has failed (too many distinct keys, a long probe, a full
+    // count field) stops inserting: its keys are counted again elsewhere
+    if (*reinterpret_cast<volatile uint32_t*>(&flags[1])) ok = false;
+    uint32_t fresh = 0;  // new keys this batch
     unsigned long long kk[kBatch];
 #pragma unroll
     for (int u = 0; u < kBatch; ++u) {
@@ -1805,8 +1832,15 @@ __device__ bool bin_packed(Node* nodes, uint32_t ni, const Node& nd, uint64_t* k
         live = valid && (int)lane_id() == __ffs(peers) - 1;
         mult = (uint32_t)__popc(peers);
       }
-      if (live && ok) ok = pack_insert(tab, rk, himask, mult, hist, dsh);
+      if (live && ok) {
+        const int r = pack_insert(tab, rk, himask, mult, hist, dsh, cmax);
+        ok = r != 0;
+        fresh += r == 2;
+      }
     }
+    const uint32_t wf = __reduce_add_sync(0xFFFFFFFFu, fresh);
+    if (lane_id() == 0 && wf && atomicAdd(&flags[0], wf) + wf > kPackMaxDistinct) flags[1] = 1;
+    if (!ok) flags[1] = 1;
   }
   if (!ok) flags[1] = 1;
   __syncthreads();

@@ -402,3 +402,25 @@ def test_chunked_upload_with_lines_shorter_than_k(engine):
         pin.free()
     small = _reads_68mb(85)[: 5_000 * 151]
     check(engine, small, 150, 31)
+
+
+@pytest.mark.parametrize("variant", VARIANTS)
+def test_repeats_in_bins_with_many_free_bits(engine, variant):
+    """A small read set is split by few bits, so its bins keep most of the
+    key's bits free and the packed table's count field is narrow: a k-mer
+    repeated past that field's limit sends its bin to the general bin kernel,
+    and the table stays exact."""
+    rng = np.random.Generator(np.random.PCG64(83))
+    acgt = np.frombuffer(b"ACGT", np.uint8)
+    W = 40
+    lines = np.empty((3000, W + 1), np.uint8)
+    lines[:, :W] = rng.choice(acgt, (3000, W))
+    lines[:1000, :W] = lines[0, :W]          # one read, 1,000 times: its 10 k-mers repeat
+    lines[:, W] = ord("\n")
+    rng.shuffle(lines)
+    text = lines.reshape(-1)
+    got = check(engine, text, W, 31, variant)
+    assert int(got.counts.max()) >= 1000
+    if variant == dk.VARIANT_HASH:
+        st = engine.stats()
+        assert st["n_bins_packed"] + st["n_bins_fallback"] >= 1
