@@ -623,7 +623,9 @@ def main():
             tj = json.load(f)
         ent = tj.get(KERNEL_NAMES[top])
         if ent and ent.get("bytes_per_kmer"):
-            traffic = ent["bytes_per_kmer"] * nk
+            # ncu's DRAM bytes per k-mer of the small case, scaled to this
+            # step's k-mers, per launch like alg_bytes_per_launch
+            traffic = ent["bytes_per_kmer"] * nk / max(kl[top], 1)
     b_alg = nbytes + 16 * nk + 12 * nd
     pipe = b_alg / (ms_per_step / 1000.0) / 1e9
 
@@ -690,7 +692,10 @@ def main():
             "gpu_launches": launches,
             "roofline": {"bound": "hbm", "kernel": KERNEL_NAMES[top], "achieved": achieved,
                          "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
-                         "traffic": traffic, "peak_kind": peak_kind,
+                         "traffic": traffic,
+                         "traffic_over_alg": (traffic / (ab[top] / max(kl[top], 1))
+                                              if traffic else None),
+                         "peak_kind": peak_kind,
                          "alg_bytes_per_launch": ab[top] / max(kl[top], 1),
                          "ms_per_launch": kms[top] / max(kl[top], 1)},
             "pipeline_roofline": {"b_alg": b_alg, "achieved": pipe, "peak": hbm_peak,

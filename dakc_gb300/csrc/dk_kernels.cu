@@ -1736,6 +1736,15 @@ __device__ __forceinline__ int pack_insert(unsigned long long* tab, unsigned lon
   const uint32_t h = ((uint32_t)(rk >> 32) ^ (uint32_t)rk) * 0x9E3779B1u;
   uint32_t slot = __umulhi(h, kPackSlots);  // h scaled to [0, kPackSlots)
   for (uint32_t probe = 0; probe < kPackMaxProbe; ++probe) {
+#ifdef DK_PHASE_TIMING
+    {  // probe steps: lanes (g_phase[0]) and warp iterations (g_phase[3])
+      const unsigned am = __activemask();
+      if (lane_id() == __ffs(am) - 1) {
+        atomicAdd(&g_phase[0], (unsigned long long)__popc(am));
+        atomicAdd(&g_phase[3], 1ull);
+      }
+    }
+#endif
     unsigned long long e = *reinterpret_cast<volatile unsigned long long*>(&tab[slot]);
     if (e == 0ull) {
       e = atomicCAS(&tab[slot], 0ull, rk | mult);
@@ -1825,6 +1834,7 @@ __device__ bool bin_packed(Node* nodes, uint32_t ni, const Node& nd, uint64_t* k
       if (i0 == 0 && u == 0) {
         const uint32_t peers = __match_any_sync(0xFFFFFFFFu, rk) & __ballot_sync(0xFFFFFFFFu, valid);
         hot = __reduce_max_sync(0xFFFFFFFFu, valid ? (uint32_t)__popc(peers) : 0u) >= 4;
+        DK_WARP_ADD(1, hot ? 1 : 0);  // warps that aggregate (instrumented builds)
       }
       if (hot) {  // copies of one key in this warp insert once with their multiplicity
         const uint32_t vm = __ballot_sync(0xFFFFFFFFu, valid);
@@ -1875,6 +1885,7 @@ __device__ bool bin_packed(Node* nodes, uint32_t ni, const Node& nd, uint64_t* k
     }
     uint32_t r = lo;
     for (uint32_t y = lo; y < hi; ++y) r += sorted[y] < v;
+    DK_WARP_ADD(2, hi - lo);  // rank comparisons, lane 0's (instrumented builds)
     ok_[r] = prefix | (v >> cbits);
     oc[r] = (uint32_t)v & cmask;
   }
