@@ -649,6 +649,23 @@ def main():
             # per call: device time, upload, and the download left after the device
             parts.append([round(st["ms_device"], 2), round(st["ms_h2d"], 2),
                           round(st["ms_d2h"], 2)])
+        # the same call with the reads in pageable memory, as the reference's
+        # caller holds them (a malloc'd chunk); read in place where the device
+        # can, else staged through page-locked slots
+        pwalls = []
+        for i in range(3 + max(1, args.e2e_steps // 2)):
+            t0 = time.perf_counter()
+            t = eng.count_raw(rs.text.ctypes.data, nbytes, hdesc)
+            if i >= 3:
+                pwalls.append(time.perf_counter() - t0)
+            eng.free_table(t)
+        pst = eng.stats()
+        pageable = {"value": nk / float(np.mean(pwalls)), "unit": UNIT,
+                    "ms_per_step": float(np.mean(pwalls)) * 1000.0,
+                    "ms_median": float(np.median(pwalls)) * 1000.0,
+                    "walls_ms": [round(x * 1000.0, 2) for x in pwalls],
+                    "read_in_place": bool(pst["upload_in_place"]),
+                    "upload_chunks": int(pst["upload_chunks"])}
         w = float(np.mean(walls))
         e2e = {"value": nk / w, "unit": UNIT, "h2d_bytes_per_step": nbytes,
                "d2h_bytes_per_step": n_out * 12, "ms_per_step": w * 1000.0,
@@ -656,7 +673,7 @@ def main():
                "value_median": nk / float(np.median(walls)),
                "ms_h2d": st["ms_h2d"], "ms_d2h": st["ms_d2h"],
                "walls_ms": [round(x * 1000.0, 2) for x in walls],
-               "device_h2d_d2h_ms": parts}
+               "device_h2d_d2h_ms": parts, "pageable_reads": pageable}
         pin.free()
 
     forms = None

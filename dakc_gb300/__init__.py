@@ -39,6 +39,7 @@ DK_ERR_NO_DEVICE = -10
 VARIANT_AUTO, VARIANT_SORT, VARIANT_HASH = 0, 1, 2
 CONV_DAKC, CONV_PAKMAN = 0, 1
 FLAG_STREAM_ALL = 1  # dk_config.flags: copy every host table out group by group
+FLAG_STAGE_PAGEABLE = 2  # dk_config.flags: stage pageable reads through page-locked slots
 
 FORMAT_LINES, FORMAT_FASTQ, FORMAT_FASTA = 0, 1, 2
 RESIDENT_HOST, RESIDENT_DEVICE = 0, 1
@@ -103,7 +104,8 @@ class Stats(ctypes.Structure):
                 ("n_bins_resorted", ctypes.c_uint64), ("n_bins_big", ctypes.c_uint64),
                 ("n_bins_retried", ctypes.c_uint64), ("n_groups", ctypes.c_uint64),
                 ("table_streamed", ctypes.c_uint64), ("upload_chunks", ctypes.c_uint64),
-                ("n_bins_packed", ctypes.c_uint64), ("n_bins_fallback", ctypes.c_uint64)]
+                ("n_bins_packed", ctypes.c_uint64), ("n_bins_fallback", ctypes.c_uint64),
+                ("upload_in_place", ctypes.c_uint64)]
 
     KERNEL_NAMES = ["extract_count", "extract_scatter", "partition_hist", "partition_scatter",
                     "bin_count", "compact", "hash_insert", "other"]

@@ -14,6 +14,9 @@
 #include "../../include/dakc_gb300.h"
 
 #include <cuda_runtime.h>
+#include <sys/mman.h>
+#include <unistd.h>
+
 #include <algorithm>
 #include <atomic>
 #include <chrono>
@@ -138,6 +141,9 @@ int Engine::init(const dk_config* cfg) {
   cudaDeviceProp p;
   DK_CUDA(cudaGetDeviceProperties(&p, device));
   sm_count = p.multiProcessorCount;
+  int pma = 0;
+  DK_CUDA(cudaDeviceGetAttribute(&pma, cudaDevAttrPageableMemoryAccess, device));
+  host_direct = pma != 0 && !(flags & DK_FLAG_STAGE_PAGEABLE);
   if (p.major * 10 + p.minor < 100) {
     set_error("engine is built for sm_103a; device is older");
     return DK_ERR_NO_DEVICE;
@@ -637,6 +643,24 @@ int Engine::count_batch(const dk_job* jobs, int njobs, const dk_input_desc* desc
 // Copy host reads into device memory: one async copy when the buffer is
 // pinned, else through two pinned staging slots so host memcpy overlaps the
 // previous slot's DMA.
+// Every page of [p, p + n) is mapped in this process (mincore fails with
+// ENOMEM on an unmapped page).  The device reads pageable reads in place, so
+// a range the caller no longer owns (freed, unmapped) is refused here rather
+// than read by a kernel.
+static bool host_range_mapped(const void* p, uint64_t n) {
+  if (!n) return true;
+  const uint64_t pg = (uint64_t)sysconf(_SC_PAGESIZE);
+  const uintptr_t a = reinterpret_cast<uintptr_t>(p) & ~(uintptr_t)(pg - 1);
+  const uint64_t len = reinterpret_cast<uintptr_t>(p) + n - a;
+  constexpr uint64_t kWin = 16384;  // pages per call
+  unsigned char vec[kWin];
+  for (uint64_t off = 0; off < len; off += pg * kWin) {
+    const uint64_t l = std::min<uint64_t>(len - off, pg * kWin);
+    if (mincore(reinterpret_cast<void*>(a + off), l, vec) != 0) return false;
+  }
+  return true;
+}
+
 static bool is_pinned(const void* h) {
   cudaPointerAttributes at;
   bool pinned = false;
@@ -682,6 +706,14 @@ int Engine::upload_segments(const std::vector<Seg>& all, uint8_t* d, cudaStream_
   for (const S& x : v) {
     if (x.pinned) {
       DK_CUDA(cudaMemcpyAsync(d + x.sg.doff, x.sg.h, x.sg.n, cudaMemcpyHostToDevice, st));
+    } else if (host_direct) {
+      // the SMs read the pageable bytes in place
+      if (!host_range_mapped(x.sg.h, x.sg.n)) {
+        set_error("reads at an unmapped host address");
+        return DK_ERR_INVALID_ARG;
+      }
+      launch_copy_in(x.sg.h, d + x.sg.doff, x.sg.n, sm_count, st);
+      DK_CUDA(cudaGetLastError());
     } else {
       any_pageable = true;
     }
@@ -1289,14 +1321,20 @@ int Engine::count_locked(const char* text, uint64_t nbytes, bool text_on_device,
   DK_CUDA(cudaSetDevice(device));
   const uint8_t* d_text = (const uint8_t*)text;
   float ms_h2d = 0;
+  bool in_place_up = false;  // pageable reads read in place by the device
   if (!text_on_device) {
     DK_TRY(Arena::ensure(this, this->text, nbytes + 64));
     DK_CUDA(cudaEventRecord(ev_h2d0, stream));
     const int W = desc->line_width;
     const int64_t Lc = frame_lines(nbytes, W);
-    if (nbytes >= kChunkMinBytes && W <= kLineMaxW && Lc >= 64 * kMaxChunks && is_pinned(text)) {
+    const bool pinned = is_pinned(text);
+    in_place_up = !pinned && host_direct && nbytes > 0;
+    if (nbytes >= kChunkMinBytes && W <= kLineMaxW && Lc >= 64 * kMaxChunks &&
+        (pinned || host_direct)) {
       // chunks of lines on s_in (after earlier work on the text buffer); the
-      // level-1 count of each runs as soon as it has landed
+      // level-1 count of each runs as soon as it has landed.  Page-locked
+      // chunks go to the DMA engine, pageable ones are read in place by a
+      // copy kernel (same link, same rate)
       DK_CUDA(cudaStreamWaitEvent(s_in, ev_h2d0, 0));
       chunks.n = kMaxChunks;
       const uint64_t stride = (uint64_t)W + 1;
@@ -1305,9 +1343,21 @@ int Engine::count_locked(const char* text, uint64_t nbytes, bool text_on_device,
         if (!chunks.ev[c]) DK_CUDA(cudaEventCreate(&chunks.ev[c]));
         const uint64_t b0 = chunks.lines[c] * stride;
         const uint64_t b1 = c + 1 == kMaxChunks ? nbytes : chunks.lines[c + 1] * stride;
-        if (b1 > b0)
+        if (b1 > b0 && pinned)
           DK_CUDA(cudaMemcpyAsync((uint8_t*)this->text.p + b0, text + b0, b1 - b0,
                                   cudaMemcpyHostToDevice, s_in));
+        if (b1 > b0 && !pinned) {
+          // the chunks launched so far read mapped memory: they finish
+          // before the call returns
+          if (!host_range_mapped(text + b0, b1 - b0)) {
+            cudaStreamSynchronize(s_in);
+            chunks.n = 0;
+            set_error("reads at an unmapped host address");
+            return DK_ERR_INVALID_ARG;
+          }
+          launch_copy_in(text + b0, (uint8_t*)this->text.p + b0, b1 - b0, sm_count, s_in);
+          DK_CUDA(cudaGetLastError());
+        }
         DK_CUDA(cudaEventRecord(chunks.ev[c], s_in));
       }
     } else if (nbytes) {
@@ -1381,6 +1431,7 @@ int Engine::count_locked(const char* text, uint64_t nbytes, bool text_on_device,
   if (chunked_up) cudaStreamSynchronize(s_in);
   chunks.n = 0;
   stats.upload_chunks = chunked_up ? (uint64_t)kMaxChunks : 0;
+  stats.upload_in_place = in_place_up ? 1 : 0;
   if (h_tb && (rc != DK_OK || !streaming || streamed != dt.n)) {
     // copies into it may still run
     cudaStreamSynchronize(s_out);

@@ -105,6 +105,9 @@ struct Engine {
   int sm_count = 0;
   uint64_t budget = 0;
   uint64_t flags = 0;  // dk_config.flags
+  // the device reads pageable host memory in place (coherent access through the
+  // host's page tables): pageable reads are then copied in by kernels
+  bool host_direct = false;
   uint64_t dev_bytes = 0, dev_peak = 0;
   cudaStream_t stream = nullptr;            // kernels
   cudaStream_t s_in = nullptr, s_out = nullptr;  // batch uploads / table downloads

@@ -133,6 +133,9 @@ int launch_l1_scan(const uint32_t* H, int grid, int F1, uint64_t* O, Node* nodes
                    const int16_t* bucket_shift, cudaStream_t s);
 // copy `bytes` between device memory and page-locked host memory with a kernel
 int launch_copy_small(const void* src, void* dst, uint64_t bytes, cudaStream_t s);
+// copy `bytes` of host memory the device reads in place (pageable memory with
+// coherent host access, or page-locked memory) into device memory, any alignment
+int launch_copy_in(const void* src, void* dst, uint64_t bytes, int sm_count, cudaStream_t s);
 
 // largest level-1 fan-out (power of two <= 2^kMaxL1Bits) whose scatter kernel
 // fits the per-block shared-memory limit for line width W

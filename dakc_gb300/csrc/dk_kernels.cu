@@ -2173,6 +2173,64 @@ __global__ void k_copy_small(const uint8_t* __restrict__ src, uint8_t* __restric
   }
 }
 
+// Host reads into device memory by the SMs, for host memory the GPU reads in
+// place: pageable memory where the device uses the host's page tables
+// (coherent chip-to-chip access), or page-locked memory.  Any alignment of
+// either side.  Each lane writes one 16-byte word of the destination; its
+// bytes come from the two 16-byte-aligned source words that straddle them,
+// the second being the next lane's first (the last lane loads it), so each
+// source word crosses the link once.  A source word is read only if it holds
+// a byte of the source range: an aligned 16-byte word never crosses a page,
+// so no read leaves the pages the range occupies.  The words at either end
+// of the destination range are written byte by byte.
+__global__ void k_copy_in(const uint8_t* __restrict__ src, uint8_t* __restrict__ dst,
+                          uint64_t bytes) {
+  const uintptr_t d_lo = reinterpret_cast<uintptr_t>(dst), d_hi = d_lo + bytes;
+  const uintptr_t d0 = d_lo & ~(uintptr_t)15;
+  const uint64_t nw = (d_hi - d0 + 15) >> 4;  // destination words touched
+  const uintptr_t s_lo = reinterpret_cast<uintptr_t>(src), s_hi = s_lo + bytes;
+  const uintptr_t delta = s_lo - d_lo;        // source address = destination + delta (mod 2^64)
+  const uint32_t m = (uint32_t)((d0 + delta) & 15);  // a word's first byte inside its source word
+  const uint32_t q = m >> 2, r = (m & 3) * 8;
+  const uint32_t lane = lane_id();
+  const uint64_t wstep = (uint64_t)gridDim.x * (blockDim.x >> 5) * 32;
+  auto load = [&](uintptr_t a) -> uint4 {
+    if (a < s_hi && a + 16 > s_lo) return *reinterpret_cast<const uint4*>(a);
+    return make_uint4(0u, 0u, 0u, 0u);
+  };
+  for (uint64_t wb = ((uint64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * 32; wb < nw;
+       wb += wstep) {  // uniform over the warp
+    const uint64_t j = wb + lane;
+    const uintptr_t D = d0 + 16 * j;
+    const uintptr_t A = D + delta - m;  // 16-byte aligned
+    const uint4 w = load(A);
+    uint4 o = w;
+    if (m) {
+      uint4 v;
+      v.x = __shfl_down_sync(0xFFFFFFFFu, w.x, 1);
+      v.y = __shfl_down_sync(0xFFFFFFFFu, w.y, 1);
+      v.z = __shfl_down_sync(0xFFFFFFFFu, w.z, 1);
+      v.w = __shfl_down_sync(0xFFFFFFFFu, w.w, 1);
+      if (lane == 31) v = load(A + 16);
+      uint32_t a0 = w.x, a1 = w.y, a2 = w.z, a3 = w.w, a4 = v.x, a5 = v.y, a6 = v.z, a7 = v.w;
+      if (q & 2) { a0 = a2; a1 = a3; a2 = a4; a3 = a5; a4 = a6; a5 = a7; }
+      if (q & 1) { a0 = a1; a1 = a2; a2 = a3; a3 = a4; a4 = a5; }
+      o.x = __funnelshift_r(a0, a1, r);
+      o.y = __funnelshift_r(a1, a2, r);
+      o.z = __funnelshift_r(a2, a3, r);
+      o.w = __funnelshift_r(a3, a4, r);
+    }
+    if (j >= nw) continue;
+    if (D >= d_lo && D + 16 <= d_hi) {
+      *reinterpret_cast<uint4*>(D) = o;
+    } else {
+      const uint8_t* ob = reinterpret_cast<const uint8_t*>(&o);
+      for (uint32_t b = 0; b < 16; ++b)
+        if (D + b >= d_lo && D + b < d_hi) reinterpret_cast<uint8_t*>(D)[b] = ob[b];
+    }
+  }
+}
+
 }  // namespace
 
 int launch_copy_small(const void* src, void* dst, uint64_t bytes, cudaStream_t s) {
@@ -2180,6 +2238,16 @@ int launch_copy_small(const void* src, void* dst, uint64_t bytes, cudaStream_t s
   const uint64_t units = (bytes + 7) / 8;
   const uint32_t blocks = (uint32_t)std::min<uint64_t>(64, (units + 255) / 256);
   k_copy_small<<<blocks, 256, 0, s>>>((const uint8_t*)src, (uint8_t*)dst, bytes);
+  return 1;
+}
+
+int launch_copy_in(const void* src, void* dst, uint64_t bytes, int sm_count, cudaStream_t s) {
+  if (!bytes) return 0;
+  const uint64_t words = bytes / 16 + 2;
+  // one CTA per SM saturates the link (any grid measures the same rate) and
+  // leaves the SMs to kernels that overlap the copy
+  const uint32_t blocks = (uint32_t)std::min<uint64_t>((uint64_t)sm_count, (words + 255) / 256);
+  k_copy_in<<<blocks, 256, 0, s>>>((const uint8_t*)src, (uint8_t*)dst, bytes);
   return 1;
 }
 

@@ -88,6 +88,11 @@ typedef struct {
  * the rest of the count runs, only when the input holds at least 64 Mi k-mers;
  * with this flag every host table is (the same table, other timing) */
 #define DK_FLAG_STREAM_ALL 1ull
+/* Pageable host reads are normally read in place by the device where it
+ * accesses pageable memory through the host's page tables (Grace: coherent
+ * chip-to-chip access), chunk by chunk like page-locked reads; with this flag
+ * they are staged through page-locked slots by host threads instead */
+#define DK_FLAG_STAGE_PAGEABLE 2ull
 
 typedef struct {
   int line_width;  /* READLEN: bytes per line before the terminator (>= 1)      */
@@ -148,6 +153,8 @@ typedef struct {
                                64-bit word per distinct k-mer)                 */
   uint64_t n_bins_fallback; /* of the final bins, those the packed table could not
                                hold (counted by the general bin kernel)        */
+  uint64_t upload_in_place; /* 1: pageable reads were read in place by the device
+                               (no page-locked staging)                        */
 } dk_stats;
 
 /* One read set of a batch (dk_count_batch). */

@@ -66,9 +66,11 @@ def test_batch_many_small_jobs(engine):
         assert got[j].n_kmers == nk and np.array_equal(got[j].kmers, keys)
 
 
-def test_batch_mixes_pinned_and_pageable_reads():
-    """Page-locked jobs go straight to DMA, pageable ones through the staging
-    slots; a staged run must never overwrite a pinned job's bytes."""
+@pytest.mark.parametrize("flags", [0, dk.FLAG_STAGE_PAGEABLE])
+def test_batch_mixes_pinned_and_pageable_reads(flags):
+    """Page-locked jobs go straight to DMA; pageable ones are read in place by
+    the device (flags 0, where it can) or go through the staging slots.  No
+    pageable copy may overwrite a pinned job's bytes."""
     texts = job_texts(24, seed=7, max_reads=4000)
     pin = [dk.PinnedBuffer(t.size) for t in texts[::2]]
     mixed = []
@@ -79,7 +81,7 @@ def test_batch_mixes_pinned_and_pageable_reads():
             mixed.append(b.array)
         else:
             mixed.append(t)
-    with dk.Engine(0, mem_budget=96 << 20) as eng:       # several pipelined waves
+    with dk.Engine(0, mem_budget=96 << 20, flags=flags) as eng:  # several pipelined waves
         got = eng.count_batch(mixed, 250, 31, dk.VARIANT_HASH)
         st = eng.stats()
     assert st["n_waves"] >= 2

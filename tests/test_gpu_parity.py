@@ -291,9 +291,10 @@ def _reads_68mb(seed):
 @pytest.mark.parametrize("nul_line", [None, 200_001])
 def test_chunked_upload_equals_single_upload(engine, nul_line):
     """Page-locked reads of 64 MB or more upload in chunks of lines, each
-    counted as soon as it lands.  The table equals the one counted from the
-    same bytes in pageable memory (uploaded whole), also when a NUL-led line
-    in the middle of a chunk ends the read set there."""
+    counted as soon as it lands; so do pageable reads where the device reads
+    them in place.  Both tables equal the one counted from the same bytes
+    staged through page-locked slots and uploaded whole, also when a NUL-led
+    line in the middle of a chunk ends the read set there."""
     text = _reads_68mb(81)
     if nul_line is not None:
         text[nul_line * 151] = 0
@@ -302,13 +303,19 @@ def test_chunked_upload_equals_single_upload(engine, nul_line):
         pin.array[:] = text
         a = engine.count(pin.array, 150, 31, dk.VARIANT_HASH)
         chunks = engine.stats()["upload_chunks"]
-        b = engine.count(text, 150, 31, dk.VARIANT_HASH)
-        assert engine.stats()["upload_chunks"] == 0
+        p = engine.count(text, 150, 31, dk.VARIANT_HASH)
+        st_p = engine.stats()
     finally:
         pin.free()
+    with dk.Engine(0, flags=dk.FLAG_STAGE_PAGEABLE) as staged:
+        b = staged.count(text, 150, 31, dk.VARIANT_HASH)
+        st_b = staged.stats()
+    assert st_b["upload_chunks"] == 0 and st_b["upload_in_place"] == 0
+    assert st_p["upload_chunks"] == (chunks if st_p["upload_in_place"] else 0)
     assert chunks >= 2
-    assert a.n_kmers == b.n_kmers and np.array_equal(a.kmers, b.kmers)
-    assert np.array_equal(a.counts, b.counts)
+    for r in (a, p):
+        assert r.n_kmers == b.n_kmers and np.array_equal(r.kmers, b.kmers)
+        assert np.array_equal(r.counts, b.counts)
     assert int(a.counts.sum(dtype=np.uint64)) == a.n_kmers
     if nul_line is not None:
         assert a.n_kmers == nul_line * 120
@@ -338,10 +345,11 @@ def test_chunked_upload_other_convention_and_variant(engine, conv, variant):
         pin.array[:] = text
         a = _count_conv(engine, pin.array, 150, 31, conv, variant)
         assert engine.stats()["upload_chunks"] >= 2
-        b = _count_conv(engine, text, 150, 31, conv, variant)
-        assert engine.stats()["upload_chunks"] == 0
     finally:
         pin.free()
+    with dk.Engine(0, flags=dk.FLAG_STAGE_PAGEABLE) as staged:
+        b = _count_conv(staged, text, 150, 31, conv, variant)
+        assert staged.stats()["upload_chunks"] == 0
     assert a[2] == b[2] and np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
     assert int(a[1].sum(dtype=np.uint64)) == a[2]
 
@@ -351,7 +359,8 @@ def test_streamed_and_chunked_together(variant):
     """A page-locked read set uploaded in chunks whose table also streams out
     in groups equals the single-upload, single-copy count of the same bytes."""
     text = _reads_68mb(83)
-    with dk.Engine(0, flags=dk.FLAG_STREAM_ALL) as e1, dk.Engine(0) as e2:
+    with dk.Engine(0, flags=dk.FLAG_STREAM_ALL) as e1, \
+            dk.Engine(0, flags=dk.FLAG_STAGE_PAGEABLE) as e2:
         pin = dk.PinnedBuffer(text.size)
         try:
             pin.array[:] = text
@@ -379,7 +388,7 @@ def test_failed_chunked_count_leaves_the_context_usable():
             with pytest.raises(dk.DkError) as ei:
                 e.count(pin.array, 150, 31, dk.VARIANT_HASH)
             assert ei.value.status in (dk.DK_ERR_ADMISSION, dk.DK_ERR_OOM)
-            small = np.ascontiguousarray(pin.array[: 20_000 * 151])
+            small = pin.array[: 20_000 * 151].copy()  # outlives the page-locked buffer
         finally:
             pin.free()
         check(e, small, 150, 31, dk.VARIANT_HASH)
