@@ -44,7 +44,7 @@ sys.path.insert(0, ROOT)
 METRIC = "k-mers/sec k=31 on 1 GB300, % HBM roofline; p50/p99 job latency batched vs plain"
 UNIT = "k-mers/s"
 KERNEL_NAMES = ["extract_count", "extract_scatter", "partition_hist", "partition_scatter",
-                "bin_count", "compact", "hash_insert", "other"]
+                "bin_count", "compact", "wave_graph", "other"]
 
 
 def peaks():
@@ -272,6 +272,7 @@ def run_batched(eng, texts, variant, residency=None, call_jobs=0, reps=3, bin_ta
         ms_dev = ms_h2d = ms_d2h = 0.0
         launches = 0
         packed = fallback = 0
+        graph_waves = graph_retries = 0
         kms[:] = 0
         for c in calls:
             a, b = eng.count_batch_nocopy(c, 250, 31, variant, residency, bin_target)
@@ -285,6 +286,8 @@ def run_batched(eng, texts, variant, residency=None, call_jobs=0, reps=3, bin_ta
             launches += st["kernel_launches"]
             packed += st["n_bins_packed"]
             fallback += st["n_bins_fallback"]
+            graph_waves += st["graph_waves"]
+            graph_retries += st["graph_retries"]
             kms += np.asarray(st["ms_kernel"])
         t_runs.append(time.perf_counter() - t0)
     t_batch = float(np.median(t_runs))
@@ -315,6 +318,7 @@ def run_batched(eng, texts, variant, residency=None, call_jobs=0, reps=3, bin_ta
                         "calls": len(calls), "waves": waves, "ms_device": ms_dev,
                         "ms_h2d": ms_h2d, "ms_d2h": ms_d2h, "kernel_launches": launches,
                         "n_bins_packed": packed, "n_bins_fallback": fallback,
+                        "graph_waves": graph_waves, "graph_retries": graph_retries,
                         "kernels_ms": {KERNEL_NAMES[i]: round(float(kms[i]), 3) for i in range(8)}},
             "one_job_per_launch": {"jobs_per_s": len(texts) / t_plain, "kmers_per_s": nk / t_plain,
                                    "seconds": t_plain,
@@ -325,7 +329,7 @@ def run_batched(eng, texts, variant, residency=None, call_jobs=0, reps=3, bin_ta
 
 
 def run_served(texts, rate, n_jobs, variant, workers, max_batch, seed=5, residency=None,
-               mem_budget=0):
+               mem_budget=0, flags=0):
     """Open-loop Poisson arrivals at `rate` jobs/s; sizes drawn from the pool.
     The same arrival stream runs once untimed first, so that every worker's
     device arenas and table pools are at their steady-state sizes.  Tables
@@ -356,7 +360,7 @@ def run_served(texts, rate, n_jobs, variant, workers, max_batch, seed=5, residen
             batches.append(info["batch_jobs"])
         return time.perf_counter() - t0, lat, nk, batches
 
-    with dk.Engine(0, mem_budget=mem_budget) as eng:
+    with dk.Engine(0, mem_budget=mem_budget, flags=flags) as eng:
         eng.serve_start(workers=workers, max_batch_jobs=max_batch)
         stream(eng)  # warm-up pass
         span, lat, nk, batches = stream(eng)

@@ -40,6 +40,8 @@ VARIANT_AUTO, VARIANT_SORT, VARIANT_HASH = 0, 1, 2
 CONV_DAKC, CONV_PAKMAN = 0, 1
 FLAG_STREAM_ALL = 1  # dk_config.flags: copy every host table out group by group
 FLAG_STAGE_PAGEABLE = 2  # dk_config.flags: stage pageable reads through page-locked slots
+FLAG_NO_GRAPH = 4  # dk_config.flags: batch waves without the CUDA graph
+FLAG_GRAPH_MIN_BUFFERS = 8  # dk_config.flags: wave graphs at minimal buffers (fallback tests)
 
 FORMAT_LINES, FORMAT_FASTQ, FORMAT_FASTA = 0, 1, 2
 RESIDENT_HOST, RESIDENT_DEVICE = 0, 1
@@ -105,10 +107,11 @@ class Stats(ctypes.Structure):
                 ("n_bins_retried", ctypes.c_uint64), ("n_groups", ctypes.c_uint64),
                 ("table_streamed", ctypes.c_uint64), ("upload_chunks", ctypes.c_uint64),
                 ("n_bins_packed", ctypes.c_uint64), ("n_bins_fallback", ctypes.c_uint64),
-                ("upload_in_place", ctypes.c_uint64)]
+                ("upload_in_place", ctypes.c_uint64), ("graph_waves", ctypes.c_uint64),
+                ("graph_builds", ctypes.c_uint64), ("graph_retries", ctypes.c_uint64)]
 
     KERNEL_NAMES = ["extract_count", "extract_scatter", "partition_hist", "partition_scatter",
-                    "bin_count", "compact", "hash_insert", "other"]
+                    "bin_count", "compact", "wave_graph", "other"]
 
     def as_dict(self) -> dict:
         arrays = ("ms_stage", "ms_kernel", "launches_kernel")
@@ -390,8 +393,8 @@ class Engine:
             kmers, counts = np.zeros(0, np.uint64), np.zeros(0, np.uint32)
         return CountResult(kmers, counts, int(t.n_kmers), int(t.variant_used))
 
-    def count_batch(self, texts, line_width: int, k: int, variant: int = VARIANT_AUTO
-                    ) -> list[CountResult]:
+    def count_batch(self, texts, line_width: int, k: int, variant: int = VARIANT_AUTO,
+                    l1_bits: int = 0, bin_target: int = 0) -> list[CountResult]:
         """Count each read set of `texts` (one pipeline, memory-bounded waves)."""
         keep = [_buf_ptr(t) for t in texts]
         jobs = (Job * max(1, len(texts)))()
@@ -399,7 +402,7 @@ class Engine:
             jobs[j].text = ptr
             jobs[j].nbytes = n
         outs = (Table * max(1, len(texts)))()
-        d = self.desc(line_width, k, variant)
+        d = self.desc(line_width, k, variant, RESIDENT_HOST, l1_bits, bin_target)
         self._check(self.lib.dk_count_batch(self.h, jobs, len(texts), ctypes.byref(d), outs),
                     "dk_count_batch")
         res = []

@@ -154,6 +154,8 @@ int Engine::init(const dk_config* cfg) {
   DK_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
   DK_CUDA(cudaStreamCreateWithFlags(&s_in, cudaStreamNonBlocking));
   DK_CUDA(cudaStreamCreateWithFlags(&s_out, cudaStreamNonBlocking));
+  DK_CUDA(cudaStreamCreateWithFlags(&s_cap, cudaStreamNonBlocking));
+  DK_CUDA(cudaMallocHost(&h_wc, sizeof(WaveCtl)));
   for (auto* evs : {ev_in0, ev_in1, ev_out0, ev_out1})
     for (int i = 0; i < 2; ++i) DK_CUDA(cudaEventCreate(&evs[i]));
   for (auto& ev : ev_stage) DK_CUDA(cudaEventCreate(&ev));
@@ -192,7 +194,10 @@ Engine::~Engine() {
   for (auto* evs : {ev_in0, ev_in1, ev_out0, ev_out1})
     for (int i = 0; i < 2; ++i)
       if (evs[i]) cudaEventDestroy(evs[i]);
-  for (cudaStream_t st : {stream, s_in, s_out})
+  if (wave_exec) cudaGraphExecDestroy(wave_exec);
+  if (wave_graph) cudaGraphDestroy(wave_graph);
+  if (h_wc) cudaFreeHost(h_wc);
+  for (cudaStream_t st : {stream, s_in, s_out, s_cap})
     if (st) cudaStreamDestroy(st);
 }
 
@@ -564,6 +569,9 @@ int Engine::count_batch(const dk_job* jobs, int njobs, const dk_input_desc* desc
       stats_batch.n_bins_resorted += stats.n_bins_resorted;
       stats_batch.n_bins_packed += stats.n_bins_packed;
       stats_batch.n_bins_fallback += stats.n_bins_fallback;
+      stats_batch.graph_waves += stats.graph_waves;
+      stats_batch.graph_builds += stats.graph_builds;
+      stats_batch.graph_retries += stats.graph_retries;
       stats_batch.partition_levels = std::max(stats_batch.partition_levels, stats.partition_levels);
       stats_batch.variant_used = stats.variant_used;
       TableBuf* h_tb = nullptr;
@@ -862,7 +870,7 @@ int Engine::count_device(const uint8_t* d_text, uint64_t nbytes, const dk_input_
   };
   DK_TRY(Arena::ensure(this, H, (size_t)NC * G * F1 * 4));
   DK_TRY(Arena::ensure(this, O, (size_t)NC * G * F1 * 8));
-  DK_TRY(Arena::ensure(this, ctrs, 256));
+  DK_TRY(Arena::ensure(this, ctrs, 512));  // counters; the wave graph's WaveCtl at byte 256
   // device counters: [0] k-mers, [1] NUL-led line marker, [2] distinct total,
   // [3] device error (a bounded wait ran out), [4] bin ticket, [5] count overflow,
   // [6] hash bins sorted instead, [7] big bins to re-partition; LevelCounters at
@@ -941,8 +949,18 @@ int Engine::count_device(const uint8_t* d_text, uint64_t nbytes, const dk_input_
     stats.ms_device = ms;
     return DK_OK;
   }
-  // level-1 nodes and offsets
+  // level-1 nodes and offsets; a batch wave's graph keeps all of its tree's
+  // nodes in this buffer (sized here: the level-1 scan writes into it)
+  bool use_graph = js && !graph_off && !(flags & DK_FLAG_NO_GRAPH);
+  const double g_scale = (flags & DK_FLAG_GRAPH_MIN_BUFFERS) ? 0.0 : graph_scale;
   node_cap_needed = (size_t)F1;
+  if (use_graph) {
+    node_cap_needed += (size_t)(g_scale * 6.0 * (double)n_kmers / bin_target) + 4096;
+    if (Arena::ensure(this, nodes, node_cap_needed * sizeof(Node)) != DK_OK) {
+      use_graph = false;  // no room for the graph's tree: the host drives this wave
+      node_cap_needed = (size_t)F1;
+    }
+  }
   DK_TRY(Arena::ensure(this, nodes, node_cap_needed * sizeof(Node)));
   if (scattered) {
     TIMED(7, launch_l1_nodes((uint32_t*)H.p, NC * G, F1, (Node*)nodes.p, shift1, stream));
@@ -969,6 +987,24 @@ int Engine::count_device(const uint8_t* d_text, uint64_t nbytes, const dk_input_
     set_error("internal: no output buffers");
     return DK_ERR_INVALID_ARG;
   }
+  const int big_ok = use_hash ? 1 : (k <= 31 ? 2 : 0);
+  uint64_t tail[21];
+  if (use_graph) {
+    const int r = wave_graph_tail(F1, n_kmers, bin_target, use_hash, big_ok, g_scale, tail);
+    if (r == kGraphRetry) {
+      // count the wave again, its tail driven from the host (the reads are
+      // still in the device buffer); later waves get larger graph buffers
+      const uint64_t builds = stats.graph_builds;
+      graph_scale = std::min(graph_scale * 2.0, 16.0);
+      graph_off = true;
+      const int rr = count_device(d_text, nbytes, desc_in, out, js);
+      graph_off = false;
+      stats.graph_retries += 1;
+      stats.graph_builds += builds;
+      return rr;
+    }
+    DK_TRY(r);
+  } else {
   // Groups of consecutive level-1 buckets, each taken through its partition
   // levels, bin count, tree offsets and compact before the next: a group's
   // slice of the table is then final and is handed to out_sink while the
@@ -1003,7 +1039,6 @@ int Engine::count_device(const uint8_t* d_text, uint64_t nbytes, const dk_input_
   // the sort variant still counts a hot node of 2^31 keys or more as one hash
   // bin: splitting it would take many levels over all its keys, and near 2^32
   // keys the partition's 32-bit per-child offsets cannot hold it
-  const int big_ok = use_hash ? 1 : (k <= 31 ? 2 : 0);
   uint32_t node_end = (uint32_t)F1;  // nodes [0, node_end) exist
   uint32_t n_final = 0;              // final nodes listed so far (all groups)
   uint32_t n_bigf = 0;               // big-bin final nodes listed so far
@@ -1147,8 +1182,8 @@ int Engine::count_device(const uint8_t* d_text, uint64_t nbytes, const dk_input_
   }
   stats.n_bins = n_final + n_bigf - (uint32_t)stats.n_bins_retried;
   stats.n_groups = group_at.size() - 1;
-  uint64_t tail[21];
   DK_TRY(sync_read(c64 + 2, sizeof(tail), tail));
+  }  // host-driven tail
   stats.n_bins_resorted = tail[4];
   stats.n_bins_big = tail[15];
   stats.n_bins_packed = tail[19];
@@ -1185,6 +1220,99 @@ int Engine::count_device(const uint8_t* d_text, uint64_t nbytes, const dk_input_
   stats.n_distinct = n_distinct;
   stats.kernel_launches = launches;
   kresolve();
+  return DK_OK;
+}
+
+// The tail of a batch wave -- partition levels, bin count, tree offsets,
+// compact -- as one launch of the wave graph, after the level-1 scatter.  The
+// graph runs the level loop on the device (a conditional WHILE node whose
+// body plans the next level the way the host loop does), so the wave costs
+// one launch and one read of its counters instead of a launch per kernel and
+// a read per level.  Returns kGraphRetry when the wave must be counted again
+// with the host-driven tail: a level needed more nodes, tiles or histogram
+// than the graph's buffers hold, more levels than the level table, or a big
+// bin must be re-partitioned.  Fills tail[] (the counters from ctr[2] on).
+int Engine::wave_graph_tail(int F1, uint64_t n_kmers, int bin_target, bool use_hash, int big_ok,
+                            double scale, uint64_t* tail) {
+  Engine* e = this;
+  const double kmers = (double)n_kmers;
+  const uint64_t nodes_cap = node_cap_needed;  // the nodes buffer was sized for the graph
+  const uint64_t tiles_cap = (uint64_t)(scale * (kmers / kTileKeys + kmers / kBinCap)) + 1024;
+  // a tile's histogram row has 2^width <= 2^kGraphSplitBits entries: with
+  // tiles_cap tiles the histogram never outgrows this (4 KB per tile)
+  const uint64_t th_cap = tiles_cap << kGraphSplitBits;
+  if (nodes_cap >= (1ull << 31) || tiles_cap >= (1ull << 31)) return kGraphRetry;
+  // buffers the budget cannot hold: the host-driven tail sizes them per level
+  for (auto b : {std::make_pair(&finals, nodes_cap * 4), std::make_pair(&bigs, nodes_cap * 4),
+                 std::make_pair(&fbl, nodes_cap * 4),
+                 std::make_pair(&tiles, tiles_cap * sizeof(Tile)),
+                 std::make_pair(&TH, th_cap * 4)})
+    if (Arena::ensure(this, *b.first, b.second) != DK_OK) return kGraphRetry;
+  unsigned long long* c64 = (unsigned long long*)ctrs.p;
+  WaveGraphArgs ga = {};
+  ga.nodes = (Node*)nodes.p;
+  ga.finals = (uint32_t*)finals.p;
+  ga.bigs = (uint32_t*)bigs.p;
+  ga.fb_list = (uint32_t*)fbl.p;
+  ga.tiles = (Tile*)tiles.p;
+  ga.TH = (uint32_t*)TH.p;
+  ga.A = (uint64_t*)keysA.p;
+  ga.B = (uint64_t*)keysB.p;
+  ga.C = (uint32_t*)cnt.p;
+  ga.out_k = out_k;
+  ga.out_c = out_c;
+  ga.lc = (LevelCounters*)((char*)ctrs.p + 64);
+  ga.ctr = c64;
+  ga.wc = (WaveCtl*)((char*)ctrs.p + 256);
+  ga.bin_cap = kBinCap;
+  ga.split_target = 2 * bin_target;
+  ga.big_ok = big_ok;
+  ga.use_hash = use_hash ? 1 : 0;
+  ga.sm_count = sm_count;
+  if (!wave_exec || std::memcmp(&ga, &wave_args, sizeof(ga)) != 0) {
+    if (wave_exec) cudaGraphExecDestroy(wave_exec);
+    if (wave_graph) cudaGraphDestroy(wave_graph);
+    wave_exec = nullptr;
+    wave_graph = nullptr;
+    DK_CUDA(build_wave_graph(ga, s_cap, &wave_graph));
+    DK_CUDA(cudaGraphInstantiate(&wave_exec, wave_graph, 0));
+    wave_args = ga;
+    ++stats.graph_builds;
+  }
+  WaveCtl& w = *h_wc;
+  std::memset(&w, 0, sizeof(w));
+  w.lo = 0;
+  w.hi = (uint32_t)F1;
+  w.node_end = (uint32_t)F1;
+  w.F1 = (uint32_t)F1;
+  w.nodes_cap = (uint32_t)nodes_cap;
+  w.tiles_cap = (uint32_t)tiles_cap;
+  w.th_cap = th_cap;
+  DK_CUDA(cudaMemcpyAsync(ga.wc, h_wc, sizeof(WaveCtl), cudaMemcpyHostToDevice, stream));
+  DK_CUDA(cudaEventRecord(ev_stage[3], stream));
+  {
+    const int i0 = kbegin();
+    DK_CUDA(cudaGraphLaunch(wave_exec, stream));
+    kend(6, i0, 1);
+  }
+  DK_CUDA(cudaEventRecord(ev_stage[4], stream));
+  // the counters and the control block in one read
+  uint64_t blob[64];
+  DK_TRY(sync_read(ctrs.p, sizeof(blob), blob));
+  const LevelCounters* lv = (const LevelCounters*)((const char*)blob + 64);
+  const WaveCtl* wr = (const WaveCtl*)((const char*)blob + 256);
+  if (wr->too_big) {
+    set_error("a partition node holds >= 2^32 keys");
+    return DK_ERR_INVALID_ARG;
+  }
+  if (wr->overflow || blob[7] /* big bins to re-partition */) return kGraphRetry;
+  for (int i = 0; i < 21; ++i) tail[i] = blob[2 + i];
+  stats.graph_waves += 1;
+  stats.n_partitioned += wr->split_keys;
+  stats.partition_levels = std::max(stats.partition_levels, (int)wr->n_levels);
+  stats.n_bins = lv->n_final + lv->n_big_final;
+  stats.n_groups = 1;
+  launches += 1;
   return DK_OK;
 }
 
@@ -1343,10 +1471,13 @@ int Engine::count_locked(const char* text, uint64_t nbytes, bool text_on_device,
         if (!chunks.ev[c]) DK_CUDA(cudaEventCreate(&chunks.ev[c]));
         const uint64_t b0 = chunks.lines[c] * stride;
         const uint64_t b1 = c + 1 == kMaxChunks ? nbytes : chunks.lines[c + 1] * stride;
-        if (b1 > b0 && pinned)
+        // (the copy engine takes pageable chunks too, but its copy returns only
+        // when done: no chunk would be counted while the next uploads)
+        const bool dma = pinned;
+        if (b1 > b0 && dma)
           DK_CUDA(cudaMemcpyAsync((uint8_t*)this->text.p + b0, text + b0, b1 - b0,
                                   cudaMemcpyHostToDevice, s_in));
-        if (b1 > b0 && !pinned) {
+        if (b1 > b0 && !dma) {
           // the chunks launched so far read mapped memory: they finish
           // before the call returns
           if (!host_range_mapped(text + b0, b1 - b0)) {

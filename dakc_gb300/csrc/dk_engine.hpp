@@ -121,6 +121,19 @@ struct Engine {
   // device arenas
   DevBuf text, text2, keysA, keysB, cnt, H, O, nodes, tiles, TH, finals, bigs, rng, ctrs;
   DevBuf fbl;  // final nodes the packed bin kernel leaves to the general one
+  // batch waves: the tail of a wave (partition levels, bins, tree offsets,
+  // compact) as one launch of a CUDA graph built over the buffers in
+  // wave_args; rebuilt when a buffer moves
+  cudaStream_t s_cap = nullptr;       // graph capture only
+  cudaGraph_t wave_graph = nullptr;
+  cudaGraphExec_t wave_exec = nullptr;
+  WaveGraphArgs wave_args = {};
+  WaveCtl* h_wc = nullptr;            // page-locked: the control block a wave starts from
+  bool graph_off = false;             // the current count runs its tail from the host
+  double graph_scale = 1.0;           // graph buffers per k-mer; doubles when a wave outgrew them
+  static constexpr int kGraphRetry = 1;  // wave_graph_tail: count the wave without the graph
+  int wave_graph_tail(int F1, uint64_t n_kmers, int bin_target, bool use_hash, int big_ok,
+                      double scale, uint64_t* tail);
   size_t node_cap_needed = 0;
   uint64_t* out_k = nullptr;
   uint32_t* out_c = nullptr;

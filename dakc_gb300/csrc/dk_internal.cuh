@@ -195,4 +195,58 @@ int launch_compact(const Node* nodes, const uint32_t* final_list, uint32_t n_fin
 
 int bin_count_smem_bytes(int variant);
 
+// ------------------------------------------------ graph-driven wave tail
+// A batch wave's partition levels, bin count, tree offsets and compact run as
+// one CUDA graph: the level loop and the two tree passes are conditional
+// WHILE nodes, and every kernel reads the extents it works on from WaveCtl
+// (device memory) instead of from launch arguments, so the graph is built
+// once per set of buffers and replayed for every wave.
+constexpr int kGraphMaxLevels = 16;   // more levels: the wave is counted without the graph
+constexpr int kGraphSplitBits = 10;   // widest split in the graph (the tile scatter's
+                                      // shared memory is sized for it: two CTAs per SM)
+struct WaveCtl {
+  uint32_t lo, hi;           // nodes of the current level
+  uint32_t next_lo, next_hi;  // nodes of the next level (set by the plan)
+  uint32_t node_end;         // nodes [0, node_end) exist
+  uint32_t child_base;       // first child of the current level's split nodes
+  uint32_t n_tiles;          // partition tiles of the current level
+  uint32_t stop;             // the levels have ended: level kernels do nothing
+  uint32_t overflow;         // a buffer or the level table was too small: the host
+                             // counts the wave again without the graph
+  uint32_t too_big;          // a split node held >= 2^32 keys
+  uint32_t n_levels;         // levels so far, each recorded below
+  uint32_t F1;               // level-1 nodes
+  uint32_t nodes_cap, tiles_cap;
+  unsigned long long th_cap;       // tile-histogram entries
+  unsigned long long split_keys;   // keys the levels partitioned (all levels)
+  int32_t pass;              // tree passes: the level the next pass works on
+  uint32_t pass_skip;        // the current pass has nothing to do
+  uint32_t cur_lo, cur_hi;   // nodes of the current tree pass
+  uint32_t lv_lo[kGraphMaxLevels], lv_hi[kGraphMaxLevels];
+};
+
+// Fixed buffers and parameters a wave graph is built over.
+struct WaveGraphArgs {
+  Node* nodes;
+  uint32_t* finals;
+  uint32_t* bigs;
+  uint32_t* fb_list;
+  Tile* tiles;
+  uint32_t* TH;
+  uint64_t* A;
+  uint64_t* B;
+  uint32_t* C;
+  uint64_t* out_k;
+  uint32_t* out_c;
+  LevelCounters* lc;
+  unsigned long long* ctr;
+  WaveCtl* wc;
+  int bin_cap, split_target, big_ok, use_hash, sm_count;
+};
+// Build the graph of a wave's tail over `a`.  The level loop is one WHILE
+// node whose body runs one partition level; bottom-up sums and top-down
+// offsets are WHILE nodes over the recorded levels.  Returns a CUDA status.
+cudaError_t build_wave_graph(const WaveGraphArgs& a, cudaStream_t capture_stream,
+                             cudaGraph_t* out);
+
 }  // namespace dk

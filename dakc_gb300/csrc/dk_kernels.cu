@@ -28,6 +28,7 @@
 #include "dk_device.cuh"
 #include <algorithm>
 #include <cstdio>
+#include <vector>
 
 namespace dk {
 
@@ -828,11 +829,10 @@ __device__ __forceinline__ uint32_t node_tiles(const Node& nd, uint32_t i, const
 
 // Mark each node of the level final / split / empty; count what the split
 // nodes need (children, tiles, histogram entries).
-__global__ void k_classify(Node* nodes, uint32_t lo, uint32_t hi, uint32_t* final_list,
-                           uint32_t* big_list, LevelCounters* ctr, int bin_cap, int split_target,
-                           int big_ok, Ranges rg) {
-  const uint32_t i = lo + blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= hi) return;
+__device__ __forceinline__ void classify_node(Node* nodes, uint32_t i, uint32_t* final_list,
+                                              uint32_t* big_list, LevelCounters* ctr,
+                                              int bin_cap, int split_target, int big_ok,
+                                              const Ranges& rg, int max_bits) {
   const Node nd = nodes[i];
   if (nd.n == 0) {
     nodes[i].state = NODE_EMPTY;
@@ -858,7 +858,7 @@ __global__ void k_classify(Node* nodes, uint32_t lo, uint32_t hi, uint32_t* fina
   }
   const uint64_t target = (uint64_t)max(1, split_target / 2);  // children ~ target keys
   int w = ceil_log2_u64((nd.n + target - 1) / target);
-  w = max(1, min(w, kMaxSplitBits));
+  w = max(1, min(w, max_bits));
   const uint32_t nt = node_tiles(nd, i, rg);
   nodes[i].state = NODE_SPLIT;
   nodes[i].width = (uint8_t)w;
@@ -871,13 +871,20 @@ __global__ void k_classify(Node* nodes, uint32_t lo, uint32_t hi, uint32_t* fina
   if (nd.n >= (1ull << 32)) atomicOr(&ctr->too_big, 1u);
 }
 
+__global__ void k_classify(Node* nodes, uint32_t lo, uint32_t hi, uint32_t* final_list,
+                           uint32_t* big_list, LevelCounters* ctr, int bin_cap, int split_target,
+                           int big_ok, Ranges rg) {
+  const uint32_t i = lo + blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= hi) return;
+  classify_node(nodes, i, final_list, big_list, ctr, bin_cap, split_target, big_ok, rg,
+                kMaxSplitBits);
+}
+
 // Give each split node its children block, its partition tiles and their
 // histogram rows (buffers sized by the host from k_classify's counts); one
 // warp per node, its lanes write the tiles.
-__global__ void k_assign(Node* nodes, uint32_t lo, uint32_t hi, uint32_t child_base, Tile* tiles,
-                         LevelCounters* ctr, Ranges rg) {
-  const uint32_t i = lo + ((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
-  if (i >= hi) return;  // warp-uniform
+__device__ __forceinline__ void assign_node(Node* nodes, uint32_t i, uint32_t child_base,
+                                            Tile* tiles, LevelCounters* ctr, const Ranges& rg) {
   const Node nd = nodes[i];
   if (nd.state != NODE_SPLIT) return;
   const uint32_t R = 1u << nd.width;
@@ -927,15 +934,22 @@ __global__ void k_assign(Node* nodes, uint32_t lo, uint32_t hi, uint32_t child_b
   }
 }
 
+__global__ void k_assign(Node* nodes, uint32_t lo, uint32_t hi, uint32_t child_base, Tile* tiles,
+                         LevelCounters* ctr, Ranges rg) {
+  const uint32_t i = lo + ((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  if (i >= hi) return;  // warp-uniform
+  assign_node(nodes, i, child_base, tiles, ctr, rg);
+}
+
 __device__ __forceinline__ uint32_t digit_of(uint64_t key, int shift, int width) {
   return (uint32_t)(key >> (shift - width)) & ((1u << width) - 1u);
 }
 
-__global__ void __launch_bounds__(256) k_tile_hist(const Node* nodes, const Tile* tiles,
-                                                   const uint64_t* A, const uint64_t* B,
-                                                   uint32_t* TH) {
-  __shared__ uint32_t hist[1u << kMaxSplitBits];
-  const Tile tl = tiles[blockIdx.x];
+// one tile's digit histogram (the whole block; hist: 2^kMaxSplitBits entries)
+__device__ __forceinline__ void tile_hist_one(const Node* nodes, const Tile* tiles, uint32_t t,
+                                              const uint64_t* A, const uint64_t* B, uint32_t* TH,
+                                              uint32_t* hist) {
+  const Tile tl = tiles[t];
   const Node nd = nodes[tl.node];
   const uint32_t R = 1u << nd.width;
   const uint64_t* src = (nd.buf ? B : A) + tl.start;
@@ -957,13 +971,19 @@ __global__ void __launch_bounds__(256) k_tile_hist(const Node* nodes, const Tile
   for (uint32_t j = threadIdx.x; j < R; j += blockDim.x) TH[tl.th + j] = hist[j];
 }
 
+__global__ void __launch_bounds__(256) k_tile_hist(const Node* nodes, const Tile* tiles,
+                                                   const uint64_t* A, const uint64_t* B,
+                                                   uint32_t* TH) {
+  __shared__ uint32_t hist[1u << kMaxSplitBits];
+  tile_hist_one(nodes, tiles, blockIdx.x, A, B, TH, hist);
+}
+
 // one CTA per node of the level; split nodes turn their tiles' counts into
 // offsets within each child and create the 2^width children
-__global__ void __launch_bounds__(1024) k_node_scan(Node* nodes, uint32_t lo, Tile* tiles,
-                                                    uint32_t* TH) {
-  __shared__ unsigned long long csize[1u << kMaxSplitBits];
-  __shared__ unsigned long long tmp[32];
-  const uint32_t i = lo + blockIdx.x;
+// one node's scan (the whole block; csize: 2^kMaxSplitBits entries)
+__device__ __forceinline__ void node_scan_one(Node* nodes, uint32_t i, Tile* tiles, uint32_t* TH,
+                                              unsigned long long* csize,
+                                              unsigned long long* tmp) {
   const Node nd = nodes[i];
   if (nd.state != NODE_SPLIT) return;
   const uint32_t R = 1u << nd.width;
@@ -1017,6 +1037,13 @@ __global__ void __launch_bounds__(1024) k_node_scan(Node* nodes, uint32_t lo, Ti
   }
 }
 
+__global__ void __launch_bounds__(1024) k_node_scan(Node* nodes, uint32_t lo, Tile* tiles,
+                                                    uint32_t* TH) {
+  __shared__ unsigned long long csize[1u << kMaxSplitBits];
+  __shared__ unsigned long long tmp[32];
+  node_scan_one(nodes, lo + blockIdx.x, tiles, TH, csize, tmp);
+}
+
 // Partition one tile by the node's next `width` bits.  Pass 1 ranks every key
 // within its digit (shared atomics); the tile is then laid out digit by digit
 // in shared memory (keys re-read from L2) so each digit's keys leave as one
@@ -1028,18 +1055,17 @@ static_assert(kTileKeys <= 65536 && kTileKeysPerThread % 2 == 0, "ranks are pack
 #ifndef DK_TILE_CTAS
 #define DK_TILE_CTAS 2
 #endif
-__global__ void __launch_bounds__(kTileThreads, DK_TILE_CTAS) k_tile_scatter(const Node* nodes,
-                                                                  const Tile* tiles, uint64_t* A,
-                                                                  uint64_t* B,
-                                                                  const uint32_t* TH,
-                                                                  int max_width) {
-  extern __shared__ __align__(16) unsigned long long dsm[];
+// one tile (the whole block): dsm holds kTileKeys keys and 2^max_width
+// (base, count, location) entries
+__device__ __forceinline__ void tile_scatter_one(const Node* nodes, const Tile* tiles, uint32_t t,
+                                                 uint64_t* A, uint64_t* B, const uint32_t* TH,
+                                                 int max_width, unsigned long long* dsm,
+                                                 uint32_t* tmp) {
   unsigned long long* stage = dsm;                                  // kTileKeys
   unsigned long long* gbase = stage + kTileKeys;                    // 2^max_width
   uint32_t* cnt = reinterpret_cast<uint32_t*>(gbase + (1u << max_width));
   uint32_t* loc = cnt + (1u << max_width);
-  __shared__ uint32_t tmp[32];
-  const Tile tl = tiles[blockIdx.x];
+  const Tile tl = tiles[t];
   const Node nd = nodes[tl.node];
   const uint32_t R = 1u << nd.width;
   const int sh = nd.shift, w = nd.width;
@@ -1086,6 +1112,16 @@ __global__ void __launch_bounds__(kTileThreads, DK_TILE_CTAS) k_tile_scatter(con
     const uint32_t d = digit_of(key, sh, w);
     dst[gbase[d] + (i - loc[d])] = key;
   }
+}
+
+__global__ void __launch_bounds__(kTileThreads, DK_TILE_CTAS) k_tile_scatter(const Node* nodes,
+                                                                  const Tile* tiles, uint64_t* A,
+                                                                  uint64_t* B,
+                                                                  const uint32_t* TH,
+                                                                  int max_width) {
+  extern __shared__ __align__(16) unsigned long long dsm[];
+  __shared__ uint32_t tmp[32];
+  tile_scatter_one(nodes, tiles, blockIdx.x, A, B, TH, max_width, dsm, tmp);
 }
 
 // ------------------------------------------------------------ bin count
@@ -1929,7 +1965,8 @@ __device__ bool bin_packed(Node* nodes, uint32_t ni, const Node& nd, uint64_t* k
 // counts the bins it finished and ctr[22] the ones it left, over all passes.
 __global__ void __launch_bounds__(kPackThreads, kPackBlocksPerSM)
     k_bin_packed(Node* nodes, const uint32_t* __restrict__ finals, uint32_t n_bins, uint64_t* A,
-                 uint64_t* B, uint32_t* C, unsigned long long* ctr, uint32_t* fb_list) {
+                 uint64_t* B, uint32_t* C, unsigned long long* ctr, uint32_t* fb_list,
+                 const uint32_t* n_bins_dev) {
   extern __shared__ __align__(16) unsigned long long region[];
   __shared__ uint32_t tmp[64];
   __shared__ uint32_t mark[(1u << kPackDigitBits) / 32];
@@ -1938,6 +1975,8 @@ __global__ void __launch_bounds__(kPackThreads, kPackBlocksPerSM)
   // thread fetches the next bin's node while the CTA counts the current one
   __shared__ uint32_t s_b[2], s_ni[2];
   __shared__ Node s_node[2];
+  // with n_bins_dev the final list's length is only known on the device
+  if (n_bins_dev) n_bins = *n_bins_dev;
   unsigned int* ticket = reinterpret_cast<unsigned int*>(&ctr[19]);
   auto take = [&](int slot) {
     const uint32_t nb = atomicAdd(ticket, 1u);
@@ -1991,7 +2030,8 @@ __global__ void __launch_bounds__(kBinThreads, kBinBlocksPerSM) k_bin_count(Node
                                                               uint64_t* B, uint32_t* C,
                                                               unsigned long long* ctr,
                                                               int use_hash,
-                                                              const unsigned int* n_finals_dev) {
+                                                              const unsigned int* n_finals_dev,
+                                                              const uint32_t* n_big_dev) {
   extern __shared__ __align__(16) unsigned long long skeys[];  // kBinCap keys / 4096 u64 counts
   __shared__ uint32_t hist[1u << kBinDigitBits];
   __shared__ uint32_t tmp[64];
@@ -2002,6 +2042,7 @@ __global__ void __launch_bounds__(kBinThreads, kBinBlocksPerSM) k_bin_count(Node
   __shared__ bool s_hot;
   // with n_finals_dev the final list's length is only known on the device
   // (the packed bins' fallback list)
+  if (n_big_dev) n_big = *n_big_dev;
   if (n_finals_dev) n_bins = n_big + *n_finals_dev;
   if (threadIdx.x == 0) s_bin = atomicAdd(reinterpret_cast<unsigned int*>(&ctr[4]), 1u);
   __syncthreads();
@@ -2062,9 +2103,7 @@ __global__ void __launch_bounds__(kBinThreads, kBinBlocksPerSM) k_bin_count(Node
 
 // ----------------------------------------------------- tree reductions
 // one warp per node: a split node's distinct keys are its children's
-__global__ void k_aggregate(Node* nodes, uint32_t lo, uint32_t hi) {
-  const uint32_t i = lo + ((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
-  if (i >= hi) return;  // warp-uniform
+__device__ __forceinline__ void aggregate_node(Node* nodes, uint32_t i) {
   const uint32_t state = nodes[i].state;
   if (state != NODE_SPLIT) return;
   const uint32_t R = 1u << nodes[i].width, fc = nodes[i].first_child;
@@ -2075,11 +2114,17 @@ __global__ void k_aggregate(Node* nodes, uint32_t lo, uint32_t hi) {
   if (lane_id() == 0) nodes[i].d = d;
 }
 
+__global__ void k_aggregate(Node* nodes, uint32_t lo, uint32_t hi) {
+  const uint32_t i = lo + ((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  if (i >= hi) return;  // warp-uniform
+  aggregate_node(nodes, i);
+}
+
 // output offsets of level-1 nodes [b0, b1): they follow the *total_d distinct
 // keys placed before them, and *total_d grows by theirs
-__global__ void k_l1_out_offsets(Node* nodes, uint32_t b0, uint32_t b1,
-                                 unsigned long long* total_d) {
-  __shared__ unsigned long long tmp[32];
+__device__ __forceinline__ void l1_out_offsets_body(Node* nodes, uint32_t b0, uint32_t b1,
+                                                    unsigned long long* total_d,
+                                                    unsigned long long* tmp) {
   const uint32_t n1 = b1 - b0;
   const unsigned long long before = *total_d;
   const uint32_t per = (n1 + blockDim.x - 1) / blockDim.x;
@@ -2096,9 +2141,15 @@ __global__ void k_l1_out_offsets(Node* nodes, uint32_t b0, uint32_t b1,
   if (threadIdx.x == 0) *total_d = before + tot;
 }
 
-__global__ void __launch_bounds__(256) k_child_offsets(Node* nodes, uint32_t lo) {
+__global__ void k_l1_out_offsets(Node* nodes, uint32_t b0, uint32_t b1,
+                                 unsigned long long* total_d) {
   __shared__ unsigned long long tmp[32];
-  const Node nd = nodes[lo + blockIdx.x];
+  l1_out_offsets_body(nodes, b0, b1, total_d, tmp);
+}
+
+__device__ __forceinline__ void child_offsets_one(Node* nodes, uint32_t i,
+                                                  unsigned long long* tmp) {
+  const Node nd = nodes[i];
   if (nd.state != NODE_SPLIT) return;
   const uint32_t R = 1u << nd.width;
   const uint32_t per = (R + blockDim.x - 1) / blockDim.x;
@@ -2111,6 +2162,11 @@ __global__ void __launch_bounds__(256) k_child_offsets(Node* nodes, uint32_t lo)
     ch.out_off = base;
     base += ch.d;
   }
+}
+
+__global__ void __launch_bounds__(256) k_child_offsets(Node* nodes, uint32_t lo) {
+  __shared__ unsigned long long tmp[32];
+  child_offsets_one(nodes, lo + blockIdx.x, tmp);
 }
 
 // Re-partition NODE_RETRY nodes: each gets a proxy copy appended after the
@@ -2141,12 +2197,11 @@ __global__ void k_make_proxies(Node* nodes, const uint32_t* __restrict__ finals,
 }
 
 // one warp per final node: staged pairs -> output table
-__global__ void k_compact(const Node* nodes, const uint32_t* __restrict__ finals, uint32_t n_final,
-                          const uint64_t* A, const uint64_t* B, const uint32_t* C,
-                          uint64_t* __restrict__ out_k, uint32_t* __restrict__ out_c) {
-  const uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  if (w >= n_final) return;
-  const Node nd = nodes[finals[w]];
+__device__ __forceinline__ void compact_one(const Node* nodes, uint32_t ni, const uint64_t* A,
+                                            const uint64_t* B, const uint32_t* C,
+                                            uint64_t* __restrict__ out_k,
+                                            uint32_t* __restrict__ out_c) {
+  const Node nd = nodes[ni];
   if (nd.state != NODE_FINAL) return;  // re-partitioned after its bin count failed
   const uint64_t* sk = (nd.buf ? B : A) + nd.start;
   const uint32_t* sc = C + nd.start;
@@ -2154,6 +2209,198 @@ __global__ void k_compact(const Node* nodes, const uint32_t* __restrict__ finals
     out_k[nd.out_off + i] = sk[i];
     out_c[nd.out_off + i] = sc[i];
   }
+}
+
+__global__ void k_compact(const Node* nodes, const uint32_t* __restrict__ finals, uint32_t n_final,
+                          const uint64_t* A, const uint64_t* B, const uint32_t* C,
+                          uint64_t* __restrict__ out_k, uint32_t* __restrict__ out_c) {
+  const uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (w >= n_final) return;
+  compact_one(nodes, finals[w], A, B, C, out_k, out_c);
+}
+
+// ------------------------------------------------ graph-driven wave tail
+// The kernels of a wave graph: each reads the extents it works on from the
+// WaveCtl and loops over them with a grid fixed when the graph was built.
+
+// A level begins: its node range (the range the previous level's plan set)
+// and its counters cleared (n_final and n_big_final run over all levels).
+__global__ void k_g_level_begin(LevelCounters* lc, WaveCtl* wc) {
+  if (threadIdx.x || blockIdx.x || wc->stop) return;
+  if (wc->n_levels) {
+    wc->lo = wc->next_lo;
+    wc->hi = wc->next_hi;
+  }
+  lc->n_split = 0;
+  lc->n_tiles = 0;
+  lc->too_big = 0;
+  lc->n_children = 0;
+  lc->max_width = 0;
+  lc->split_keys = 0;
+  lc->th_entries = 0;
+  lc->n_tiles_assigned = 0;
+  lc->n_children_assigned = 0;
+  lc->th_assigned = 0;
+}
+
+__global__ void k_g_classify(Node* nodes, uint32_t* finals, uint32_t* bigs, LevelCounters* lc,
+                             int bin_cap, int split_target, int big_ok, const WaveCtl* wc) {
+  if (wc->stop) return;
+  const uint32_t lo = wc->lo, hi = wc->hi;
+  const Ranges rg{nullptr, nullptr, 0, 0};
+  for (uint32_t i = lo + blockIdx.x * blockDim.x + threadIdx.x; i < hi;
+       i += gridDim.x * blockDim.x)
+    classify_node(nodes, i, finals, bigs, lc, bin_cap, split_target, big_ok, rg,
+                  kGraphSplitBits);
+}
+
+// What the host does between classify and assign: record the level, end the
+// loop when nothing splits (or a buffer would overflow), else lay out the
+// children and tiles of the split nodes.  One thread.
+__global__ void k_g_plan(LevelCounters* lc, WaveCtl* wc, cudaGraphConditionalHandle h) {
+  if (threadIdx.x || blockIdx.x) return;
+  if (wc->stop) {
+    cudaGraphSetConditional(h, 0);
+    return;
+  }
+  const uint32_t L = wc->n_levels;
+  bool end = false;
+  if (L >= (uint32_t)kGraphMaxLevels) {
+    wc->overflow = 1;
+    end = true;
+  } else {
+    wc->lv_lo[L] = wc->lo;
+    wc->lv_hi[L] = wc->hi;
+    wc->n_levels = L + 1;
+    if (lc->too_big) {
+      wc->too_big = 1;
+      end = true;
+    } else if (lc->n_split == 0) {
+      end = true;
+    } else if ((unsigned long long)wc->node_end + lc->n_children > wc->nodes_cap ||
+               lc->n_tiles > wc->tiles_cap || lc->th_entries > wc->th_cap) {
+      wc->overflow = 1;
+      end = true;
+    }
+  }
+  if (end) {
+    wc->stop = 1;
+    if (wc->overflow || wc->too_big) {  // nothing after the levels runs
+      lc->n_final = 0;
+      lc->n_big_final = 0;
+    }
+    cudaGraphSetConditional(h, 0);
+    return;
+  }
+  wc->split_keys += lc->split_keys;
+  wc->n_tiles = lc->n_tiles;
+  wc->child_base = wc->node_end;
+  wc->next_lo = wc->node_end;
+  wc->next_hi = wc->node_end + lc->n_children;
+  wc->node_end = wc->next_hi;
+}
+
+__global__ void k_g_assign(Node* nodes, Tile* tiles, LevelCounters* lc, const WaveCtl* wc) {
+  if (wc->stop) return;
+  const uint32_t lo = wc->lo, hi = wc->hi, cb = wc->child_base;
+  const Ranges rg{nullptr, nullptr, 0, 0};
+  const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+  for (uint32_t i = lo + ((blockIdx.x * blockDim.x + threadIdx.x) >> 5); i < hi; i += nw)
+    assign_node(nodes, i, cb, tiles, lc, rg);  // warp-uniform
+}
+
+__global__ void __launch_bounds__(256) k_g_tile_hist(const Node* nodes, const Tile* tiles,
+                                                     const uint64_t* A, const uint64_t* B,
+                                                     uint32_t* TH, const WaveCtl* wc) {
+  __shared__ uint32_t hist[1u << kMaxSplitBits];
+  if (wc->stop) return;
+  const uint32_t nt = wc->n_tiles;
+  for (uint32_t t = blockIdx.x; t < nt; t += gridDim.x) {
+    tile_hist_one(nodes, tiles, t, A, B, TH, hist);
+    __syncthreads();
+  }
+}
+
+__global__ void __launch_bounds__(512) k_g_node_scan(Node* nodes, Tile* tiles, uint32_t* TH,
+                                                     const WaveCtl* wc) {
+  __shared__ unsigned long long csize[1u << kMaxSplitBits];
+  __shared__ unsigned long long tmp[32];
+  if (wc->stop) return;
+  const uint32_t lo = wc->lo, hi = wc->hi;
+  for (uint32_t i = lo + blockIdx.x; i < hi; i += gridDim.x) {
+    node_scan_one(nodes, i, tiles, TH, csize, tmp);
+    __syncthreads();
+  }
+}
+
+__global__ void __launch_bounds__(kTileThreads, DK_TILE_CTAS) k_g_tile_scatter(
+    const Node* nodes, const Tile* tiles, uint64_t* A, uint64_t* B, const uint32_t* TH,
+    const WaveCtl* wc) {
+  extern __shared__ __align__(16) unsigned long long dsm[];
+  __shared__ uint32_t tmp[32];
+  if (wc->stop) return;
+  const uint32_t nt = wc->n_tiles;
+  for (uint32_t t = blockIdx.x; t < nt; t += gridDim.x) {
+    tile_scatter_one(nodes, tiles, t, A, B, TH, kGraphSplitBits, dsm, tmp);
+    __syncthreads();
+  }
+}
+
+// Tree passes over the recorded levels: bottom-up (up = 1, distinct counts)
+// from the last splitting level, top-down (up = 0, offsets) from level 0.
+__global__ void k_g_pass_begin(WaveCtl* wc, int up) {
+  if (threadIdx.x || blockIdx.x) return;
+  wc->pass = up ? (int)wc->n_levels - 2 : 0;
+}
+
+__global__ void k_g_pass_step(WaveCtl* wc, cudaGraphConditionalHandle h, int up) {
+  if (threadIdx.x || blockIdx.x) return;
+  const int p = wc->pass, last = (int)wc->n_levels - 2;  // the levels that split
+  if (wc->overflow || wc->too_big || p < 0 || p > last) {
+    wc->pass_skip = 1;
+    cudaGraphSetConditional(h, 0);
+    return;
+  }
+  wc->pass_skip = 0;
+  wc->cur_lo = wc->lv_lo[p];
+  wc->cur_hi = wc->lv_hi[p];
+  const int np = up ? p - 1 : p + 1;
+  wc->pass = np;
+  cudaGraphSetConditional(h, (np >= 0 && np <= last) ? 1u : 0u);
+}
+
+__global__ void k_g_aggregate(Node* nodes, const WaveCtl* wc) {
+  if (wc->pass_skip) return;
+  const uint32_t lo = wc->cur_lo, hi = wc->cur_hi;
+  const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+  for (uint32_t i = lo + ((blockIdx.x * blockDim.x + threadIdx.x) >> 5); i < hi; i += nw)
+    aggregate_node(nodes, i);  // warp-uniform
+}
+
+__global__ void __launch_bounds__(256) k_g_child_offsets(Node* nodes, const WaveCtl* wc) {
+  __shared__ unsigned long long tmp[32];
+  if (wc->pass_skip) return;
+  const uint32_t lo = wc->cur_lo, hi = wc->cur_hi;
+  for (uint32_t i = lo + blockIdx.x; i < hi; i += gridDim.x) {
+    child_offsets_one(nodes, i, tmp);
+    __syncthreads();
+  }
+}
+
+__global__ void k_g_l1_offsets(Node* nodes, unsigned long long* total_d, const WaveCtl* wc) {
+  __shared__ unsigned long long tmp[32];
+  if (wc->overflow || wc->too_big) return;
+  l1_out_offsets_body(nodes, 0, wc->F1, total_d, tmp);
+}
+
+__global__ void k_g_compact(const Node* nodes, const uint32_t* __restrict__ finals,
+                            const uint32_t* n_dev, const uint64_t* A, const uint64_t* B,
+                            const uint32_t* C, uint64_t* __restrict__ out_k,
+                            uint32_t* __restrict__ out_c) {
+  const uint32_t n = *n_dev;
+  const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+  for (uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < n; w += nw)
+    compact_one(nodes, finals[w], A, B, C, out_k, out_c);  // warp-uniform
 }
 
 // Small copies between device and page-locked host memory done by a kernel
@@ -2244,9 +2491,14 @@ int launch_copy_small(const void* src, void* dst, uint64_t bytes, cudaStream_t s
 int launch_copy_in(const void* src, void* dst, uint64_t bytes, int sm_count, cudaStream_t s) {
   if (!bytes) return 0;
   const uint64_t words = bytes / 16 + 2;
-  // one CTA per SM saturates the link (any grid measures the same rate) and
-  // leaves the SMs to kernels that overlap the copy
-  const uint32_t blocks = (uint32_t)std::min<uint64_t>((uint64_t)sm_count, (words + 255) / 256);
+  // a CTA on every other SM: the chunked upload overlaps the level-1 kernels,
+  // which it slows least at this size (large_100m end to end, pageable reads:
+  // 71.0 ms with 76 CTAs, 76.3 with 152, 74.6 with 38; page-locked 69.0)
+#ifndef DK_COPY_IN_CTAS_PCT
+#define DK_COPY_IN_CTAS_PCT 50
+#endif
+  const uint64_t ctas = std::max<uint64_t>(1, (uint64_t)sm_count * DK_COPY_IN_CTAS_PCT / 100);
+  const uint32_t blocks = (uint32_t)std::min<uint64_t>(ctas, (words + 255) / 256);
   k_copy_in<<<blocks, 256, 0, s>>>((const uint8_t*)src, (uint8_t*)dst, bytes);
   return 1;
 }
@@ -2497,7 +2749,7 @@ int launch_bin_count(Node* nodes, const uint32_t* big_list, uint32_t n_big,
   if (!use_hash || !fb_list) {
     const uint32_t grid = std::min<uint32_t>(n_bins, (uint32_t)(kBinBlocksPerSM * sm_count));
     k_bin_count<<<grid, kBinThreads, kBinCap * 8, s>>>(nodes, big_list, n_big, final_list, n_bins,
-                                                       A, B, C, ctr, use_hash, nullptr);
+                                                       A, B, C, ctr, use_hash, nullptr, nullptr);
     return 1;
   }
   // hash variant: the packed kernel takes the final list; what it leaves
@@ -2507,13 +2759,14 @@ int launch_bin_count(Node* nodes, const uint32_t* big_list, uint32_t n_big,
     allow_max_smem(k_bin_packed);
     const uint32_t grid = std::min<uint32_t>(n_final, (uint32_t)(kPackBlocksPerSM * sm_count));
     k_bin_packed<<<grid, kPackThreads, kPackSmem, s>>>(nodes, final_list, n_final, A, B, C, ctr,
-                                                       fb_list);
+                                                       fb_list, nullptr);
     ++launches;
   }
   const uint32_t grid = std::min<uint32_t>(n_bins, (uint32_t)(kBinBlocksPerSM * sm_count));
   k_bin_count<<<grid, kBinThreads, kBinCap * 8, s>>>(nodes, big_list, n_big, fb_list, 0, A, B, C,
                                                      ctr, use_hash,
-                                                     reinterpret_cast<const unsigned int*>(&ctr[20]));
+                                                     reinterpret_cast<const unsigned int*>(&ctr[20]),
+                                                     nullptr);
   return launches + 1;
 }
 
@@ -2543,6 +2796,138 @@ int launch_compact(const Node* nodes, const uint32_t* final_list, uint32_t n_fin
   k_compact<<<(n_final + warps_per_block - 1) / warps_per_block, 256, 0, s>>>(
       nodes, final_list, n_final, A, B, C, out_k, out_c);
   return 1;
+}
+
+
+// The wave graph (see dk_internal.cuh):
+//   WHILE level: [begin, classify, plan, assign, tile hist, node scan, tile scatter]
+//   packed bins -> general bins -> up-pass start
+//   WHILE up:    [pass step, aggregate]
+//   level-1 offsets -> down-pass start
+//   WHILE down:  [pass step, child offsets]
+//   compact finals -> compact big bins
+// Segments between conditional nodes are captured from `cs` into the graph.
+namespace {
+
+#define DK_GTRY(x)                          \
+  do {                                      \
+    const cudaError_t _e = (x);             \
+    if (_e != cudaSuccess) return _e;       \
+  } while (0)
+
+// add a WHILE node after deps; *body receives its body graph
+cudaError_t add_while(cudaGraph_t g, const std::vector<cudaGraphNode_t>& deps,
+                      cudaGraphConditionalHandle* h, cudaGraphNode_t* node, cudaGraph_t* body) {
+  DK_GTRY(cudaGraphConditionalHandleCreate(h, g, 1, cudaGraphCondAssignDefault));
+  cudaGraphNodeParams p = {};
+  p.type = cudaGraphNodeTypeConditional;
+  p.conditional.handle = *h;
+  p.conditional.type = cudaGraphCondTypeWhile;
+  p.conditional.size = 1;
+  DK_GTRY(cudaGraphAddNode(node, g, deps.empty() ? nullptr : deps.data(), nullptr, deps.size(),
+                           &p));
+  *body = p.conditional.phGraph_out[0];
+  return cudaSuccess;
+}
+
+// end a capture into g, returning the nodes the next segment depends on
+cudaError_t end_segment(cudaStream_t cs, cudaGraph_t g, std::vector<cudaGraphNode_t>* leaves) {
+  cudaStreamCaptureStatus st;
+  const cudaGraphNode_t* deps = nullptr;
+  size_t nd = 0;
+  DK_GTRY(cudaStreamGetCaptureInfo(cs, &st, nullptr, nullptr, &deps, nullptr, &nd));
+  std::vector<cudaGraphNode_t> v(deps, deps + nd);
+  cudaGraph_t out = g;
+  DK_GTRY(cudaStreamEndCapture(cs, &out));
+  *leaves = v;
+  return cudaSuccess;
+}
+
+cudaError_t begin_segment(cudaStream_t cs, cudaGraph_t g, const std::vector<cudaGraphNode_t>& deps) {
+  return cudaStreamBeginCaptureToGraph(cs, g, deps.empty() ? nullptr : deps.data(), nullptr,
+                                       deps.size(), cudaStreamCaptureModeRelaxed);
+}
+
+}  // namespace
+
+cudaError_t build_wave_graph(const WaveGraphArgs& a, cudaStream_t cs, cudaGraph_t* out) {
+  const int S = a.sm_count;
+  const size_t scatter_smem = (size_t)kTileKeys * 8 + ((size_t)1 << kGraphSplitBits) * 16;
+  allow_max_smem(k_g_tile_scatter);
+  allow_max_smem(k_bin_packed);
+  allow_max_smem(k_bin_count);
+  cudaGraph_t g = nullptr;
+  DK_GTRY(cudaGraphCreate(&g, 0));
+  cudaError_t err = [&]() -> cudaError_t {
+    // the level loop
+    cudaGraphConditionalHandle h_lvl, h_up, h_down;
+    cudaGraphNode_t n_lvl, n_up, n_down;
+    cudaGraph_t body;
+    DK_GTRY(add_while(g, {}, &h_lvl, &n_lvl, &body));
+    DK_GTRY(begin_segment(cs, body, {}));
+    k_g_level_begin<<<1, 32, 0, cs>>>(a.lc, a.wc);
+    k_g_classify<<<2 * S, 256, 0, cs>>>(a.nodes, a.finals, a.bigs, a.lc, a.bin_cap,
+                                        a.split_target, a.big_ok, a.wc);
+    k_g_plan<<<1, 32, 0, cs>>>(a.lc, a.wc, h_lvl);
+    k_g_assign<<<2 * S, 256, 0, cs>>>(a.nodes, a.tiles, a.lc, a.wc);
+    k_g_tile_hist<<<4 * S, 256, 0, cs>>>(a.nodes, a.tiles, a.A, a.B, a.TH, a.wc);
+    k_g_node_scan<<<2 * S, 512, 0, cs>>>(a.nodes, a.tiles, a.TH, a.wc);
+    k_g_tile_scatter<<<DK_TILE_CTAS * S, kTileThreads, scatter_smem, cs>>>(a.nodes, a.tiles, a.A,
+                                                                          a.B, a.TH, a.wc);
+    std::vector<cudaGraphNode_t> leaves;
+    DK_GTRY(end_segment(cs, body, &leaves));
+    // the bins of the final nodes, big bins first
+    DK_GTRY(begin_segment(cs, g, {n_lvl}));
+    const uint32_t* n_final = &a.lc->n_final;
+    const uint32_t* n_big = &a.lc->n_big_final;
+    if (a.use_hash) {
+      k_bin_packed<<<kPackBlocksPerSM * S, kPackThreads, kPackSmem, cs>>>(
+          a.nodes, a.finals, 0, a.A, a.B, a.C, a.ctr, a.fb_list, n_final);
+      k_bin_count<<<kBinBlocksPerSM * S, kBinThreads, kBinCap * 8, cs>>>(
+          a.nodes, a.bigs, 0, a.fb_list, 0, a.A, a.B, a.C, a.ctr, 1,
+          reinterpret_cast<const unsigned int*>(&a.ctr[20]), n_big);
+    } else {
+      k_bin_count<<<kBinBlocksPerSM * S, kBinThreads, kBinCap * 8, cs>>>(
+          a.nodes, a.bigs, 0, a.finals, 0, a.A, a.B, a.C, a.ctr, 0, n_final, n_big);
+    }
+    k_g_pass_begin<<<1, 32, 0, cs>>>(a.wc, 1);
+    DK_GTRY(end_segment(cs, g, &leaves));
+    // distinct counts up the tree
+    DK_GTRY(add_while(g, leaves, &h_up, &n_up, &body));
+    DK_GTRY(begin_segment(cs, body, {}));
+    k_g_pass_step<<<1, 32, 0, cs>>>(a.wc, h_up, 1);
+    k_g_aggregate<<<S, 256, 0, cs>>>(a.nodes, a.wc);
+    DK_GTRY(end_segment(cs, body, &leaves));
+    // level-1 offsets, then offsets down the tree
+    DK_GTRY(begin_segment(cs, g, {n_up}));
+    k_g_l1_offsets<<<1, 1024, 0, cs>>>(a.nodes, &a.ctr[2], a.wc);
+    k_g_pass_begin<<<1, 32, 0, cs>>>(a.wc, 0);
+    DK_GTRY(end_segment(cs, g, &leaves));
+    DK_GTRY(add_while(g, leaves, &h_down, &n_down, &body));
+    DK_GTRY(begin_segment(cs, body, {}));
+    k_g_pass_step<<<1, 32, 0, cs>>>(a.wc, h_down, 0);
+    k_g_child_offsets<<<2 * S, 256, 0, cs>>>(a.nodes, a.wc);
+    DK_GTRY(end_segment(cs, body, &leaves));
+    // the bins' pairs into the table
+    DK_GTRY(begin_segment(cs, g, {n_down}));
+    k_g_compact<<<4 * S, 256, 0, cs>>>(a.nodes, a.finals, n_final, a.A, a.B, a.C, a.out_k,
+                                       a.out_c);
+    k_g_compact<<<4 * S, 256, 0, cs>>>(a.nodes, a.bigs, n_big, a.A, a.B, a.C, a.out_k, a.out_c);
+    DK_GTRY(end_segment(cs, g, &leaves));
+    return cudaGetLastError();
+  }();
+  if (err != cudaSuccess) {
+    cudaStreamCaptureStatus st;
+    if (cudaStreamIsCapturing(cs, &st) == cudaSuccess && st != cudaStreamCaptureStatusNone) {
+      cudaGraph_t junk = nullptr;
+      cudaStreamEndCapture(cs, &junk);
+    }
+    cudaGraphDestroy(g);
+    cudaGetLastError();
+    return err;
+  }
+  *out = g;
+  return cudaSuccess;
 }
 
 }  // namespace dk

@@ -177,6 +177,7 @@ int dk_serve_start(dk_ctx* ctx, int workers, int max_batch_jobs) {
     dk_config cfg{};
     cfg.device = base->device;
     cfg.mem_budget = share;
+    cfg.flags = base->flags;  // workers count as the context would
     const int rc = s->workers[w].eng->init(&cfg);
     if (rc != DK_OK) {
       delete s;

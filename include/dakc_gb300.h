@@ -93,6 +93,15 @@ typedef struct {
  * chip-to-chip access), chunk by chunk like page-locked reads; with this flag
  * they are staged through page-locked slots by host threads instead */
 #define DK_FLAG_STAGE_PAGEABLE 2ull
+/* Batch waves (dk_count_batch, serving) run their partition levels, bin
+ * count, tree offsets and compact as one launch of a CUDA graph whose level
+ * loop is a conditional node; with this flag the host drives them launch by
+ * launch, as for dk_count (the same tables) */
+#define DK_FLAG_NO_GRAPH 4ull
+/* Size the wave graph's buffers at their minimum, so that a wave whose
+ * levels outgrow them is counted again with the host-driven tail (tests the
+ * fallback; tables are the same) */
+#define DK_FLAG_GRAPH_MIN_BUFFERS 8ull
 
 typedef struct {
   int line_width;  /* READLEN: bytes per line before the terminator (>= 1)      */
@@ -132,7 +141,9 @@ typedef struct {
   uint64_t n_bins;
   /* CUDA-event time of the main kernels (ms, summed over launches):
      [0] extract+count  [1] extract+scatter  [2] partition histogram
-     [3] partition scatter  [4] bin count  [5] compact  [6] hash insert
+     [3] partition scatter  [4] bin count  [5] compact
+     [6] batch waves' graphs (partition levels, bin count, tree offsets and
+         compact of a wave in one CUDA graph launch)
      [7] everything else (scans, classify, tree offsets) */
   double ms_kernel[8];
   uint64_t launches_kernel[8];
@@ -155,6 +166,11 @@ typedef struct {
                                hold (counted by the general bin kernel)        */
   uint64_t upload_in_place; /* 1: pageable reads were read in place by the device
                                (no page-locked staging)                        */
+  uint64_t graph_waves;     /* batch waves whose tail ran as one graph launch   */
+  uint64_t graph_builds;    /* wave graphs built (and instantiated) by the call */
+  uint64_t graph_retries;   /* waves counted again with the host-driven tail (a
+                               level outgrew the graph's buffers, or a big bin
+                               had to be re-partitioned)                       */
 } dk_stats;
 
 /* One read set of a batch (dk_count_batch). */
