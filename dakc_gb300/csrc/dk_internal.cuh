@@ -222,6 +222,10 @@ struct WaveCtl {
   int32_t pass;              // tree passes: the level the next pass works on
   uint32_t pass_skip;        // the current pass has nothing to do
   uint32_t cur_lo, cur_hi;   // nodes of the current tree pass
+  // work tickets: tiles of the level's histogram and scatter, final and
+  // big-bin nodes of the compact (taken one at a time, so blocks that finish
+  // early take more, as with a grid of one block per item)
+  uint32_t tk_hist, tk_scatter, tk_compact[2];
   uint32_t lv_lo[kGraphMaxLevels], lv_hi[kGraphMaxLevels];
 };
 

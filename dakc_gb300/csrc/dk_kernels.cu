@@ -2294,6 +2294,8 @@ __global__ void k_g_plan(LevelCounters* lc, WaveCtl* wc, cudaGraphConditionalHan
   }
   wc->split_keys += lc->split_keys;
   wc->n_tiles = lc->n_tiles;
+  wc->tk_hist = 0;
+  wc->tk_scatter = 0;
   wc->child_base = wc->node_end;
   wc->next_lo = wc->node_end;
   wc->next_hi = wc->node_end + lc->n_children;
@@ -2309,19 +2311,29 @@ __global__ void k_g_assign(Node* nodes, Tile* tiles, LevelCounters* lc, const Wa
     assign_node(nodes, i, cb, tiles, lc, rg);  // warp-uniform
 }
 
+// the next work ticket of the block (thread 0 takes it, all threads get it)
+__device__ __forceinline__ uint32_t block_ticket(uint32_t* tk, uint32_t* s_t) {
+  if (threadIdx.x == 0) *s_t = atomicAdd(tk, 1u);
+  __syncthreads();
+  const uint32_t t = *s_t;
+  __syncthreads();  // every thread has read it before it is replaced
+  return t;
+}
+
 __global__ void __launch_bounds__(256) k_g_tile_hist(const Node* nodes, const Tile* tiles,
                                                      const uint64_t* A, const uint64_t* B,
-                                                     uint32_t* TH, const WaveCtl* wc) {
+                                                     uint32_t* TH, WaveCtl* wc) {
   __shared__ uint32_t hist[1u << kMaxSplitBits];
+  __shared__ uint32_t s_t;
   if (wc->stop) return;
   const uint32_t nt = wc->n_tiles;
-  for (uint32_t t = blockIdx.x; t < nt; t += gridDim.x) {
+  for (uint32_t t = block_ticket(&wc->tk_hist, &s_t); t < nt; t = block_ticket(&wc->tk_hist, &s_t)) {
     tile_hist_one(nodes, tiles, t, A, B, TH, hist);
     __syncthreads();
   }
 }
 
-__global__ void __launch_bounds__(512) k_g_node_scan(Node* nodes, Tile* tiles, uint32_t* TH,
+__global__ void __launch_bounds__(256) k_g_node_scan(Node* nodes, Tile* tiles, uint32_t* TH,
                                                      const WaveCtl* wc) {
   __shared__ unsigned long long csize[1u << kMaxSplitBits];
   __shared__ unsigned long long tmp[32];
@@ -2335,12 +2347,14 @@ __global__ void __launch_bounds__(512) k_g_node_scan(Node* nodes, Tile* tiles, u
 
 __global__ void __launch_bounds__(kTileThreads, DK_TILE_CTAS) k_g_tile_scatter(
     const Node* nodes, const Tile* tiles, uint64_t* A, uint64_t* B, const uint32_t* TH,
-    const WaveCtl* wc) {
+    WaveCtl* wc) {
   extern __shared__ __align__(16) unsigned long long dsm[];
   __shared__ uint32_t tmp[32];
+  __shared__ uint32_t s_t;
   if (wc->stop) return;
   const uint32_t nt = wc->n_tiles;
-  for (uint32_t t = blockIdx.x; t < nt; t += gridDim.x) {
+  for (uint32_t t = block_ticket(&wc->tk_scatter, &s_t); t < nt;
+       t = block_ticket(&wc->tk_scatter, &s_t)) {
     tile_scatter_one(nodes, tiles, t, A, B, TH, kGraphSplitBits, dsm, tmp);
     __syncthreads();
   }
@@ -2351,6 +2365,8 @@ __global__ void __launch_bounds__(kTileThreads, DK_TILE_CTAS) k_g_tile_scatter(
 __global__ void k_g_pass_begin(WaveCtl* wc, int up) {
   if (threadIdx.x || blockIdx.x) return;
   wc->pass = up ? (int)wc->n_levels - 2 : 0;
+  wc->tk_compact[0] = 0;
+  wc->tk_compact[1] = 0;
 }
 
 __global__ void k_g_pass_step(WaveCtl* wc, cudaGraphConditionalHandle h, int up) {
@@ -2393,14 +2409,19 @@ __global__ void k_g_l1_offsets(Node* nodes, unsigned long long* total_d, const W
   l1_out_offsets_body(nodes, 0, wc->F1, total_d, tmp);
 }
 
+// one warp per node, nodes taken by ticket (*tk)
 __global__ void k_g_compact(const Node* nodes, const uint32_t* __restrict__ finals,
-                            const uint32_t* n_dev, const uint64_t* A, const uint64_t* B,
-                            const uint32_t* C, uint64_t* __restrict__ out_k,
+                            const uint32_t* n_dev, uint32_t* tk, const uint64_t* A,
+                            const uint64_t* B, const uint32_t* C, uint64_t* __restrict__ out_k,
                             uint32_t* __restrict__ out_c) {
   const uint32_t n = *n_dev;
-  const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
-  for (uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < n; w += nw)
-    compact_one(nodes, finals[w], A, B, C, out_k, out_c);  // warp-uniform
+  for (;;) {
+    uint32_t w = 0;
+    if (lane_id() == 0) w = atomicAdd(tk, 1u);
+    w = __shfl_sync(0xFFFFFFFFu, w, 0);
+    if (w >= n) break;  // warp-uniform
+    compact_one(nodes, finals[w], A, B, C, out_k, out_c);
+  }
 }
 
 // Small copies between device and page-locked host memory done by a kernel
@@ -2807,6 +2828,8 @@ int launch_compact(const Node* nodes, const uint32_t* final_list, uint32_t n_fin
 //   WHILE down:  [pass step, child offsets]
 //   compact finals -> compact big bins
 // Segments between conditional nodes are captured from `cs` into the graph.
+// Grids are fixed: the memory-bound kernels fill every SM (8 CTAs of 256
+// threads), as the host path's one-block-per-item launches do.
 namespace {
 
 #define DK_GTRY(x)                          \
@@ -2866,12 +2889,12 @@ cudaError_t build_wave_graph(const WaveGraphArgs& a, cudaStream_t cs, cudaGraph_
     DK_GTRY(add_while(g, {}, &h_lvl, &n_lvl, &body));
     DK_GTRY(begin_segment(cs, body, {}));
     k_g_level_begin<<<1, 32, 0, cs>>>(a.lc, a.wc);
-    k_g_classify<<<2 * S, 256, 0, cs>>>(a.nodes, a.finals, a.bigs, a.lc, a.bin_cap,
+    k_g_classify<<<4 * S, 256, 0, cs>>>(a.nodes, a.finals, a.bigs, a.lc, a.bin_cap,
                                         a.split_target, a.big_ok, a.wc);
     k_g_plan<<<1, 32, 0, cs>>>(a.lc, a.wc, h_lvl);
-    k_g_assign<<<2 * S, 256, 0, cs>>>(a.nodes, a.tiles, a.lc, a.wc);
-    k_g_tile_hist<<<4 * S, 256, 0, cs>>>(a.nodes, a.tiles, a.A, a.B, a.TH, a.wc);
-    k_g_node_scan<<<2 * S, 512, 0, cs>>>(a.nodes, a.tiles, a.TH, a.wc);
+    k_g_assign<<<4 * S, 256, 0, cs>>>(a.nodes, a.tiles, a.lc, a.wc);
+    k_g_tile_hist<<<8 * S, 256, 0, cs>>>(a.nodes, a.tiles, a.A, a.B, a.TH, a.wc);
+    k_g_node_scan<<<4 * S, 256, 0, cs>>>(a.nodes, a.tiles, a.TH, a.wc);
     k_g_tile_scatter<<<DK_TILE_CTAS * S, kTileThreads, scatter_smem, cs>>>(a.nodes, a.tiles, a.A,
                                                                           a.B, a.TH, a.wc);
     std::vector<cudaGraphNode_t> leaves;
@@ -2896,7 +2919,7 @@ cudaError_t build_wave_graph(const WaveGraphArgs& a, cudaStream_t cs, cudaGraph_
     DK_GTRY(add_while(g, leaves, &h_up, &n_up, &body));
     DK_GTRY(begin_segment(cs, body, {}));
     k_g_pass_step<<<1, 32, 0, cs>>>(a.wc, h_up, 1);
-    k_g_aggregate<<<S, 256, 0, cs>>>(a.nodes, a.wc);
+    k_g_aggregate<<<8 * S, 256, 0, cs>>>(a.nodes, a.wc);
     DK_GTRY(end_segment(cs, body, &leaves));
     // level-1 offsets, then offsets down the tree
     DK_GTRY(begin_segment(cs, g, {n_up}));
@@ -2906,13 +2929,14 @@ cudaError_t build_wave_graph(const WaveGraphArgs& a, cudaStream_t cs, cudaGraph_
     DK_GTRY(add_while(g, leaves, &h_down, &n_down, &body));
     DK_GTRY(begin_segment(cs, body, {}));
     k_g_pass_step<<<1, 32, 0, cs>>>(a.wc, h_down, 0);
-    k_g_child_offsets<<<2 * S, 256, 0, cs>>>(a.nodes, a.wc);
+    k_g_child_offsets<<<8 * S, 256, 0, cs>>>(a.nodes, a.wc);
     DK_GTRY(end_segment(cs, body, &leaves));
     // the bins' pairs into the table
     DK_GTRY(begin_segment(cs, g, {n_down}));
-    k_g_compact<<<4 * S, 256, 0, cs>>>(a.nodes, a.finals, n_final, a.A, a.B, a.C, a.out_k,
-                                       a.out_c);
-    k_g_compact<<<4 * S, 256, 0, cs>>>(a.nodes, a.bigs, n_big, a.A, a.B, a.C, a.out_k, a.out_c);
+    k_g_compact<<<8 * S, 256, 0, cs>>>(a.nodes, a.finals, n_final, &a.wc->tk_compact[0], a.A,
+                                       a.B, a.C, a.out_k, a.out_c);
+    k_g_compact<<<8 * S, 256, 0, cs>>>(a.nodes, a.bigs, n_big, &a.wc->tk_compact[1], a.A, a.B,
+                                       a.C, a.out_k, a.out_c);
     DK_GTRY(end_segment(cs, g, &leaves));
     return cudaGetLastError();
   }();
