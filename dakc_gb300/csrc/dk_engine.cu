@@ -280,8 +280,30 @@ int Engine::acquire_table(uint64_t n, bool on_device, TableBuf** out) {
     // over), so that tables of varying sizes -- batches of different jobs --
     // reuse pooled buffers instead of pinning or allocating new ones
     t.cap = size_class(std::max<uint64_t>(n, 1));
+    if (on_device && budget && dev_bytes + t.cap * 12 > budget) {
+      // pooled tables nobody holds give their memory back, largest first,
+      // until the new one fits.  Entries stay (emptied, capacity 0): callers
+      // hold pointers into the deque, so nothing is erased
+      std::vector<TableBuf*> idle;
+      for (auto& x : tables)
+        if (!x.in_use && x.cap) idle.push_back(&x);
+      std::sort(idle.begin(), idle.end(),
+                [](const TableBuf* a, const TableBuf* b) { return a->cap > b->cap; });
+      for (TableBuf* x : idle) {
+        if (dev_bytes + t.cap * 12 <= budget) break;
+        cudaFree(x->k);
+        cudaFree(x->c);
+        dev_bytes -= x->cap * 12;
+        x->k = nullptr;
+        x->c = nullptr;
+        x->cap = 0;
+      }
+    }
     if (on_device) {
-      if (budget && dev_bytes + t.cap * 12 > budget) return DK_ERR_ADMISSION;
+      if (budget && dev_bytes + t.cap * 12 > budget) {
+        set_error("a device table does not fit the memory budget");
+        return DK_ERR_ADMISSION;
+      }
       if (cudaMalloc(&t.k, t.cap * 8) != cudaSuccess || cudaMalloc(&t.c, t.cap * 4) != cudaSuccess) {
         cudaGetLastError();
         if (t.k) cudaFree(t.k);
@@ -298,8 +320,19 @@ int Engine::acquire_table(uint64_t n, bool on_device, TableBuf** out) {
       }
     }
     t.id = ++g_table_ids;
-    tables.push_back(t);
-    best = &tables.back();
+    TableBuf* slot = nullptr;  // an emptied entry, else a new one
+    for (auto& x : tables)
+      if (!x.in_use && !x.cap && x.on_device == on_device) {
+        slot = &x;
+        break;
+      }
+    if (slot) {
+      *slot = t;
+      best = slot;
+    } else {
+      tables.push_back(t);
+      best = &tables.back();
+    }
   }
   best->in_use = true;
   best->refs = 1;
@@ -1259,8 +1292,6 @@ int Engine::wave_graph_tail(int F1, uint64_t n_kmers, int bin_target, bool use_h
   ga.A = (uint64_t*)keysA.p;
   ga.B = (uint64_t*)keysB.p;
   ga.C = (uint32_t*)cnt.p;
-  ga.out_k = out_k;
-  ga.out_c = out_c;
   ga.lc = (LevelCounters*)((char*)ctrs.p + 64);
   ga.ctr = c64;
   ga.wc = (WaveCtl*)((char*)ctrs.p + 256);
@@ -1288,6 +1319,8 @@ int Engine::wave_graph_tail(int F1, uint64_t n_kmers, int bin_target, bool use_h
   w.nodes_cap = (uint32_t)nodes_cap;
   w.tiles_cap = (uint32_t)tiles_cap;
   w.th_cap = th_cap;
+  w.out_k = out_k;
+  w.out_c = out_c;
   DK_CUDA(cudaMemcpyAsync(ga.wc, h_wc, sizeof(WaveCtl), cudaMemcpyHostToDevice, stream));
   DK_CUDA(cudaEventRecord(ev_stage[3], stream));
   {

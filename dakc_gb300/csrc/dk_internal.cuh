@@ -226,8 +226,12 @@ struct WaveCtl {
   // big-bin nodes of the compact (taken one at a time, so blocks that finish
   // early take more, as with a grid of one block per item)
   uint32_t tk_hist, tk_scatter, tk_compact[2];
+  // the wave's table (each wave has its own: read here, not built into the graph)
+  uint64_t* out_k;
+  uint32_t* out_c;
   uint32_t lv_lo[kGraphMaxLevels], lv_hi[kGraphMaxLevels];
 };
+static_assert(sizeof(WaveCtl) <= 256, "WaveCtl lives in the last 256 bytes of the counter block");
 
 // Fixed buffers and parameters a wave graph is built over.
 struct WaveGraphArgs {
@@ -240,8 +244,6 @@ struct WaveGraphArgs {
   uint64_t* A;
   uint64_t* B;
   uint32_t* C;
-  uint64_t* out_k;
-  uint32_t* out_c;
   LevelCounters* lc;
   unsigned long long* ctr;
   WaveCtl* wc;

@@ -2412,9 +2412,10 @@ __global__ void k_g_l1_offsets(Node* nodes, unsigned long long* total_d, const W
 // one warp per node, nodes taken by ticket (*tk)
 __global__ void k_g_compact(const Node* nodes, const uint32_t* __restrict__ finals,
                             const uint32_t* n_dev, uint32_t* tk, const uint64_t* A,
-                            const uint64_t* B, const uint32_t* C, uint64_t* __restrict__ out_k,
-                            uint32_t* __restrict__ out_c) {
+                            const uint64_t* B, const uint32_t* C, const WaveCtl* wc) {
   const uint32_t n = *n_dev;
+  uint64_t* __restrict__ out_k = wc->out_k;
+  uint32_t* __restrict__ out_c = wc->out_c;
   for (;;) {
     uint32_t w = 0;
     if (lane_id() == 0) w = atomicAdd(tk, 1u);
@@ -2934,9 +2935,9 @@ cudaError_t build_wave_graph(const WaveGraphArgs& a, cudaStream_t cs, cudaGraph_
     // the bins' pairs into the table
     DK_GTRY(begin_segment(cs, g, {n_down}));
     k_g_compact<<<8 * S, 256, 0, cs>>>(a.nodes, a.finals, n_final, &a.wc->tk_compact[0], a.A,
-                                       a.B, a.C, a.out_k, a.out_c);
+                                       a.B, a.C, a.wc);
     k_g_compact<<<8 * S, 256, 0, cs>>>(a.nodes, a.bigs, n_big, &a.wc->tk_compact[1], a.A, a.B,
-                                       a.C, a.out_k, a.out_c);
+                                       a.C, a.wc);
     DK_GTRY(end_segment(cs, g, &leaves));
     return cudaGetLastError();
   }();
