@@ -2203,11 +2203,15 @@ __device__ __forceinline__ void compact_one(const Node* nodes, uint32_t ni, cons
                                             uint32_t* __restrict__ out_c) {
   const Node nd = nodes[ni];
   if (nd.state != NODE_FINAL) return;  // re-partitioned after its bin count failed
-  const uint64_t* sk = (nd.buf ? B : A) + nd.start;
-  const uint32_t* sc = C + nd.start;
+  const uint64_t* __restrict__ sk = (nd.buf ? B : A) + nd.start;
+  const uint32_t* __restrict__ sc = C + nd.start;
+  // both loads of a pair are issued before its stores (read-only path: the
+  // staged pairs were written by an earlier kernel)
   for (uint64_t i = lane_id(); i < nd.d; i += 32) {
-    out_k[nd.out_off + i] = sk[i];
-    out_c[nd.out_off + i] = sc[i];
+    const uint64_t kv = __ldg(sk + i);
+    const uint32_t cv = __ldg(sc + i);
+    out_k[nd.out_off + i] = kv;
+    out_c[nd.out_off + i] = cv;
   }
 }
 
