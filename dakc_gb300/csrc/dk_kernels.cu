@@ -1765,10 +1765,13 @@ static_assert(kPackSlots % (2 * kPackThreads) == 0, "slot loops");
 // Insert one key (rk = key << (64 - s)) with multiplicity mult: 2 when it is
 // new, 1 when it was there, 0 when the probe runs past kPackMaxProbe slots or
 // (cmax != 0: a narrow count field of at most cmax) its count would not fit.
+// kNarrow: the count field may carry (s > kPackWideShift); the wide form
+// skips those checks (C2: bin count 21.30 -> 21.14 ms)
+template <bool kNarrow>
 __device__ __forceinline__ int pack_insert(unsigned long long* tab, unsigned long long rk,
                                            unsigned long long himask, uint32_t mult,
                                            uint32_t* hist, int dsh, uint32_t cmax) {
-  if (cmax && mult > cmax) return 0;
+  if (kNarrow && mult > cmax) return 0;
   const uint32_t h = ((uint32_t)(rk >> 32) ^ (uint32_t)rk) * 0x9E3779B1u;
   uint32_t slot = __umulhi(h, kPackSlots);  // h scaled to [0, kPackSlots)
   for (uint32_t probe = 0; probe < kPackMaxProbe; ++probe) {
@@ -1791,7 +1794,7 @@ __device__ __forceinline__ int pack_insert(unsigned long long* tab, unsigned lon
     }
     if ((e & himask) == rk) {
       unsigned int* lo = reinterpret_cast<unsigned int*>(&tab[slot]);  // the low word
-      if (!cmax) {
+      if (!kNarrow) {
         atomicAdd(lo, mult);
         return 1;
       }
@@ -1879,7 +1882,8 @@ __device__ bool bin_packed(Node* nodes, uint32_t ni, const Node& nd, uint64_t* k
         mult = (uint32_t)__popc(peers);
       }
       if (live && ok) {
-        const int r = pack_insert(tab, rk, himask, mult, hist, dsh, cmax);
+        const int r = cmax ? pack_insert<true>(tab, rk, himask, mult, hist, dsh, cmax)
+                           : pack_insert<false>(tab, rk, himask, mult, hist, dsh, cmax);
         ok = r != 0;
         fresh += r == 2;
       }
