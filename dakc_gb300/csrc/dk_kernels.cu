@@ -1114,13 +1114,26 @@ __device__ __forceinline__ void tile_scatter_one(const Node* nodes, const Tile* 
   }
 }
 
+// Pull tile t's keys into L2 (thread 0; nothing waits for it): with one
+// block per tile, blocks start in index order, so the block that takes tile
+// blockIdx + (resident blocks) starts about one tile's time later.
+__device__ __forceinline__ void prefetch_tile(const Node* nodes, const Tile* tiles, uint32_t t,
+                                              uint32_t n_tiles, const uint64_t* A,
+                                              const uint64_t* B) {
+  if (threadIdx.x != 0 || t >= n_tiles) return;
+  const Tile tl = tiles[t];
+  const Node& nd = nodes[tl.node];
+  prefetch_l2_range((nd.buf ? B : A) + tl.start, (uint64_t)tl.n * 8);
+}
+
 __global__ void __launch_bounds__(kTileThreads, DK_TILE_CTAS) k_tile_scatter(const Node* nodes,
                                                                   const Tile* tiles, uint64_t* A,
                                                                   uint64_t* B,
                                                                   const uint32_t* TH,
-                                                                  int max_width) {
+                                                                  int max_width, uint32_t ahead) {
   extern __shared__ __align__(16) unsigned long long dsm[];
   __shared__ uint32_t tmp[32];
+  prefetch_tile(nodes, tiles, blockIdx.x + ahead, gridDim.x, A, B);
   tile_scatter_one(nodes, tiles, blockIdx.x, A, B, TH, max_width, dsm, tmp);
 }
 
@@ -2763,7 +2776,14 @@ int launch_tile_scatter(const Node* nodes, const Tile* tiles, uint32_t n_tiles, 
   if (!n_tiles) return 0;
   const size_t smem = (size_t)kTileKeys * 8 + ((size_t)1 << max_width) * 16;
   allow_max_smem(k_tile_scatter);
-  k_tile_scatter<<<n_tiles, kTileThreads, smem, s>>>(nodes, tiles, A, B, TH, max_width);
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  // prefetch one resident wave ahead (large_100m: partition scatter 9.90 ->
+  // 9.33 ms; two waves ahead 10.07 ms; prefetching text tiles the same way
+  // slowed the level-1 count)
+  k_tile_scatter<<<n_tiles, kTileThreads, smem, s>>>(nodes, tiles, A, B, TH, max_width,
+                                                     (uint32_t)(DK_TILE_CTAS * sms));
   return 1;
 }
 
