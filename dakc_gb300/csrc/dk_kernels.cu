@@ -945,6 +945,18 @@ __device__ __forceinline__ uint32_t digit_of(uint64_t key, int shift, int width)
   return (uint32_t)(key >> (shift - width)) & ((1u << width) - 1u);
 }
 
+// Pull tile t's keys into L2 (thread 0; nothing waits for it): with one
+// block per tile, blocks start in index order, so the block that takes tile
+// blockIdx + (resident blocks) starts about one tile's time later.
+__device__ __forceinline__ void prefetch_tile(const Node* nodes, const Tile* tiles, uint32_t t,
+                                              uint32_t n_tiles, const uint64_t* A,
+                                              const uint64_t* B) {
+  if (threadIdx.x != 0 || t >= n_tiles) return;
+  const Tile tl = tiles[t];
+  const Node& nd = nodes[tl.node];
+  prefetch_l2_range((nd.buf ? B : A) + tl.start, (uint64_t)tl.n * 8);
+}
+
 // one tile's digit histogram (the whole block; hist: 2^kMaxSplitBits entries)
 __device__ __forceinline__ void tile_hist_one(const Node* nodes, const Tile* tiles, uint32_t t,
                                               const uint64_t* A, const uint64_t* B, uint32_t* TH,
@@ -1112,18 +1124,6 @@ __device__ __forceinline__ void tile_scatter_one(const Node* nodes, const Tile* 
     const uint32_t d = digit_of(key, sh, w);
     dst[gbase[d] + (i - loc[d])] = key;
   }
-}
-
-// Pull tile t's keys into L2 (thread 0; nothing waits for it): with one
-// block per tile, blocks start in index order, so the block that takes tile
-// blockIdx + (resident blocks) starts about one tile's time later.
-__device__ __forceinline__ void prefetch_tile(const Node* nodes, const Tile* tiles, uint32_t t,
-                                              uint32_t n_tiles, const uint64_t* A,
-                                              const uint64_t* B) {
-  if (threadIdx.x != 0 || t >= n_tiles) return;
-  const Tile tl = tiles[t];
-  const Node& nd = nodes[tl.node];
-  prefetch_l2_range((nd.buf ? B : A) + tl.start, (uint64_t)tl.n * 8);
 }
 
 __global__ void __launch_bounds__(kTileThreads, DK_TILE_CTAS) k_tile_scatter(const Node* nodes,
@@ -2780,8 +2780,9 @@ int launch_tile_scatter(const Node* nodes, const Tile* tiles, uint32_t n_tiles, 
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   // prefetch one resident wave ahead (large_100m: partition scatter 9.90 ->
-  // 9.33 ms; two waves ahead 10.07 ms; prefetching text tiles the same way
-  // slowed the level-1 count)
+  // 9.33 ms; two waves ahead 10.07 ms).  The same prefetch slowed the
+  // bandwidth-bound kernels: text tiles of the level-1 count, tiles of the
+  // partition histogram (2.94 -> 3.24 ms), bins of the compact (2.90 -> 3.68)
   k_tile_scatter<<<n_tiles, kTileThreads, smem, s>>>(nodes, tiles, A, B, TH, max_width,
                                                      (uint32_t)(DK_TILE_CTAS * sms));
   return 1;
