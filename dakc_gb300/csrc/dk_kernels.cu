@@ -347,16 +347,26 @@ __global__ void k_chunk_offsets_rows(const uint32_t* __restrict__ H, int G, int 
 // OR'ed into the shifted window ((key << 2) | code) and a k-mer ends at every
 // position from the k-th on (Sliding_window, pakman_star/src/
 // kmer_counting.cpp:313-341).
+// Roll modes: DAKC's convention for k >= 2, PakMan*'s convention, and DAKC's
+// for k = 1, whose last position follows the reference's last-run rule
+// (kcounter_funcs.cpp:102-110) and needs the previous code.  The k >= 2 form
+// carries neither that rule nor the previous code through its steps.
+enum : int { kRollDakc = 0, kRollPak = 1, kRollDakcK1 = 2 };
+
+__host__ __device__ constexpr int roll_mode(int conv, int k) {
+  return conv == 1 ? kRollPak : (k == 1 ? kRollDakcK1 : kRollDakc);
+}
+
 struct LineRoll {
   uint64_t key;
   int run;
   uint32_t prev;
   bool stopped;
   __device__ __forceinline__ void reset() { key = 0; run = 0; prev = 0; stopped = false; }
-  template <bool PAK = false>
+  template <int MODE>
   __device__ __forceinline__ bool step(uint32_t c, int p, int W, int k, uint64_t kmask) {
     if (stopped || c == 0xF0u) { stopped = true; return false; }
-    if (PAK) {
+    if (MODE == kRollPak) {
       key = ((key << 2) | c) & kmask;
       ++run;
       return run >= k;
@@ -367,9 +377,10 @@ struct LineRoll {
     } else {
       key = ((key << 2) | c) & kmask;
       ++run;
-      emit = run >= k && !(k == 1 && p == W - 1 && (W == 1 || prev == 0xFFu));
+      emit = run >= k;
+      if (MODE == kRollDakcK1) emit = emit && !(p == W - 1 && (W == 1 || prev == 0xFFu));
     }
-    prev = c;
+    if (MODE == kRollDakcK1) prev = c;
     return emit;
   }
 };
@@ -413,7 +424,7 @@ __device__ __forceinline__ void setup_tiles(TextTiles* T, const ExtractArgs& a, 
 }
 
 // COUNT: per-CTA bucket histogram H[cta][bucket] and the k-mer total.
-template <bool PAK>
+template <int MODE>
 __global__ void __launch_bounds__(kCountThreads) k_l1_lines_count(ExtractArgs a,
                                                                  uint32_t* __restrict__ H,
                                                                  unsigned long long* __restrict__ counters) {
@@ -451,7 +462,7 @@ __global__ void __launch_bounds__(kCountThreads) k_l1_lines_count(ExtractArgs a,
         for (int u = 0; u < 8; ++u) c8[u] = p0 + u < W ? lut[line[p0 + u]] : 0xF0u;
 #pragma unroll
         for (int u = 0; u < 8; ++u)
-          if (r.template step<PAK>(c8[u], p0 + u, W, k, a.kmask)) {
+          if (r.template step<MODE>(c8[u], p0 + u, W, k, a.kmask)) {
             atomicAdd(&cnt[a.njobs ? jb(r.key) : (uint32_t)(r.key >> a.shift1)], 1u);
             ++mine;
           }
@@ -481,7 +492,7 @@ __global__ void __launch_bounds__(kCountThreads) k_l1_lines_count(ExtractArgs a,
 // keeps shared memory at two CTAs per SM.  A chunk's codes are read from the
 // tile once, with independent loads, into registers (4 per word); both rolls
 // step through them unrolled.
-template <bool PAK, int CH>
+template <int MODE, int CH>
 __global__ void __launch_bounds__(kLineThreads, 2) k_l1_lines_chunked(ExtractArgs a,
                                                                      const uint64_t* __restrict__ O,
                                                                      uint64_t* __restrict__ keys_out,
@@ -535,7 +546,7 @@ __global__ void __launch_bounds__(kLineThreads, 2) k_l1_lines_chunked(ExtractArg
       for (int u = 0; u < 4; ++u) c4[u] = live && p0 + u < warm ? lut[line[p0 + u]] : 0xF0u;
 #pragma unroll
       for (int u = 0; u < 4; ++u)
-        if (p0 + u < warm) r.template step<PAK>(c4[u], p0 + u, W, k, a.kmask);
+        if (p0 + u < warm) r.template step<MODE>(c4[u], p0 + u, W, k, a.kmask);
     }
     for (int p0 = warm; p0 < W; p0 += chunk) {  // uniform over the block
       const int np = min(W - p0, chunk);        // positions of this chunk (uniform)
@@ -555,7 +566,7 @@ __global__ void __launch_bounds__(kLineThreads, 2) k_l1_lines_chunked(ExtractArg
       const LineRoll r0 = r;
 #pragma unroll
       for (int q = 0; q < CH; ++q)
-        if (q < np && r.template step<PAK>((cw[q >> 2] >> (8 * (q & 3))) & 0xFFu, p0 + q, W, k,
+        if (q < np && r.template step<MODE>((cw[q >> 2] >> (8 * (q & 3))) & 0xFFu, p0 + q, W, k,
                                            a.kmask))
           atomicAdd(&ccount[(uint32_t)(r.key >> a.shift1)], 1u);
       __syncthreads();
@@ -570,7 +581,7 @@ __global__ void __launch_bounds__(kLineThreads, 2) k_l1_lines_chunked(ExtractArg
       r = r0;
 #pragma unroll
       for (int q = 0; q < CH; ++q)
-        if (q < np && r.template step<PAK>((cw[q >> 2] >> (8 * (q & 3))) & 0xFFu, p0 + q, W, k,
+        if (q < np && r.template step<MODE>((cw[q >> 2] >> (8 * (q & 3))) & 0xFFu, p0 + q, W, k,
                                            a.kmask)) {
           const uint32_t b = (uint32_t)(r.key >> a.shift1);
           const uint32_t pos = coff[b] + atomicAdd(&ccount[b], 1u);
@@ -598,7 +609,7 @@ __global__ void __launch_bounds__(kLineThreads, 2) k_l1_lines_chunked(ExtractArg
 // key per bucket and staging would not lengthen the runs; writing directly
 // keeps shared memory small (text tiles and cursors only).  Consecutive keys
 // of a bucket land next to each other, so L2 merges the 8-byte stores.
-template <bool PAK>
+template <int MODE>
 __global__ void __launch_bounds__(kLineThreads) k_l1_lines_direct(ExtractArgs a,
                                                                   const uint64_t* __restrict__ O,
                                                                   uint64_t* __restrict__ keys_out,
@@ -643,7 +654,7 @@ __global__ void __launch_bounds__(kLineThreads) k_l1_lines_direct(ExtractArgs a,
         for (int u = 0; u < 4; ++u) c4[u] = p0 + u < W ? lut[line[p0 + u]] : 0xF0u;
 #pragma unroll
         for (int u = 0; u < 4; ++u)
-          if (r.template step<PAK>(c4[u], p0 + u, W, k, a.kmask)) {
+          if (r.template step<MODE>(c4[u], p0 + u, W, k, a.kmask)) {
             const uint32_t b = a.njobs ? jb(r.key) : (uint32_t)(r.key >> a.shift1);
             keys_out[cursor[b] + atomicAdd(&cnt[b], 1u)] = r.key;
           }
@@ -2618,7 +2629,10 @@ static int chunk_positions(const ExtractArgs& a) {
 int launch_l1_count(const ExtractArgs& a, int grid, uint32_t* H, unsigned long long* counters,
                     cudaStream_t s) {
   if (a.W <= kLineMaxW) {
-    auto* kern = a.conv == 1 ? k_l1_lines_count<true> : k_l1_lines_count<false>;
+    const int m = roll_mode(a.conv, a.k);
+    auto* kern = m == kRollPak ? k_l1_lines_count<kRollPak>
+                               : (m == kRollDakcK1 ? k_l1_lines_count<kRollDakcK1>
+                                                   : k_l1_lines_count<kRollDakc>);
     allow_max_smem(kern);
     kern<<<grid, kCountThreads, count_lines_smem(a), s>>>(a, H, counters);
     return 1;
@@ -2703,17 +2717,24 @@ int launch_l1_scatter(const ExtractArgs& a, int grid, const uint64_t* O, uint64_
                       unsigned long long* counters, cudaStream_t s) {
   if (chunked_scatter(a)) {
     const int chunk = chunk_positions(a);
-    auto* kern = chunk == 2 * kLineChunk
-                     ? (a.conv == 1 ? k_l1_lines_chunked<true, 2 * kLineChunk>
-                                    : k_l1_lines_chunked<false, 2 * kLineChunk>)
-                     : (a.conv == 1 ? k_l1_lines_chunked<true, kLineChunk>
-                                    : k_l1_lines_chunked<false, kLineChunk>);
+    const int m = roll_mode(a.conv, a.k);
+    auto* kern =
+        chunk == 2 * kLineChunk
+            ? (m == kRollPak ? k_l1_lines_chunked<kRollPak, 2 * kLineChunk>
+                             : (m == kRollDakcK1 ? k_l1_lines_chunked<kRollDakcK1, 2 * kLineChunk>
+                                                 : k_l1_lines_chunked<kRollDakc, 2 * kLineChunk>))
+            : (m == kRollPak ? k_l1_lines_chunked<kRollPak, kLineChunk>
+                             : (m == kRollDakcK1 ? k_l1_lines_chunked<kRollDakcK1, kLineChunk>
+                                                 : k_l1_lines_chunked<kRollDakc, kLineChunk>));
     allow_max_smem(kern);
     kern<<<grid, kLineThreads, chunked_smem(a, chunk), s>>>(a, O, keys, counters);
     return 1;
   }
   if (direct_scatter(a.W, a.njobs != 0)) {
-    auto* kern = a.conv == 1 ? k_l1_lines_direct<true> : k_l1_lines_direct<false>;
+    const int m = roll_mode(a.conv, a.k);
+    auto* kern = m == kRollPak ? k_l1_lines_direct<kRollPak>
+                               : (m == kRollDakcK1 ? k_l1_lines_direct<kRollDakcK1>
+                                                   : k_l1_lines_direct<kRollDakc>);
     allow_max_smem(kern);
     kern<<<grid, kLineThreads, lines_smem(a, true), s>>>(a, O, keys, counters);
     return 1;
