@@ -385,6 +385,85 @@ struct LineRoll {
   }
 };
 
+// k-mer windows of a line a chunk of positions at a time (DAKC's convention,
+// k >= 2), with no step depending on the one before: the 2-bit codes of the
+// 32 positions before the chunk (P) and their break bits (B) carry from chunk
+// to chunk; the k-mer ending at chunk position q is a fixed bit field of
+// P:C (C: the chunk's codes), and it is counted when no break lies in its
+// window (B:Bc smeared over k positions) and no stop came before it.
+// Codes: 0-3 bases, 0xFF break, 0xF0 stop (bit 7 marks both; bit 0 tells
+// them apart).  Emits exactly what LineRoll::step<kRollDakc> emits.
+__device__ __forceinline__ uint32_t pack4_codes(uint32_t w) {  // first code in bits 7..6
+  const uint32_t x = w & 0x03030303u;
+  return ((x & 3u) << 6) | ((x >> 4) & 0x30u) | ((x >> 14) & 0x0Cu) | (x >> 24);
+}
+__device__ __forceinline__ uint32_t byte_flags4(uint32_t m) {  // bit 7 of byte u -> bit u
+  return ((((m >> 7) & 0x01010101u) * 0x00204081u) >> 21) & 0xFu;
+}
+struct LineWin {
+  uint64_t P;    // codes of positions p0-32 .. p0-1, position p0-1 in bits 1..0
+  uint32_t B;    // their break bits, bit i: position p0-32+i (before the line: set)
+  bool stopped;  // a stop came before p0
+  // pack a chunk of CH codes (cw: byte u of word g is position 4g+u)
+  template <int CH>
+  __device__ __forceinline__ static void pack(const uint32_t* cw, uint64_t* C, uint32_t* brk,
+                                              uint32_t* stp) {
+    uint64_t c = 0;
+    uint32_t b = 0, t = 0;
+#pragma unroll
+    for (int g = 0; g < CH / 4; ++g) {
+      const uint32_t w = cw[g];
+      c |= (uint64_t)pack4_codes(w) << (2 * CH - 8 - 8 * g);
+      b |= byte_flags4(w & 0x80808080u) << (4 * g);
+      t |= byte_flags4(w & ~(w << 7) & 0x80808080u) << (4 * g);
+    }
+    *C = c;
+    *brk = b;
+    *stp = t;
+  }
+  // the 32 positions before the first chunk (iw: codes of positions
+  // p0-32 .. p0-1, breaks before the line)
+  __device__ __forceinline__ void init(const uint32_t* iw) {
+    uint32_t t;
+    pack<32>(iw, &P, &B, &t);
+    stopped = t != 0;
+  }
+  // emit mask of a chunk (bit q: the k-mer ending at p0+q); *M keeps the
+  // combined break bits for advance()
+  template <int CH>
+  __device__ __forceinline__ uint32_t valid(uint32_t brk, uint32_t stp, int k,
+                                            uint64_t* M) const {
+    const uint64_t m = ((uint64_t)brk << 32) | B;
+    uint64_t sm = m;  // bit i: a break among positions i-k+1 .. i
+    int w = 1;
+    while (2 * w <= k) {
+      sm |= sm << w;
+      w <<= 1;
+    }
+    if (w < k) sm |= sm << (k - w);
+    uint32_t v = ~(uint32_t)(sm >> 32);
+    if (CH < 32) v &= (1u << CH) - 1u;
+    if (stopped) v = 0;
+    if (stp) v &= (1u << (__ffs(stp) - 1)) - 1u;
+    *M = m;
+    return v;
+  }
+  template <int CH>
+  __device__ __forceinline__ uint64_t key(uint64_t C, int q, uint64_t kmask) const {
+    const int s = 2 * (CH - 1 - q);  // a constant once q's loop is unrolled
+    const uint64_t lo = CH == 32 ? C : ((P << (2 * CH)) | C);
+    const uint64_t hi = CH == 32 ? P : (P >> (64 - 2 * CH));
+    const uint64_t x = s == 0 ? lo : ((lo >> s) | (hi << (64 - s)));
+    return x & kmask;
+  }
+  template <int CH>
+  __device__ __forceinline__ void advance(uint64_t C, uint64_t M, uint32_t stp) {
+    P = CH == 32 ? C : ((P << (2 * CH)) | C);
+    B = (uint32_t)(M >> CH);
+    stopped = stopped || stp != 0;
+  }
+};
+
 // Per-line prologue of a tile: is line l parsed, and its bucket rule (batch
 // mode); records NUL-led lines.
 __device__ __forceinline__ bool line_prologue(const ExtractArgs& a, uint64_t l, uint64_t l1,
@@ -540,13 +619,30 @@ __global__ void __launch_bounds__(kLineThreads, 2) k_l1_lines_chunked(ExtractArg
     if (!live) r.stopped = true;
     // warm-up: positions before the first possible k-mer end emit nothing
     const int warm = min(k - 1, W);
-    for (int p0 = 0; p0 < warm; p0 += 4) {
-      uint32_t c4[4];
+    LineWin win;
+    if (MODE == kRollDakc) {
+      // the window of the 32 positions before the first chunk
+      uint32_t iw[8];
 #pragma unroll
-      for (int u = 0; u < 4; ++u) c4[u] = live && p0 + u < warm ? lut[line[p0 + u]] : 0xF0u;
+      for (int g = 0; g < 8; ++g) {
+        uint32_t w = 0;
 #pragma unroll
-      for (int u = 0; u < 4; ++u)
-        if (p0 + u < warm) r.template step<MODE>(c4[u], p0 + u, W, k, a.kmask);
+        for (int u = 0; u < 4; ++u) {
+          const int p = warm - 32 + g * 4 + u;
+          w |= (p < 0 ? 0xFFu : (live ? (uint32_t)lut[line[p]] : 0xF0u)) << (8 * u);
+        }
+        iw[g] = w;
+      }
+      win.init(iw);
+    } else {
+      for (int p0 = 0; p0 < warm; p0 += 4) {
+        uint32_t c4[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) c4[u] = live && p0 + u < warm ? lut[line[p0 + u]] : 0xF0u;
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+          if (p0 + u < warm) r.template step<MODE>(c4[u], p0 + u, W, k, a.kmask);
+      }
     }
     for (int p0 = warm; p0 < W; p0 += chunk) {  // uniform over the block
       const int np = min(W - p0, chunk);        // positions of this chunk (uniform)
@@ -564,11 +660,23 @@ __global__ void __launch_bounds__(kLineThreads, 2) k_l1_lines_chunked(ExtractArg
         cw[g] = w;
       }
       const LineRoll r0 = r;
+      uint64_t wc = 0, wm = 0;  // window path: the chunk's codes and break bits
+      uint32_t wv = 0, wstp = 0;
+      if (MODE == kRollDakc) {
+        uint32_t brk;
+        LineWin::pack<CH>(cw, &wc, &brk, &wstp);
+        wv = win.valid<CH>(brk, wstp, k, &wm);
 #pragma unroll
-      for (int q = 0; q < CH; ++q)
-        if (q < np && r.template step<MODE>((cw[q >> 2] >> (8 * (q & 3))) & 0xFFu, p0 + q, W, k,
-                                           a.kmask))
-          atomicAdd(&ccount[(uint32_t)(r.key >> a.shift1)], 1u);
+        for (int q = 0; q < CH; ++q)
+          if ((wv >> q) & 1u)
+            atomicAdd(&ccount[(uint32_t)(win.key<CH>(wc, q, a.kmask) >> a.shift1)], 1u);
+      } else {
+#pragma unroll
+        for (int q = 0; q < CH; ++q)
+          if (q < np && r.template step<MODE>((cw[q >> 2] >> (8 * (q & 3))) & 0xFFu, p0 + q, W, k,
+                                             a.kmask))
+            atomicAdd(&ccount[(uint32_t)(r.key >> a.shift1)], 1u);
+      }
       __syncthreads();
       for (int b = threadIdx.x; b < F1; b += blockDim.x) {
         coff[b] = ccount[b];
@@ -578,15 +686,27 @@ __global__ void __launch_bounds__(kLineThreads, 2) k_l1_lines_chunked(ExtractArg
       }
       __syncthreads();
       const uint32_t Tn = block_scan_array<uint32_t>(coff, F1, tmp);
-      r = r0;
+      if (MODE == kRollDakc) {
 #pragma unroll
-      for (int q = 0; q < CH; ++q)
-        if (q < np && r.template step<MODE>((cw[q >> 2] >> (8 * (q & 3))) & 0xFFu, p0 + q, W, k,
-                                           a.kmask)) {
-          const uint32_t b = (uint32_t)(r.key >> a.shift1);
-          const uint32_t pos = coff[b] + atomicAdd(&ccount[b], 1u);
-          if (DK_OK_IDX(pos < (uint32_t)blockDim.x * chunk, 41, pos)) stage[pos] = r.key;
-        }
+        for (int q = 0; q < CH; ++q)
+          if ((wv >> q) & 1u) {
+            const uint64_t key = win.key<CH>(wc, q, a.kmask);
+            const uint32_t b = (uint32_t)(key >> a.shift1);
+            const uint32_t pos = coff[b] + atomicAdd(&ccount[b], 1u);
+            if (DK_OK_IDX(pos < (uint32_t)blockDim.x * chunk, 41, pos)) stage[pos] = key;
+          }
+        win.advance<CH>(wc, wm, wstp);
+      } else {
+        r = r0;
+#pragma unroll
+        for (int q = 0; q < CH; ++q)
+          if (q < np && r.template step<MODE>((cw[q >> 2] >> (8 * (q & 3))) & 0xFFu, p0 + q, W, k,
+                                             a.kmask)) {
+            const uint32_t b = (uint32_t)(r.key >> a.shift1);
+            const uint32_t pos = coff[b] + atomicAdd(&ccount[b], 1u);
+            if (DK_OK_IDX(pos < (uint32_t)blockDim.x * chunk, 41, pos)) stage[pos] = r.key;
+          }
+      }
       __syncthreads();
       for (uint32_t i = threadIdx.x; i < Tn; i += blockDim.x) {
         const uint64_t key = stage[i];
