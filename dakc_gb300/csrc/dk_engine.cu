@@ -674,6 +674,7 @@ int Engine::count_batch(const dk_job* jobs, int njobs, const dk_input_desc* desc
   stats_batch.ms_device = ms_device;
   stats_batch.ms_h2d = ms_h2d;
   stats_batch.ms_d2h = ms_d2h;
+  stats_batch.dev_bytes_peak = dev_peak;
   stats_batch.kernel_launches = launches_total;
   stats_batch.ms_wall =
       std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - w0).count();
