@@ -649,15 +649,28 @@ __global__ void __launch_bounds__(kLineThreads, 2) k_l1_lines_chunked(ExtractArg
       uint32_t* ccount = cnt2 + (cur ? F1 : 0);  // this chunk's counts
       uint32_t* cprev = cnt2 + (cur ? 0 : F1);   // the previous chunk's
       uint32_t cw[CH / 4];  // the chunk's codes, byte q & 3 of word q >> 2
+      {
+        // the chunk's bytes through aligned 32-bit loads, 9 instead of 32 byte
+        // loads (large_100m: 9.56 -> 9.41 ms).  A few bytes past the line are
+        // read from the tile buffer's slack or the stage after it, and never
+        // used: positions past np are stops
+        const uintptr_t ad = reinterpret_cast<uintptr_t>(line + p0);
+        const uint32_t* wp = reinterpret_cast<const uint32_t*>(ad & ~(uintptr_t)3);
+        const uint32_t fs = (uint32_t)(ad & 3) * 8;
+        uint32_t tw[CH / 4 + 1];
 #pragma unroll
-      for (int g = 0; g < CH / 4; ++g) {
-        uint32_t w = 0;
+        for (int g = 0; g <= CH / 4; ++g) tw[g] = wp[g];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
-          const int q = g * 4 + u;
-          w |= (live && q < np ? (uint32_t)lut[line[p0 + q]] : 0xF0u) << (8 * u);
+        for (int g = 0; g < CH / 4; ++g) {
+          const uint32_t b4 = __funnelshift_r(tw[g], tw[g + 1], fs);
+          uint32_t w = 0;
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            const int q = g * 4 + u;
+            w |= (live && q < np ? (uint32_t)lut[(b4 >> (8 * u)) & 0xFFu] : 0xF0u) << (8 * u);
+          }
+          cw[g] = w;
         }
-        cw[g] = w;
       }
       const LineRoll r0 = r;
       uint64_t wc = 0, wm = 0;  // window path: the chunk's codes and break bits
