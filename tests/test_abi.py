@@ -91,3 +91,53 @@ def test_autotune_rejects_bad_arguments_without_a_device():
     tune = dk.Tune()
     assert lib.dk_autotune(None, None, 0, ctypes.byref(d), ctypes.byref(tune)) == dk.DK_ERR_INVALID_ARG
     assert lib.dk_autotune_reset(None) == dk.DK_ERR_INVALID_ARG
+
+
+def _c_struct_fields(name):
+    """(field, C type, array length) of `typedef struct {...} name;` in the header."""
+    src = re.sub(r"/\*.*?\*/", "", open(HEADER).read(), flags=re.S)
+    m = re.search(r"typedef struct \{([^{}]*)\}\s*" + name + r"\s*;", src)
+    assert m, name
+    out = []
+    for decl in m.group(1).split(";"):
+        decl = decl.strip()
+        if not decl:
+            continue
+        parts = decl.split(None, 1)
+        ctype, names = parts[0], parts[1]
+        for nm in names.split(","):
+            nm = nm.strip().lstrip("*")
+            a = re.match(r"(\w+)\s*\[(\d+)\]", nm)
+            out.append((a.group(1), ctype, int(a.group(2))) if a else (nm, ctype, 1))
+    return out
+
+
+_CTYPES = {"double": ctypes.c_double, "uint64_t": ctypes.c_uint64, "int": ctypes.c_int,
+           "uint32_t": ctypes.c_uint32}
+
+
+@pytest.mark.parametrize("cname,pystruct", [("dk_stats", dk.Stats), ("dk_config", dk.Config),
+                                             ("dk_input_desc", dk.InputDesc)])
+def test_python_structs_mirror_the_header(cname, pystruct):
+    """The ctypes mirrors match the header field by field (order, type, array
+    length), so a field added on one side only fails here, not as shifted
+    statistics on a GPU machine."""
+    cfields = _c_struct_fields(cname)
+    pyfields = pystruct._fields_
+    assert [f[0] for f in cfields] == [f[0] for f in pyfields]
+    for (name, ctype, n), (_, pytype) in zip(cfields, pyfields):
+        want = _CTYPES[ctype] * n if n > 1 else _CTYPES[ctype]
+        assert ctypes.sizeof(pytype) == ctypes.sizeof(want), name
+        if n > 1:
+            assert pytype._length_ == n and pytype._type_ == _CTYPES[ctype], name
+        else:
+            assert pytype == want, name
+
+
+def test_flags_match_the_header():
+    src = open(HEADER).read()
+    flags = dict((k, int(v)) for k, v in re.findall(r"#define (DK_FLAG_\w+) (\d+)ull", src))
+    assert flags == {"DK_FLAG_STREAM_ALL": dk.FLAG_STREAM_ALL,
+                     "DK_FLAG_STAGE_PAGEABLE": dk.FLAG_STAGE_PAGEABLE,
+                     "DK_FLAG_NO_GRAPH": dk.FLAG_NO_GRAPH,
+                     "DK_FLAG_GRAPH_MIN_BUFFERS": dk.FLAG_GRAPH_MIN_BUFFERS}
