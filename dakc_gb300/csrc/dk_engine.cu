@@ -685,22 +685,28 @@ int Engine::count_batch(const dk_job* jobs, int njobs, const dk_input_desc* desc
 // Copy host reads into device memory: one async copy when the buffer is
 // pinned, else through two pinned staging slots so host memcpy overlaps the
 // previous slot's DMA.
-// Every page of [p, p + n) is mapped in this process (mincore fails with
-// ENOMEM on an unmapped page).  The device reads pageable reads in place, so
-// a range the caller no longer owns (freed, unmapped) is refused here rather
-// than read by a kernel.
-static bool host_range_mapped(const void* p, uint64_t n) {
-  if (!n) return true;
+// Pages of [p, p + n): 0 if one is not mapped in this process (mincore fails
+// with ENOMEM), 1 if all are mapped and resident, 2 if all are mapped but some
+// are not resident (never touched, swapped out, a file not yet read).  The
+// device reads pageable reads in place only in case 1: a range the caller no
+// longer owns is refused rather than read by a kernel, and pages the CPU
+// would first have to fault in are staged through host threads instead.
+static int host_range_state(const void* p, uint64_t n) {
+  if (!n) return 1;
   const uint64_t pg = (uint64_t)sysconf(_SC_PAGESIZE);
   const uintptr_t a = reinterpret_cast<uintptr_t>(p) & ~(uintptr_t)(pg - 1);
   const uint64_t len = reinterpret_cast<uintptr_t>(p) + n - a;
   constexpr uint64_t kWin = 16384;  // pages per call
   unsigned char vec[kWin];
+  int state = 1;
   for (uint64_t off = 0; off < len; off += pg * kWin) {
     const uint64_t l = std::min<uint64_t>(len - off, pg * kWin);
-    if (mincore(reinterpret_cast<void*>(a + off), l, vec) != 0) return false;
+    if (mincore(reinterpret_cast<void*>(a + off), l, vec) != 0) return 0;
+    const uint64_t np = (l + pg - 1) / pg;
+    for (uint64_t i = 0; i < np && state == 1; ++i)
+      if (!(vec[i] & 1)) state = 2;
   }
-  return true;
+  return state;
 }
 
 static bool is_pinned(const void* h) {
@@ -728,35 +734,40 @@ static void gather_range(const std::vector<Engine::Seg>& segs, uint64_t dst_lo, 
 }
 
 // Host -> device copy of segments laid out at segs[i].doff in d.  Pinned
-// segments go straight to the DMA engine; runs of pageable segments (no pinned
-// segment between them) are packed into two 64 MB pinned slots by several host
-// threads while the other slot's DMA runs.  A slot copy covers only its run,
-// so it never overwrites a pinned segment's bytes; bytes inside a run that no
-// segment covers are missing final terminators, which are never examined.  A
-// slot is refilled only after the copy that last read it has finished.
+// segments go straight to the DMA engine, and pageable ones the device can
+// read in place (resident pages) are copied by a kernel.  Runs of the other
+// pageable segments (no DMA or in-place segment between them) are packed into
+// two 64 MB pinned slots by several host threads while the other slot's DMA
+// runs.  A slot copy covers only its run, so it never overwrites another
+// segment's bytes; bytes inside a run that no segment covers are missing
+// final terminators, which are never examined.  A slot is refilled only after
+// the copy that last read it has finished.
 int Engine::upload_segments(const std::vector<Seg>& all, uint8_t* d, cudaStream_t st) {
   Engine* e = this;
   struct S {
     Seg sg;
-    bool pinned;
+    bool staged;  // packed through the pinned slots by host threads
   };
   std::vector<S> v;
   for (const Seg& sg : all)
-    if (sg.n) v.push_back({sg, is_pinned(sg.h)});
+    if (sg.n) v.push_back({sg, false});
   std::sort(v.begin(), v.end(), [](const S& x, const S& y) { return x.sg.doff < y.sg.doff; });
   bool any_pageable = false;
-  for (const S& x : v) {
-    if (x.pinned) {
+  for (S& x : v) {
+    if (is_pinned(x.sg.h)) {
       DK_CUDA(cudaMemcpyAsync(d + x.sg.doff, x.sg.h, x.sg.n, cudaMemcpyHostToDevice, st));
-    } else if (host_direct) {
-      // the SMs read the pageable bytes in place
-      if (!host_range_mapped(x.sg.h, x.sg.n)) {
-        set_error("reads at an unmapped host address");
-        return DK_ERR_INVALID_ARG;
-      }
+      continue;
+    }
+    const int hs = host_direct ? host_range_state(x.sg.h, x.sg.n) : 2;
+    if (hs == 0) {
+      set_error("reads at an unmapped host address");
+      return DK_ERR_INVALID_ARG;
+    }
+    if (hs == 1) {  // resident pageable bytes: the SMs read them in place
       launch_copy_in(x.sg.h, d + x.sg.doff, x.sg.n, sm_count, st);
       DK_CUDA(cudaGetLastError());
     } else {
+      x.staged = true;
       any_pageable = true;
     }
   }
@@ -770,10 +781,10 @@ int Engine::upload_segments(const std::vector<Seg>& all, uint8_t* d, cudaStream_
   const int nthreads = (int)std::min<unsigned>(16, std::max(1u, hw - 1));
   size_t r0 = 0;
   while (r0 < v.size()) {
-    if (v[r0].pinned) { ++r0; continue; }
+    if (!v[r0].staged) { ++r0; continue; }
     size_t r1 = r0;
     std::vector<Seg> run;
-    while (r1 < v.size() && !v[r1].pinned) run.push_back(v[r1++].sg);
+    while (r1 < v.size() && v[r1].staged) run.push_back(v[r1++].sg);
     uint64_t lo = run.front().doff;
     const uint64_t end = run.back().doff + run.back().n;
     while (lo < end) {
@@ -1490,9 +1501,17 @@ int Engine::count_locked(const char* text, uint64_t nbytes, bool text_on_device,
     const int W = desc->line_width;
     const int64_t Lc = frame_lines(nbytes, W);
     const bool pinned = is_pinned(text);
-    in_place_up = !pinned && host_direct && nbytes > 0;
+    int hs = 1;  // pageable pages: 0 unmapped, 1 resident, 2 mapped but not all resident
+    if (!pinned && host_direct && nbytes) {
+      hs = host_range_state(text, nbytes);
+      if (hs == 0) {
+        set_error("reads at an unmapped host address");
+        return DK_ERR_INVALID_ARG;
+      }
+    }
+    in_place_up = !pinned && host_direct && nbytes > 0 && hs == 1;
     if (nbytes >= kChunkMinBytes && W <= kLineMaxW && Lc >= 64 * kMaxChunks &&
-        (pinned || host_direct)) {
+        (pinned || in_place_up)) {
       // chunks of lines on s_in (after earlier work on the text buffer); the
       // level-1 count of each runs as soon as it has landed.  Page-locked
       // chunks go to the DMA engine, pageable ones are read in place by a
@@ -1512,14 +1531,7 @@ int Engine::count_locked(const char* text, uint64_t nbytes, bool text_on_device,
           DK_CUDA(cudaMemcpyAsync((uint8_t*)this->text.p + b0, text + b0, b1 - b0,
                                   cudaMemcpyHostToDevice, s_in));
         if (b1 > b0 && !dma) {
-          // the chunks launched so far read mapped memory: they finish
-          // before the call returns
-          if (!host_range_mapped(text + b0, b1 - b0)) {
-            cudaStreamSynchronize(s_in);
-            chunks.n = 0;
-            set_error("reads at an unmapped host address");
-            return DK_ERR_INVALID_ARG;
-          }
+          // (the whole range was checked above: mapped and resident)
           launch_copy_in(text + b0, (uint8_t*)this->text.p + b0, b1 - b0, sm_count, s_in);
           DK_CUDA(cudaGetLastError());
         }

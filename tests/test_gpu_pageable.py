@@ -140,3 +140,31 @@ def test_unmapped_reads_are_refused(engine):
     keys, counts, nk = pyoracle.count(check_text, 150, 31)
     assert got.n_kmers == nk and np.array_equal(got.kmers, keys)
     assert np.array_equal(got.counts, counts)
+
+
+def test_mapped_but_not_resident_reads_are_staged(engine):
+    """Pageable reads whose pages are mapped but not all resident (here: an
+    anonymous mapping whose second half was never touched) are staged through
+    host threads, not read in place; the untouched half reads as zeros, so
+    the read set ends at its first NUL-led line, as in the reference."""
+    import ctypes
+    import mmap
+    W, n_lines = 150, 4000
+    text = synth.random_lines(601, n_lines, W)
+    half = (n_lines // 2) * (W + 1)
+    buf = mmap.mmap(-1, text.size)            # untouched pages are not resident
+    buf[:half] = text[:half].tobytes()
+    view = ctypes.c_char.from_buffer(buf)     # keeps the mapping exported while in use
+    t = engine.count_raw(ctypes.addressof(view), text.size, dk.Engine.desc(W, 31))
+    try:
+        n = int(t.n)
+        keys = np.ctypeslib.as_array(t.kmers, shape=(n,)).copy()
+        counts = np.ctypeslib.as_array(t.counts, shape=(n,)).copy()
+        nk = int(t.n_kmers)
+    finally:
+        engine.free_table(t)
+    assert engine.stats()["upload_in_place"] == 0
+    ref = pyoracle.count(text[:half], W, 31)
+    assert nk == ref[2] and np.array_equal(keys, ref[0]) and np.array_equal(counts, ref[1])
+    del view
+    buf.close()
