@@ -3,6 +3,8 @@
 * ``_build/libdakc_gb300.so`` -- the engine: sm_103a kernels + C++ host
   pipeline + C ABI (include/dakc_gb300.h), compiled by nvcc for
   ``-gencode arch=compute_103a,code=sm_103a`` only.
+* ``_build/dakc-gpu`` -- the command-line counter (host C++ over the C ABI,
+  linked against the engine library beside it).
 * ``synth/_build/libdk_synth.so`` -- the seeded workload generator (host C++).
 
 Translation units compile in parallel; a rebuild is skipped when the library
@@ -21,6 +23,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 ENGINE_SO = os.path.join(BUILD, "libdakc_gb300.so")
+CLI = os.path.join(BUILD, "dakc-gpu")
 SYNTH_SO = os.path.join(HERE, "synth", "_build", "libdk_synth.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
@@ -40,7 +43,7 @@ def _stale(target: str, sources: list[str]) -> bool:
 
 
 def build_engine(force: bool = False, verbose: bool = False) -> str:
-    units = sorted(glob.glob(os.path.join(CSRC, "*.cu")))
+    units = sorted(glob.glob(os.path.join(CSRC, "*.cu")))  # the engine: every .cu file
     deps = units + glob.glob(os.path.join(CSRC, "*.cuh")) + glob.glob(os.path.join(CSRC, "*.hpp")) + \
         [os.path.join(ROOT, "include", "dakc_gb300.h")]
     if not force and not _stale(ENGINE_SO, deps):
@@ -83,9 +86,26 @@ def build_synth(force: bool = False) -> str:
     return SYNTH_SO
 
 
+def build_cli(force: bool = False) -> str:
+    """The command-line counter; it finds the engine library beside itself."""
+    src = os.path.join(CSRC, "dk_cli.cpp")
+    header = os.path.join(ROOT, "include", "dakc_gb300.h")
+    if not force and not _stale(CLI, [src, header, ENGINE_SO]):
+        return CLI
+    tmp = CLI + ".tmp"
+    cmd = ["g++", "-O2", "-std=c++17", "-Wall", "-I", os.path.join(ROOT, "include"), "-o", tmp, src,
+           "-L", BUILD, "-ldakc_gb300", "-Wl,-rpath,$ORIGIN"]
+    p = subprocess.run(cmd, capture_output=True, text=True)
+    if p.returncode != 0:
+        raise RuntimeError(f"g++ failed: {' '.join(cmd)}\n{p.stdout}{p.stderr}")
+    os.replace(tmp, CLI)
+    return CLI
+
+
 def build_all(force: bool = False) -> None:
     build_synth(force)
     build_engine(force)
+    build_cli(force)
 
 
 if __name__ == "__main__":

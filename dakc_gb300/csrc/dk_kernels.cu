@@ -442,7 +442,7 @@ struct LineWin {
     }
     if (w < k) sm |= sm << (k - w);
     uint32_t v = ~(uint32_t)(sm >> 32);
-    if (CH < 32) v &= (1u << CH) - 1u;
+    if (CH < 32) v &= (1u << (CH & 31)) - 1u;  // (CH & 31: no shift by 32 in the dead branch)
     if (stopped) v = 0;
     if (stp) v &= (1u << (__ffs(stp) - 1)) - 1u;
     *M = m;
