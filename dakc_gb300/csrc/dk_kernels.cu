@@ -1899,10 +1899,12 @@ __device__ bool bin_hashed(Node* nodes, uint32_t ni, const Node& nd, uint64_t* k
 // take go to a list that k_bin_count handles after it.
 #ifndef DK_PACK_SLOTS
 #define DK_PACK_SLOTS 4096
+#define DK_PACK_SLOT_BITS 12
 #define DK_PACK_MAXD 2048
 #define DK_PACK_CTAS 4
 #endif
 constexpr uint32_t kPackSlots = DK_PACK_SLOTS;        // table slots (32 KB)
+constexpr int kPackSlotBits = DK_PACK_SLOT_BITS;
 constexpr uint32_t kPackMaxDistinct = DK_PACK_MAXD;   // sorted entries (16 KB): load <= 0.5
 constexpr int kPackDigitBits = 10;                    // counting-sort digits (4 KB)
 constexpr uint32_t kPackMaxProbe = 64;
@@ -1918,20 +1920,25 @@ constexpr size_t kPackSmem = kPackSlots * 8 + kPackMaxDistinct * 8 + (4u << kPac
 static_assert(kBinCap < (1 << (64 - kPackWideShift)), "a bin's largest count fits a wide field");
 static_assert(kPackMaxDistinct * 12 <= kPackSlots * 8, "the output stage fits the table");
 static_assert(kPackSlots % (2 * kPackThreads) == 0, "slot loops");
+static_assert(kPackSlots == (1u << kPackSlotBits), "the probe cursor masks its slot");
+static_assert(kPackDigitBits <= 32, "digits come from the entry's high word");
 
 // Insert one key (rk = key << (64 - s)) with multiplicity mult: 2 when it is
 // new, 1 when it was there, 0 when the probe runs past kPackMaxProbe slots or
-// (cmax != 0: a narrow count field of at most cmax) its count would not fit.
+// (kNarrow: a count field of at most cmax) its count would not fit.  A new
+// key counts its digit, the top D bits of rk (hist[(rk >> 32) >> dsh32],
+// dsh32 = 32 - D).  The probe walks a cursor whose low bits are the slot.
 // kNarrow: the count field may carry (s > kPackWideShift); the wide form
 // skips those checks (C2: bin count 21.30 -> 21.14 ms)
 template <bool kNarrow>
 __device__ __forceinline__ int pack_insert(unsigned long long* tab, unsigned long long rk,
                                            unsigned long long himask, uint32_t mult,
-                                           uint32_t* hist, int dsh, uint32_t cmax) {
+                                           uint32_t* hist, int dsh32, uint32_t cmax) {
   if (kNarrow && mult > cmax) return 0;
-  const uint32_t h = ((uint32_t)(rk >> 32) ^ (uint32_t)rk) * 0x9E3779B1u;
-  uint32_t slot = __umulhi(h, kPackSlots);  // h scaled to [0, kPackSlots)
-  for (uint32_t probe = 0; probe < kPackMaxProbe; ++probe) {
+  const uint32_t hi = (uint32_t)(rk >> 32);
+  const uint32_t h = (hi ^ (uint32_t)rk) * 0x9E3779B1u;
+  uint32_t slot = h >> (32 - kPackSlotBits);  // h scaled to [0, kPackSlots)
+  for (const uint32_t end = slot + kPackMaxProbe; slot != end; ++slot) {
 #ifdef DK_PHASE_TIMING
     {  // probe steps: lanes (g_phase[0]) and warp iterations (g_phase[3])
       const unsigned am = __activemask();
@@ -1941,16 +1948,17 @@ __device__ __forceinline__ int pack_insert(unsigned long long* tab, unsigned lon
       }
     }
 #endif
-    unsigned long long e = *reinterpret_cast<volatile unsigned long long*>(&tab[slot]);
+    unsigned long long* const p = &tab[slot & (kPackSlots - 1)];
+    unsigned long long e = *reinterpret_cast<volatile unsigned long long*>(p);
     if (e == 0ull) {
-      e = atomicCAS(&tab[slot], 0ull, rk | mult);
+      e = atomicCAS(p, 0ull, rk | mult);
       if (e == 0ull) {
-        atomicAdd(&hist[(uint32_t)(rk >> dsh)], 1u);
+        atomicAdd(&hist[hi >> dsh32], 1u);
         return 2;
       }
     }
     if ((e & himask) == rk) {
-      unsigned int* lo = reinterpret_cast<unsigned int*>(&tab[slot]);  // the low word
+      unsigned int* lo = reinterpret_cast<unsigned int*>(p);  // the low word
       if (!kNarrow) {
         atomicAdd(lo, mult);
         return 1;
@@ -1958,9 +1966,68 @@ __device__ __forceinline__ int pack_insert(unsigned long long* tab, unsigned lon
       // a carry out of a narrow field corrupts the entry: the bin is dropped
       return (atomicAdd(lo, mult) & cmax) + mult <= cmax ? 1 : 0;
     }
-    slot = slot + 1 == kPackSlots ? 0 : slot + 1;
   }
   return 0;
+}
+
+// Insert a bin's n keys into the packed table, kPackBatch keys per thread at
+// a time.  A warp whose first 32 keys repeat one key four times or more holds
+// a hot k-mer: its copies then insert once per warp with their multiplicity.
+// flags[0] counts distinct keys (once per warp and batch); flags[1] is set
+// when the bin fails (too many distinct keys, a long probe, a full count
+// field), and every thread then stops inserting: the bin's keys are counted
+// again elsewhere.  The per-bin choices (count field, hot warp) are made
+// outside the key loop (large_100m bin count 21.12 -> 20.97 ms).  A loop
+// without per-key bounds checks for full batches issued 4.5% fewer
+// instructions and ran slower (22.83 ms), as did one batch loop whose
+// failure test moved to the batch (21.54 ms).
+template <bool kNarrow>
+__device__ __forceinline__ void pack_insert_keys(unsigned long long* tab, const uint64_t* keys,
+                                                 uint32_t n, int cbits,
+                                                 unsigned long long himask, uint32_t* hist,
+                                                 int dsh32, uint32_t cmax, uint32_t* flags) {
+  constexpr uint32_t T = kPackThreads;
+  constexpr int kBatch = kPackBatch;
+  bool hot;
+  {
+    const bool valid = threadIdx.x < n;
+    const unsigned long long rk = valid ? __ldg(keys + threadIdx.x) << cbits : 0ull;
+    const uint32_t peers = __match_any_sync(0xFFFFFFFFu, rk) & __ballot_sync(0xFFFFFFFFu, valid);
+    hot = __reduce_max_sync(0xFFFFFFFFu, valid ? (uint32_t)__popc(peers) : 0u) >= 4;
+    DK_WARP_ADD(1, hot ? 1 : 0);  // warps that aggregate (instrumented builds)
+  }
+  bool ok = true;
+  for (uint32_t i0 = 0; i0 < n; i0 += kBatch * T) {
+    if (*reinterpret_cast<volatile uint32_t*>(&flags[1])) ok = false;
+    uint32_t fresh = 0;  // new keys this batch
+    unsigned long long rk[kBatch];
+#pragma unroll
+    for (int u = 0; u < kBatch; ++u) {
+      const uint32_t i = i0 + (uint32_t)u * T + threadIdx.x;
+      rk[u] = i < n ? __ldg(keys + i) << cbits : 0ull;
+    }
+#pragma unroll
+    for (int u = 0; u < kBatch; ++u) {
+      if (i0 + (uint32_t)u * T >= n) break;  // uniform
+      const bool valid = i0 + (uint32_t)u * T + threadIdx.x < n;
+      uint32_t mult = 1;
+      bool live = valid;
+      if (hot) {  // uniform over the warp
+        const uint32_t peers =
+            __match_any_sync(0xFFFFFFFFu, rk[u]) & __ballot_sync(0xFFFFFFFFu, valid);
+        live = valid && (int)lane_id() == __ffs(peers) - 1;
+        mult = (uint32_t)__popc(peers);
+      }
+      if (live && ok) {
+        const int r = pack_insert<kNarrow>(tab, rk[u], himask, mult, hist, dsh32, cmax);
+        ok = r != 0;
+        fresh += r == 2;
+      }
+    }
+    const uint32_t wf = __reduce_add_sync(0xFFFFFFFFu, fresh);
+    if (lane_id() == 0 && wf && atomicAdd(&flags[0], wf) + wf > kPackMaxDistinct) flags[1] = 1;
+    if (!ok) flags[1] = 1;
+  }
 }
 
 // One bin with at most kBinCap keys and kDenseBits < s <= kPackMaxShift free
@@ -2004,52 +2071,10 @@ __device__ bool bin_packed(Node* nodes, uint32_t ni, const Node& nd, uint64_t* k
   }
   __syncthreads();
   DK_PHASE(11);
-  constexpr int kBatch = kPackBatch;
-  bool ok = true;
-  // a warp whose first 32 keys repeat one key four times or more holds a hot
-  // k-mer: its copies then insert once per warp with their multiplicity
-  bool hot = false;
-  for (uint32_t i0 = 0; i0 < n; i0 += kBatch * T) {
-    // a bin that has failed (too many distinct keys, a long probe, a full
-    // count field) stops inserting: its keys are counted again elsewhere
-    if (*reinterpret_cast<volatile uint32_t*>(&flags[1])) ok = false;
-    uint32_t fresh = 0;  // new keys this batch
-    unsigned long long kk[kBatch];
-#pragma unroll
-    for (int u = 0; u < kBatch; ++u) {
-      const uint32_t i = i0 + (uint32_t)u * T + threadIdx.x;
-      kk[u] = i < n ? __ldg(keys + i) : 0ull;
-    }
-#pragma unroll
-    for (int u = 0; u < kBatch; ++u) {
-      if (i0 + (uint32_t)u * T >= n) break;  // uniform
-      const bool valid = i0 + (uint32_t)u * T + threadIdx.x < n;
-      const unsigned long long rk = kk[u] << cbits;
-      uint32_t mult = 1;
-      bool live = valid;
-      if (i0 == 0 && u == 0) {
-        const uint32_t peers = __match_any_sync(0xFFFFFFFFu, rk) & __ballot_sync(0xFFFFFFFFu, valid);
-        hot = __reduce_max_sync(0xFFFFFFFFu, valid ? (uint32_t)__popc(peers) : 0u) >= 4;
-        DK_WARP_ADD(1, hot ? 1 : 0);  // warps that aggregate (instrumented builds)
-      }
-      if (hot) {  // copies of one key in this warp insert once with their multiplicity
-        const uint32_t vm = __ballot_sync(0xFFFFFFFFu, valid);
-        const uint32_t peers = __match_any_sync(0xFFFFFFFFu, rk) & vm;
-        live = valid && (int)lane_id() == __ffs(peers) - 1;
-        mult = (uint32_t)__popc(peers);
-      }
-      if (live && ok) {
-        const int r = cmax ? pack_insert<true>(tab, rk, himask, mult, hist, dsh, cmax)
-                           : pack_insert<false>(tab, rk, himask, mult, hist, dsh, cmax);
-        ok = r != 0;
-        fresh += r == 2;
-      }
-    }
-    const uint32_t wf = __reduce_add_sync(0xFFFFFFFFu, fresh);
-    if (lane_id() == 0 && wf && atomicAdd(&flags[0], wf) + wf > kPackMaxDistinct) flags[1] = 1;
-    if (!ok) flags[1] = 1;
-  }
-  if (!ok) flags[1] = 1;
+  if (cmax)
+    pack_insert_keys<true>(tab, keys, n, cbits, himask, hist, dsh - 32, cmax, flags);
+  else
+    pack_insert_keys<false>(tab, keys, n, cbits, himask, hist, dsh - 32, cmax, flags);
   __syncthreads();
   DK_PHASE(12);
   if (flags[1]) return false;
