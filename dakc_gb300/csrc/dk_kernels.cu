@@ -604,11 +604,15 @@ __global__ void __launch_bounds__(kLineThreads, 2) k_l1_lines_chunked(ExtractArg
     cursor[b] = O[(size_t)blockIdx.x * F1 + b];
     cnt2[b] = 0;
     cnt2[F1 + b] = 0;
+    coff[b] = 0;
   }
   // Bucket counts alternate between two arrays by chunk: chunk c counts in
   // cnt2[c & 1], and the next chunk advances the cursors by them (after its
   // first barrier, when every thread has finished chunk c's flush) and clears
-  // them for the chunk after.
+  // them for the chunk after.  While a chunk flushes, cursor[b] holds its
+  // bucket's output position minus the bucket's offset in the stage (modulo
+  // 2^64), so a staged key at stage index i goes to cursor[b] + i; the next
+  // chunk adds the offset back with the counts.
   int cur = 0;
   init_lut(lut, a.conv);
   __syncthreads();
@@ -702,13 +706,14 @@ __global__ void __launch_bounds__(kLineThreads, 2) k_l1_lines_chunked(ExtractArg
       }
       __syncthreads();
       for (int b = threadIdx.x; b < F1; b += blockDim.x) {
+        cursor[b] += coff[b] + cprev[b];  // the previous chunk's offset and count
         coff[b] = ccount[b];
         ccount[b] = 0;
-        cursor[b] += cprev[b];
         cprev[b] = 0;
       }
       __syncthreads();
       const uint32_t Tn = block_scan_array<uint32_t>(coff, F1, tmp);
+      for (int b = threadIdx.x; b < F1; b += blockDim.x) cursor[b] -= coff[b];
       if (MODE == kRollDakc) {
 #pragma unroll
         for (int q = 0; q < CH; ++q)
@@ -733,8 +738,7 @@ __global__ void __launch_bounds__(kLineThreads, 2) k_l1_lines_chunked(ExtractArg
       __syncthreads();
       for (uint32_t i = threadIdx.x; i < Tn; i += blockDim.x) {
         const uint64_t key = stage[i];
-        const uint32_t b = l1_bucket<kHi>(key, a.shift1);
-        keys_out[cursor[b] + (i - coff[b])] = key;
+        keys_out[cursor[l1_bucket<kHi>(key, a.shift1)] + i] = key;
       }
       cur ^= 1;
     }

@@ -169,3 +169,54 @@ def test_fastq_format(cli, tmp_path):
     keys, counts, nk = pyoracle.count(np.frombuffer(txt, np.uint8), w, 25)
     got_k, got_c = records(out)
     assert np.array_equal(got_k, keys) and np.array_equal(got_c, counts)
+
+
+@pytest.mark.gpu
+def test_fasta_pakman_convention(cli, tmp_path):
+    """FASTA reads under PakMan*'s convention; the text table names bases in
+    PakMan*'s code (A=0 C=1 T=2 G=3)."""
+    from oracle import pyoracle
+    rng = np.random.Generator(np.random.PCG64(9))
+    g = rng.choice(np.frombuffer(b"ACGT", np.uint8), 40_000)
+    reads = []
+    for i in range(1500):
+        L = int(rng.integers(50, 180))
+        s = int(rng.integers(0, g.size - L))
+        reads.append(g[s:s + L].tobytes())
+    fa = b"".join(b">r%d\n%s\n" % (i, x) for i, x in enumerate(reads))
+    path = tmp_path / "reads.fa"
+    path.write_bytes(fa)
+    out, tsv = tmp_path / "table.bin", tmp_path / "table.tsv"
+    r = run(cli, "-f", path, "-k", 19, "--format", "fasta", "--pakman", "-o", out, "--tsv", tsv)
+    assert r.returncode == 0, r.stderr
+    keys, counts, nk = pyoracle.table_of(pyoracle.pakman_kmers(fa, 19))
+    got_k, got_c = records(out)
+    assert np.array_equal(got_k, keys) and np.array_equal(got_c, counts)
+    assert figures(r.stdout)["global_kmers"] == nk
+    first = tsv.read_text().splitlines()[0]
+    x = int(keys[0])
+    assert first == "".join("ACTG"[(x >> (2 * (18 - i))) & 3] for i in range(19)) + f"\t{counts[0]}"
+
+
+@pytest.mark.gpu
+def test_table_kept_on_device(cli, tmp_path):
+    """--keep-on-device: the table stays in device memory; the histogram and
+    the filter read it there."""
+    from dakc_gb300 import synth
+    from oracle import pyoracle
+    g = synth.genome_uniform(61, 80_000)
+    text = synth.reads(62, g, 20_000, 100, 100, 100, rc_frac=0.5, err_rate=0.02)
+    reads = tmp_path / "reads.txt"
+    text.tofile(reads)
+    r = run(cli, "-f", reads, "-k", 27, "-r", 100, "--keep-on-device", "--histogram", 32,
+            "--min-count", 2)
+    assert r.returncode == 0, r.stderr
+    keys, counts, nk = pyoracle.count(text, 100, 27)
+    assert figures(r.stdout) == {"global_kmers": nk, "global_distinct_kmers": keys.size}
+    hist, cut = pyoracle.pakman_histogram_cutoff(counts, 32)
+    printed = dict(tuple(map(int, ln.split("\t"))) for ln in
+                   r.stdout.split("cut-off")[1].splitlines()[1:] if "\t" in ln)
+    assert printed == {c: int(hist[c]) for c in range(1, 32) if hist[c]}
+    keep = counts >= 2
+    assert re.search(rf"kept \(count >= 2\): {int(keep.sum())} distinct, "
+                     rf"{int(counts[keep].sum())} k-mers", r.stdout)
