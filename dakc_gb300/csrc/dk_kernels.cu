@@ -1937,8 +1937,8 @@ static_assert(kPackSlots % (2 * kPackThreads) == 0, "slot loops");
 static_assert(kPackSlots == (1u << kPackSlotBits), "the probe cursor masks its slot");
 static_assert(kPackDigitBits <= 32, "digits come from the entry's high word");
 
-// Insert one key (rk = key << (64 - s)) with multiplicity mult: 2 when it is
-// new, 1 when it was there, 0 when the probe runs past kPackMaxProbe slots or
+// Insert one occurrence of a key (rk = key << (64 - s)): 2 when it is new, 1
+// when it was there, 0 when the probe runs past kPackMaxProbe slots or
 // (kNarrow: a count field of at most cmax) its count would not fit.  A new
 // key counts its digit, the top D bits of rk (hist[(rk >> 32) >> dsh32],
 // dsh32 = 32 - D).  The probe walks a cursor whose low bits are the slot.
@@ -1946,9 +1946,8 @@ static_assert(kPackDigitBits <= 32, "digits come from the entry's high word");
 // skips those checks (C2: bin count 21.30 -> 21.14 ms)
 template <bool kNarrow>
 __device__ __forceinline__ int pack_insert(unsigned long long* tab, unsigned long long rk,
-                                           unsigned long long himask, uint32_t mult,
-                                           uint32_t* hist, int dsh32, uint32_t cmax) {
-  if (kNarrow && mult > cmax) return 0;
+                                           unsigned long long himask, uint32_t* hist, int dsh32,
+                                           uint32_t cmax) {
   const uint32_t hi = (uint32_t)(rk >> 32);
   const uint32_t h = (hi ^ (uint32_t)rk) * 0x9E3779B1u;
   uint32_t slot = h >> (32 - kPackSlotBits);  // h scaled to [0, kPackSlots)
@@ -1965,7 +1964,7 @@ __device__ __forceinline__ int pack_insert(unsigned long long* tab, unsigned lon
     unsigned long long* const p = &tab[slot & (kPackSlots - 1)];
     unsigned long long e = *reinterpret_cast<volatile unsigned long long*>(p);
     if (e == 0ull) {
-      e = atomicCAS(p, 0ull, rk | mult);
+      e = atomicCAS(p, 0ull, rk | 1ull);
       if (e == 0ull) {
         atomicAdd(&hist[hi >> dsh32], 1u);
         return 2;
@@ -1974,27 +1973,29 @@ __device__ __forceinline__ int pack_insert(unsigned long long* tab, unsigned lon
     if ((e & himask) == rk) {
       unsigned int* lo = reinterpret_cast<unsigned int*>(p);  // the low word
       if (!kNarrow) {
-        atomicAdd(lo, mult);
+        atomicAdd(lo, 1u);
         return 1;
       }
       // a carry out of a narrow field corrupts the entry: the bin is dropped
-      return (atomicAdd(lo, mult) & cmax) + mult <= cmax ? 1 : 0;
+      return (atomicAdd(lo, 1u) & cmax) + 1u <= cmax ? 1 : 0;
     }
   }
   return 0;
 }
 
-// Insert a bin's n keys into the packed table, kPackBatch keys per thread at
-// a time.  A warp whose first 32 keys repeat one key four times or more holds
-// a hot k-mer: its copies then insert once per warp with their multiplicity.
-// flags[0] counts distinct keys (once per warp and batch); flags[1] is set
-// when the bin fails (too many distinct keys, a long probe, a full count
-// field), and every thread then stops inserting: the bin's keys are counted
-// again elsewhere.  The per-bin choices (count field, hot warp) are made
-// outside the key loop (large_100m bin count 21.12 -> 20.97 ms).  A loop
-// without per-key bounds checks for full batches issued 4.5% fewer
-// instructions and ran slower (22.83 ms), as did one batch loop whose
-// failure test moved to the batch (21.54 ms).
+// Insert a bin's keys[0, n) into the packed table, kPackBatch keys per thread
+// at a time.  flags[0] counts distinct keys (once per warp and batch);
+// flags[1] is set when the bin fails (too many distinct keys, a long probe, a
+// full count field), and every thread then stops inserting: the bin's keys
+// are counted again elsewhere.  The count field's width is chosen once per
+// bin, outside the key loop.  There is no warp-wide call per key: copies of a
+// hot k-mer in one warp add to their entry one by one.  A hot-k-mer path
+// (__match_any_sync per key, copies inserted once with their multiplicity,
+// in warps whose first 32 keys repeat one key four times) made the whole
+// kernel slower even where no warp took it: large_100m bin count 17.35 ms
+// without it against 20.90-20.98 ms with it (inline, or as a second loop
+// chosen per warp); Zipf-skewed reads (k = 31, 17) 8.36 / 9.66 ms against
+// 10.45 / 12.06.  Nodes made of one hot k-mer are counted by k_bin_count.
 template <bool kNarrow>
 __device__ __forceinline__ void pack_insert_keys(unsigned long long* tab, const uint64_t* keys,
                                                  uint32_t n, int cbits,
@@ -2002,14 +2003,6 @@ __device__ __forceinline__ void pack_insert_keys(unsigned long long* tab, const 
                                                  int dsh32, uint32_t cmax, uint32_t* flags) {
   constexpr uint32_t T = kPackThreads;
   constexpr int kBatch = kPackBatch;
-  bool hot;
-  {
-    const bool valid = threadIdx.x < n;
-    const unsigned long long rk = valid ? __ldg(keys + threadIdx.x) << cbits : 0ull;
-    const uint32_t peers = __match_any_sync(0xFFFFFFFFu, rk) & __ballot_sync(0xFFFFFFFFu, valid);
-    hot = __reduce_max_sync(0xFFFFFFFFu, valid ? (uint32_t)__popc(peers) : 0u) >= 4;
-    DK_WARP_ADD(1, hot ? 1 : 0);  // warps that aggregate (instrumented builds)
-  }
   bool ok = true;
   for (uint32_t i0 = 0; i0 < n; i0 += kBatch * T) {
     if (*reinterpret_cast<volatile uint32_t*>(&flags[1])) ok = false;
@@ -2023,17 +2016,8 @@ __device__ __forceinline__ void pack_insert_keys(unsigned long long* tab, const 
 #pragma unroll
     for (int u = 0; u < kBatch; ++u) {
       if (i0 + (uint32_t)u * T >= n) break;  // uniform
-      const bool valid = i0 + (uint32_t)u * T + threadIdx.x < n;
-      uint32_t mult = 1;
-      bool live = valid;
-      if (hot) {  // uniform over the warp
-        const uint32_t peers =
-            __match_any_sync(0xFFFFFFFFu, rk[u]) & __ballot_sync(0xFFFFFFFFu, valid);
-        live = valid && (int)lane_id() == __ffs(peers) - 1;
-        mult = (uint32_t)__popc(peers);
-      }
-      if (live && ok) {
-        const int r = pack_insert<kNarrow>(tab, rk[u], himask, mult, hist, dsh32, cmax);
+      if (i0 + (uint32_t)u * T + threadIdx.x < n && ok) {
+        const int r = pack_insert<kNarrow>(tab, rk[u], himask, hist, dsh32, cmax);
         ok = r != 0;
         fresh += r == 2;
       }
