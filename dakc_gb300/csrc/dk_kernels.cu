@@ -1937,15 +1937,15 @@ static_assert(kPackSlots % (2 * kPackThreads) == 0, "slot loops");
 static_assert(kPackSlots == (1u << kPackSlotBits), "the probe cursor masks its slot");
 static_assert(kPackDigitBits <= 32, "digits come from the entry's high word");
 
-// Insert one occurrence of a key (rk = key << (64 - s)): 2 when it is new, 1
-// when it was there, 0 when the probe runs past kPackMaxProbe slots or
-// (kNarrow: a count field of at most cmax) its count would not fit.  A new
+// Insert one occurrence of a key (rk = key << (64 - s)); false when the probe
+// runs past kPackMaxProbe slots or (kNarrow: a count field of at most cmax)
+// its count would not fit.  A new
 // key counts its digit, the top D bits of rk (hist[(rk >> 32) >> dsh32],
 // dsh32 = 32 - D).  The probe walks a cursor whose low bits are the slot.
 // kNarrow: the count field may carry (s > kPackWideShift); the wide form
 // skips those checks (C2: bin count 21.30 -> 21.14 ms)
 template <bool kNarrow>
-__device__ __forceinline__ int pack_insert(unsigned long long* tab, unsigned long long rk,
+__device__ __forceinline__ bool pack_insert(unsigned long long* tab, unsigned long long rk,
                                            unsigned long long himask, uint32_t* hist, int dsh32,
                                            uint32_t cmax) {
   const uint32_t hi = (uint32_t)(rk >> 32);
@@ -1967,35 +1967,38 @@ __device__ __forceinline__ int pack_insert(unsigned long long* tab, unsigned lon
       e = atomicCAS(p, 0ull, rk | 1ull);
       if (e == 0ull) {
         atomicAdd(&hist[hi >> dsh32], 1u);
-        return 2;
+        return true;
       }
     }
     if ((e & himask) == rk) {
       unsigned int* lo = reinterpret_cast<unsigned int*>(p);  // the low word
       if (!kNarrow) {
         atomicAdd(lo, 1u);
-        return 1;
+        return true;
       }
       // a carry out of a narrow field corrupts the entry: the bin is dropped
-      return (atomicAdd(lo, 1u) & cmax) + 1u <= cmax ? 1 : 0;
+      return (atomicAdd(lo, 1u) & cmax) + 1u <= cmax;
     }
   }
-  return 0;
+  return false;
 }
 
 // Insert a bin's keys[0, n) into the packed table, kPackBatch keys per thread
-// at a time.  flags[0] counts distinct keys (once per warp and batch);
-// flags[1] is set when the bin fails (too many distinct keys, a long probe, a
-// full count field), and every thread then stops inserting: the bin's keys
-// are counted again elsewhere.  The count field's width is chosen once per
-// bin, outside the key loop.  There is no warp-wide call per key: copies of a
-// hot k-mer in one warp add to their entry one by one.  A hot-k-mer path
-// (__match_any_sync per key, copies inserted once with their multiplicity,
-// in warps whose first 32 keys repeat one key four times) made the whole
-// kernel slower even where no warp took it: large_100m bin count 17.35 ms
-// without it against 20.90-20.98 ms with it (inline, or as a second loop
-// chosen per warp); Zipf-skewed reads (k = 31, 17) 8.36 / 9.66 ms against
-// 10.45 / 12.06.  Nodes made of one hot k-mer are counted by k_bin_count.
+// at a time.  flags[1] is set when the bin fails (a long probe, a full count
+// field), and every thread then stops inserting at its next batch: the bin's
+// keys are counted again elsewhere.  A bin with more distinct keys than the
+// sorted stage holds is caught after the digit scan, and a full table ends
+// every probe at kPackMaxProbe slots, so nothing is tallied per batch (a
+// per-warp tally of new keys cost 17.34 against 16.73 ms on large_100m).  The
+// count field's width is chosen once per bin, outside the key loop.  There is
+// no warp-wide call per key either: copies of a hot k-mer in one warp add to
+// their entry one by one.  A hot-k-mer path (__match_any_sync per key, copies
+// inserted once with their multiplicity, in warps whose first 32 keys repeat
+// one key four times) made the whole kernel slower even where no warp took
+// it: large_100m bin count 17.35 ms without it against 20.90-20.98 ms with it
+// (inline, or as a second loop chosen per warp); Zipf-skewed reads (k = 31,
+// 17) 8.36 / 9.66 ms against 10.45 / 12.06.  Nodes made of one hot k-mer are
+// counted by k_bin_count.
 template <bool kNarrow>
 __device__ __forceinline__ void pack_insert_keys(unsigned long long* tab, const uint64_t* keys,
                                                  uint32_t n, int cbits,
@@ -2006,7 +2009,6 @@ __device__ __forceinline__ void pack_insert_keys(unsigned long long* tab, const 
   bool ok = true;
   for (uint32_t i0 = 0; i0 < n; i0 += kBatch * T) {
     if (*reinterpret_cast<volatile uint32_t*>(&flags[1])) ok = false;
-    uint32_t fresh = 0;  // new keys this batch
     unsigned long long rk[kBatch];
 #pragma unroll
     for (int u = 0; u < kBatch; ++u) {
@@ -2016,14 +2018,9 @@ __device__ __forceinline__ void pack_insert_keys(unsigned long long* tab, const 
 #pragma unroll
     for (int u = 0; u < kBatch; ++u) {
       if (i0 + (uint32_t)u * T >= n) break;  // uniform
-      if (i0 + (uint32_t)u * T + threadIdx.x < n && ok) {
-        const int r = pack_insert<kNarrow>(tab, rk[u], himask, hist, dsh32, cmax);
-        ok = r != 0;
-        fresh += r == 2;
-      }
+      if (i0 + (uint32_t)u * T + threadIdx.x < n && ok)
+        ok = pack_insert<kNarrow>(tab, rk[u], himask, hist, dsh32, cmax);
     }
-    const uint32_t wf = __reduce_add_sync(0xFFFFFFFFu, fresh);
-    if (lane_id() == 0 && wf && atomicAdd(&flags[0], wf) + wf > kPackMaxDistinct) flags[1] = 1;
     if (!ok) flags[1] = 1;
   }
 }
@@ -2063,10 +2060,7 @@ __device__ bool bin_packed(Node* nodes, uint32_t ni, const Node& nd, uint64_t* k
   }
   for (uint32_t j = threadIdx.x; j < R; j += T) hist[j] = 0;
   for (uint32_t w = threadIdx.x; w < (R + 31) / 32; w += T) mark[w] = 0;
-  if (threadIdx.x == 0) {
-    flags[0] = 0;  // distinct keys so far (updated once per warp and batch)
-    flags[1] = 0;  // the bin has failed
-  }
+  if (threadIdx.x == 0) flags[1] = 0;  // the bin has failed
   __syncthreads();
   DK_PHASE(11);
   if (cmax)
