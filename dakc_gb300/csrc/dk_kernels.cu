@@ -2048,7 +2048,7 @@ __device__ bool bin_packed(Node* nodes, uint32_t ni, const Node& nd, uint64_t* k
   int D = ceil_log2_u64(n) - 3;
   D = max(4, min(D, kPackDigitBits));
   D = min(D, s);
-  const int dsh = 64 - D;
+  const int dsh32 = 32 - D;  // an entry's digit: its high word >> dsh32
   const uint32_t R = 1u << D;
   const uint64_t prefix = n ? (__ldg(keys) >> s) << s : 0ull;
   DK_PHASE_BEGIN();
@@ -2064,9 +2064,9 @@ __device__ bool bin_packed(Node* nodes, uint32_t ni, const Node& nd, uint64_t* k
   __syncthreads();
   DK_PHASE(11);
   if (cmax)
-    pack_insert_keys<true>(tab, keys, n, cbits, himask, hist, dsh - 32, cmax, flags);
+    pack_insert_keys<true>(tab, keys, n, cbits, himask, hist, dsh32, cmax, flags);
   else
-    pack_insert_keys<false>(tab, keys, n, cbits, himask, hist, dsh - 32, cmax, flags);
+    pack_insert_keys<false>(tab, keys, n, cbits, himask, hist, dsh32, cmax, flags);
   __syncthreads();
   DK_PHASE(12);
   if (flags[1]) return false;
@@ -2079,8 +2079,8 @@ __device__ bool bin_packed(Node* nodes, uint32_t ni, const Node& nd, uint64_t* k
 #pragma unroll
     for (uint32_t u = 0; u < kPackSlots / 2 / T; ++u) {
       const ulonglong2 e = t2[threadIdx.x + u * T];
-      if (e.x) sorted[atomicAdd(&hist[(uint32_t)(e.x >> dsh)], 1u)] = e.x;
-      if (e.y) sorted[atomicAdd(&hist[(uint32_t)(e.y >> dsh)], 1u)] = e.y;
+      if (e.x) sorted[atomicAdd(&hist[(uint32_t)(e.x >> 32) >> dsh32], 1u)] = e.x;
+      if (e.y) sorted[atomicAdd(&hist[(uint32_t)(e.y >> 32) >> dsh32], 1u)] = e.y;
     }
   }
   __syncthreads();
@@ -2091,7 +2091,7 @@ __device__ bool bin_packed(Node* nodes, uint32_t ni, const Node& nd, uint64_t* k
   uint32_t* oc = reinterpret_cast<uint32_t*>(tab + d);    // d counts
   for (uint32_t x = threadIdx.x; x < d; x += T) {
     const unsigned long long v = sorted[x];
-    const uint32_t j = (uint32_t)(v >> dsh);
+    const uint32_t j = (uint32_t)(v >> 32) >> dsh32;
     const uint32_t lo = j ? hist[j - 1] : 0, hi = hist[j];
     if (hi - lo > kRankMax) {
       atomicOr(&mark[j >> 5], 1u << (j & 31));
