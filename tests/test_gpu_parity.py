@@ -163,6 +163,22 @@ def test_skew_heavy_hitters(engine, variant):
 
 
 @pytest.mark.parametrize("variant", VARIANTS)
+def test_one_kmer_dominates_a_normal_bin(engine, variant):
+    """A k-mer with about 2,000 copies among 24 M background k-mers: its bin is
+    a normal one (its node is far from half of its parent), so the packed
+    table takes it, and its copies add to one entry lane by lane."""
+    W = 150
+    g = synth.genome_uniform(31, 3_000_000)
+    bg = synth.reads(32, g, 200_000, 150, 150, W, rc_frac=0.5, err_rate=0.01)
+    hot = np.frombuffer(lines(b"A" * 150, W=150) * 17, dtype=np.uint8)
+    text = np.concatenate([bg[: 1000 * (W + 1)], hot, bg[1000 * (W + 1):]])
+    got = check(engine, text, W, 31, variant)
+    a31 = int("01" * 31, 2)
+    i = int(np.searchsorted(got.kmers, np.uint64(a31)))
+    assert got.kmers[i] == a31 and got.counts[i] >= 17 * 120
+
+
+@pytest.mark.parametrize("variant", VARIANTS)
 def test_two_partition_levels(engine, variant):
     # > 4096 * 6144 k-mers forces the 8-bit partition level below level 1
     g = synth.genome_uniform(21, 30_000_000)
