@@ -1948,11 +1948,11 @@ static_assert(kPackDigitBits <= 32, "digits come from the entry's high word");
 
 // Insert one occurrence of a key (rk = key << (64 - s)); false when the probe
 // runs past kPackMaxProbe slots or (kNarrow: a count field of at most cmax)
-// its count would not fit.  A new
-// key counts its digit, the top D bits of rk (hist[(rk >> 32) >> dsh32],
-// dsh32 = 32 - D).  The probe walks a cursor whose low bits are the slot.
-// kNarrow: the count field may carry (s > kPackWideShift); the wide form
-// skips those checks (C2: bin count 21.30 -> 21.14 ms)
+// its count would not fit.  A new key enters with count 1 and counts its
+// digit, the top D bits of rk (hist[(rk >> 32) >> dsh32], dsh32 = 32 - D).
+// The probe walks a cursor whose low bits are the slot.  kNarrow: the count
+// field may carry (s > kPackWideShift; cmax >= 3, since s <= kPackMaxShift);
+// the wide form skips those checks (C2: bin count 21.30 -> 21.14 ms).
 template <bool kNarrow>
 __device__ __forceinline__ bool pack_insert(unsigned long long* tab, unsigned long long rk,
                                            unsigned long long himask, uint32_t* hist, int dsh32,
