@@ -591,12 +591,6 @@ def main():
     nbytes = rs.text.size
     variant = {"auto": dk.VARIANT_AUTO, "sort": dk.VARIANT_SORT, "hash": dk.VARIANT_HASH}[args.variant]
 
-    # CPU baseline first (rank 0, N=1 only), before the GPU is busy
-    cpu = None
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        cpu = run_cpu(rs, cpu_reads_for(rs, args.cpu_reads, args.cpu_steps), args.cpu_steps, 0,
-                      os.cpu_count() or 1)
-
     eng = dk.Engine(local)
     d_text = torch.empty(nbytes + 64, dtype=torch.uint8, device=f"cuda:{local}")
     d_text[:nbytes].copy_(torch.from_numpy(rs.text))
@@ -730,6 +724,15 @@ def main():
                          "device in both arms; served: Poisson 2,000 jobs/s (the top offered "
                          "rate; --mode serve sweeps 10-2,000), 2 workers in both arms, "
                          f"{args.mem_budget_gb:g} GB admission budget"}
+
+    # CPU baseline last (rank 0, N=1 only), once the GPU is idle: its tens of
+    # GB of host buffers are allocated and freed after the end-to-end calls,
+    # whose copies share the host's memory (run first, they were followed by
+    # slower copies in some of those calls)
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = run_cpu(rs, cpu_reads_for(rs, args.cpu_reads, args.cpu_steps), args.cpu_steps, 0,
+                      os.cpu_count() or 1)
 
     if rank == 0:
         line = {
