@@ -35,30 +35,45 @@ __device__ __forceinline__ void init_lut(uint8_t* lut, int conv = 0) {
 
 // Walk one line with one warp.  Lane i owns positions seg + i*C .. seg + i*C + C-1.
 // f(t, key, valid) is called for t = 0..C-1 (once per segment of 32*C positions).
-template <int C, typename F>
+// CONV 0: DAKC's rules (codes 0-3, 0xFF splits the run, 0xF0 ends the line).
+// CONV 1: PakMan*'s (kmer = ((kmer << 2) | code) & mask with 3-bit codes,
+// Sliding_window, pakman_star/src/kmer_counting.cpp:313-341): nothing splits
+// a run, '\n' (0xF0) ends the read, and a k-mer ends at every position from
+// the k-th.  A code's bit 2 lands on bit 0 of the slot before it, so the key
+// is the 2-bit window of the codes' low bits OR'ed with a second window of
+// their bit 2, one slot up; both windows are carried across lanes alike.
+template <int C, int CONV = 0, typename F>
 __device__ __forceinline__ void warp_line_kmers(const uint8_t* __restrict__ line, int W, int k,
                                                 uint64_t kmask, const uint8_t* __restrict__ lut,
                                                 F&& f) {
   const uint32_t lane = lane_id();
   constexpr int B = 2 * C;  // bits per lane chunk
-  uint64_t carry_win = 0;
+  uint64_t carry_win = 0, carry_sp = 0;
   int carry_lb = -1;
   int carry_stop = W;
   // k = 1 keeps a final run only if it starts before W-1 (kcounter_funcs.cpp:97)
-  const bool k1_drop_last = (k == 1) && (W == 1 || lut[line[W - 2]] == 0xFF);
+  const bool k1_drop_last = CONV == 0 && (k == 1) && (W == 1 || lut[line[W - 2]] == 0xFF);
   for (int seg = 0; seg < W; seg += 32 * C) {
     const int p0 = seg + (int)lane * C;
-    uint64_t chunk = 0;
+    uint64_t chunk = 0, spill = 0;
     int lb_lane = -1, firstM = 0x7FFFFFFF;
     uint32_t bad_mask = 0;  // bit t: position p0+t is not a base
 #pragma unroll
     for (int t = 0; t < C; ++t) {
       const int p = p0 + t;
-      uint8_t c = 0xFF;
-      if (p < W) c = lut[line[p]];  // shared-memory tile or global line
-      chunk = (chunk << 2) | (c & 3u);
-      if (c >= 4) { lb_lane = p; bad_mask |= (1u << t); }
-      if (c == 0xF0 && firstM == 0x7FFFFFFF) firstM = p;
+      if (CONV == 0) {
+        uint8_t c = 0xFF;
+        if (p < W) c = lut[line[p]];  // shared-memory tile or global line
+        chunk = (chunk << 2) | (c & 3u);
+        if (c >= 4) { lb_lane = p; bad_mask |= (1u << t); }
+        if (c == 0xF0 && firstM == 0x7FFFFFFF) firstM = p;
+      } else {
+        const uint32_t c = p < W ? lut[line[p]] : 0u;  // past the line: never a key's
+        const bool end = c == 0xF0u;
+        chunk = (chunk << 2) | (end ? 0u : (c & 3u));
+        spill = (spill << 2) | (end ? 0u : (c >> 2));
+        if (end && firstM == 0x7FFFFFFF) firstM = p;
+      }
     }
     // first 'M' over the warp
     int m = firstM;
@@ -67,32 +82,49 @@ __device__ __forceinline__ void warp_line_kmers(const uint8_t* __restrict__ line
     const int stop = min(carry_stop, m);
     // last non-base position before this lane's chunk (exclusive max scan)
     int lb_inc = lb_lane;
+    if (CONV == 0) {
 #pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const int v = __shfl_up_sync(0xFFFFFFFFu, lb_inc, o);
-      if ((int)lane >= o) lb_inc = max(lb_inc, v);
+      for (int o = 1; o < 32; o <<= 1) {
+        const int v = __shfl_up_sync(0xFFFFFFFFu, lb_inc, o);
+        if ((int)lane >= o) lb_inc = max(lb_inc, v);
+      }
     }
-    int lb_exc = __shfl_up_sync(0xFFFFFFFFu, lb_inc, 1);
-    if (lane == 0) lb_exc = -1;
-    lb_exc = max(lb_exc, carry_lb);
+    int lb_exc = -1;
+    if (CONV == 0) {
+      lb_exc = __shfl_up_sync(0xFFFFFFFFu, lb_inc, 1);
+      if (lane == 0) lb_exc = -1;
+      lb_exc = max(lb_exc, carry_lb);
+    }
     // 2-bit window of all bases before this lane's chunk (exclusive shift-or scan)
-    uint64_t w_inc = chunk;
+    uint64_t w_inc = chunk, s_inc = spill;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
       const uint64_t v = __shfl_up_sync(0xFFFFFFFFu, w_inc, o);
       if ((int)lane >= o && B * o < 64) w_inc |= v << (B * o);
+      if (CONV != 0) {
+        const uint64_t sv = __shfl_up_sync(0xFFFFFFFFu, s_inc, o);
+        if ((int)lane >= o && B * o < 64) s_inc |= sv << (B * o);
+      }
     }
     uint64_t w_exc = __shfl_up_sync(0xFFFFFFFFu, w_inc, 1);
     if (lane == 0) w_exc = 0;
     if (B * (int)lane < 64) w_exc |= carry_win << (B * lane);
+    uint64_t s_exc = 0;
+    if (CONV != 0) {
+      s_exc = __shfl_up_sync(0xFFFFFFFFu, s_inc, 1);
+      if (lane == 0) s_exc = 0;
+      if (B * (int)lane < 64) s_exc |= carry_sp << (B * lane);
+    }
     // k-mers ending at each of this lane's positions
     int lb = lb_exc;
 #pragma unroll
     for (int t = 0; t < C; ++t) {
       const int p = p0 + t;
-      if (bad_mask & (1u << t)) lb = p;
+      if (CONV == 0 && (bad_mask & (1u << t))) lb = p;
       const int up = 2 * (t + 1);
-      const uint64_t win = (up < 64 ? (w_exc << up) : 0ull) | (chunk >> (2 * (C - 1 - t)));
+      uint64_t win = (up < 64 ? (w_exc << up) : 0ull) | (chunk >> (2 * (C - 1 - t)));
+      if (CONV != 0)
+        win |= ((up < 64 ? (s_exc << up) : 0ull) | (spill >> (2 * (C - 1 - t)))) << 2;
       const uint64_t key = win & kmask;
       bool valid = (p < stop) && (p - lb >= k);
       if (k1_drop_last && p == W - 1) valid = false;
@@ -101,7 +133,11 @@ __device__ __forceinline__ void warp_line_kmers(const uint8_t* __restrict__ line
     // carry to the next segment
     const uint64_t win_all = __shfl_sync(0xFFFFFFFFu, w_inc, 31);
     carry_win = (B * 32 < 64) ? ((carry_win << (B * 32)) | win_all) : win_all;
-    carry_lb = max(carry_lb, __shfl_sync(0xFFFFFFFFu, lb_inc, 31));
+    if (CONV != 0) {
+      const uint64_t sp_all = __shfl_sync(0xFFFFFFFFu, s_inc, 31);
+      carry_sp = (B * 32 < 64) ? ((carry_sp << (B * 32)) | sp_all) : sp_all;
+    }
+    if (CONV == 0) carry_lb = max(carry_lb, __shfl_sync(0xFFFFFFFFu, lb_inc, 31));
     carry_stop = stop;
   }
 }

@@ -229,10 +229,10 @@ int Engine::write_small(void* ddst, const void* hsrc, size_t bytes) {
   return DK_OK;
 }
 
-// DAKC's convention for any line width; PakMan*'s on the thread-per-line
-// kernels (lines of at most kLineMaxW bytes)
+// DAKC's and PakMan*'s conventions, for any line width (thread-per-line
+// kernels up to kLineMaxW bytes, warp-per-line kernels beyond)
 bool convention_ok(const dk_input_desc& d) {
-  return d.convention == DK_CONV_DAKC || (d.convention == DK_CONV_PAKMAN && d.line_width <= kLineMaxW);
+  return d.convention == DK_CONV_DAKC || d.convention == DK_CONV_PAKMAN;
 }
 
 // framing: lines in a buffer of nbytes (host-side part; NUL lines are found on device)

@@ -131,7 +131,7 @@ int Engine::count_format(const char* text, uint64_t nbytes, int format, const dk
     return DK_ERR_INVALID_ARG;
   }
   std::memset(out, 0, sizeof(*out));
-  const int max_w = desc->convention == DK_CONV_PAKMAN ? kLineMaxW : 1024;
+  const int max_w = 1024;
   // input lines: newline-terminated, the last one may lack its newline
   const bool last_nl = nbytes && text[nbytes - 1] == '\n';
   // FASTA: the reads start after the line holding the first '>'

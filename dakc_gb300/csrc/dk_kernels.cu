@@ -169,8 +169,9 @@ __device__ __forceinline__ void tile_jobs(const ExtractArgs& a, uint64_t l0, uin
   __syncthreads();
 }
 
-// counters[0] = k-mers, [1] = n_lines - (first NUL-led line), [3] = device error
-template <int C>
+// counters[0] = k-mers, [1] = n_lines - (first NUL-led line), [3] = device error.
+// CONV: the k-mer convention (0 DAKC, 1 PakMan*), a kernel of its own each.
+template <int C, int CONV>
 __global__ void __launch_bounds__(512) k_l1_count(ExtractArgs a, uint32_t* __restrict__ H,
                                                   unsigned long long* __restrict__ counters,
                                                   uint32_t lt) {
@@ -196,7 +197,7 @@ __global__ void __launch_bounds__(512) k_l1_count(ExtractArgs a, uint32_t* __res
     fence_barrier_init();
   }
   for (int b = threadIdx.x; b < a.F1; b += blockDim.x) hist[b] = 0;
-  init_lut(lut);
+  init_lut(lut, a.conv);
   __syncthreads();
   const uint32_t warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   const uint32_t nt = T.ntiles();
@@ -221,16 +222,18 @@ __global__ void __launch_bounds__(512) k_l1_count(ExtractArgs a, uint32_t* __res
           atomicMax(&counters[1], 1ull);
         }
         const JobBucket jb(a, job);
-        warp_line_kmers<C>(line, a.W, a.k, a.kmask, lut, [&](int, uint64_t key, bool valid) {
+        auto on_kmer = [&](int, uint64_t key, bool valid) {
           if (valid) { atomicAdd(&hist[jb(key)], 1u); ++mine; }
-        });
+        };
+        warp_line_kmers<C, CONV>(line, a.W, a.k, a.kmask, lut, on_kmer);
         continue;
       }
       if (lane_id() == 0 && a.line_base + l > 0 && line[0] == 0)
         atomicMax(&counters[1], a.lines_total - (a.line_base + l));
-      warp_line_kmers<C>(line, a.W, a.k, a.kmask, lut, [&](int, uint64_t key, bool valid) {
+      auto on_kmer = [&](int, uint64_t key, bool valid) {
         if (valid) { atomicAdd(&hist[key >> a.shift1], 1u); ++mine; }
-      });
+      };
+      warp_line_kmers<C, CONV>(line, a.W, a.k, a.kmask, lut, on_kmer);
     }
     __syncthreads();
   }
@@ -820,7 +823,7 @@ __global__ void __launch_bounds__(kLineThreads) k_l1_lines_direct(ExtractArgs a,
   }
 }
 
-template <int C, int LPW>
+template <int C, int LPW, int CONV>
 __global__ void __launch_bounds__(512, 2) k_l1_scatter(ExtractArgs a, const uint64_t* __restrict__ O,
                                                     uint64_t* __restrict__ keys_out,
                                                     int stage_cap,
@@ -858,7 +861,7 @@ __global__ void __launch_bounds__(512, 2) k_l1_scatter(ExtractArgs a, const uint
     cursor[b] = O[(size_t)blockIdx.x * F1 + b];
     tile_hist[b] = 0;
   }
-  init_lut(lut);
+  init_lut(lut, a.conv);
   __syncthreads();
   const uint32_t warp = threadIdx.x >> 5;
   const uint32_t nt = T.ntiles();
@@ -887,13 +890,12 @@ __global__ void __launch_bounds__(512, 2) k_l1_scatter(ExtractArgs a, const uint
       if (live) {
         if (a.njobs) jbr[j] = JobBucket(a, job);
         const JobBucket jb = jbr[j];
-        warp_line_kmers<C>(base + (l - t0) * stride, a.W, a.k, a.kmask, lut,
-                           [&](int t, uint64_t key, bool valid) {
-                             kr[j][t] = key;
-                             const uint32_t bkt =
-                                 a.njobs ? jb(key) : (uint32_t)(key >> a.shift1);
-                             sr[j][t] = valid ? atomicAdd(&tile_hist[bkt], 1u) : 0xFFFFFFFFu;
-                           });
+        auto on_kmer = [&](int t, uint64_t key, bool valid) {
+          kr[j][t] = key;
+          const uint32_t bkt = a.njobs ? jb(key) : (uint32_t)(key >> a.shift1);
+          sr[j][t] = valid ? atomicAdd(&tile_hist[bkt], 1u) : 0xFFFFFFFFu;
+        };
+        warp_line_kmers<C, CONV>(base + (l - t0) * stride, a.W, a.k, a.kmask, lut, on_kmer);
       } else {
 #pragma unroll
         for (int t = 0; t < C; ++t) { kr[j][t] = 0; sr[j][t] = 0xFFFFFFFFu; }
@@ -2751,8 +2753,9 @@ static void count_launch(const ExtractArgs& a, int grid, uint32_t* H, unsigned l
   const uint64_t stride = (uint64_t)a.W + 1;
   const uint32_t lt = (uint32_t)std::max<uint64_t>(16, std::min<uint64_t>(128, 16384 / stride));
   const size_t smem = 128 + 2 * (size_t)tile_buf_bytes(lt, stride) + (size_t)a.F1 * 4 + 256;
-  allow_max_smem(k_l1_count<C>);
-  k_l1_count<C><<<grid, 512, smem, s>>>(a, H, counters, lt);
+  auto* kern = a.conv == 1 ? k_l1_count<C, 1> : k_l1_count<C, 0>;
+  allow_max_smem(kern);
+  kern<<<grid, 512, smem, s>>>(a, H, counters, lt);
 }
 
 static size_t lines_smem(const ExtractArgs& a, bool scatter) {
@@ -2868,8 +2871,9 @@ static void scatter_launch(const ExtractArgs& a, int grid, const uint64_t* O, ui
   const int stage_cap = (int)lt * 32 * C;  // >= k-mers of one tile
   static_assert(LPW == (C <= 2 ? 4 : (C <= 8 ? 2 : 1)), "scatter_smem mirrors this tiling");
   const size_t smem = scatter_smem(a.W, a.F1, a.njobs != 0);
-  allow_max_smem(k_l1_scatter<C, LPW>);
-  k_l1_scatter<C, LPW><<<grid, threads, smem, s>>>(a, O, keys, stage_cap, counters);
+  auto* kern = a.conv == 1 ? k_l1_scatter<C, LPW, 1> : k_l1_scatter<C, LPW, 0>;
+  allow_max_smem(kern);
+  kern<<<grid, threads, smem, s>>>(a, O, keys, stage_cap, counters);
 }
 
 // the chunked scatter for roll mode m

@@ -68,8 +68,7 @@ extern "C" {
                               distribute_kmers.h), nothing splits a run, a read
                               ends at '\n' (padding), and a k-mer ends at each
                               position from the k-th (Sliding_window,
-                              pakman_star/src/kmer_counting.cpp:283-341).  Lines
-                              of at most 256 bytes.                                */
+                              pakman_star/src/kmer_counting.cpp:283-341).        */
 
 /* where dk_count leaves the table */
 #define DK_RESIDENT_HOST 0   /* kmers/counts are host arrays owned by the context  */

@@ -88,8 +88,44 @@ def test_format_edge_cases(engine):
     assert r.n_kmers == 0
     with pytest.raises(dk.DkError):       # a read longer than the line width asked for
         engine.count_format(b"ACGTACGTAC\n", dk.FORMAT_LINES, 3, dk.CONV_DAKC, line_width=5)
-    with pytest.raises(dk.DkError):       # PakMan* lines are limited to 256 bytes
-        engine.count_format(b">h\n" + b"A" * 300 + b"\n", dk.FORMAT_FASTA, 3, dk.CONV_PAKMAN)
+    with pytest.raises(dk.DkError):       # reads of more than 1,024 bytes
+        engine.count_format(b">h\n" + b"A" * 1100 + b"\n", dk.FORMAT_FASTA, 3, dk.CONV_PAKMAN)
+
+
+@pytest.mark.parametrize("k", [11, 25, 32])
+def test_fasta_pakman_long_reads(engine, k):
+    """Reads of 257-1,024 bytes under PakMan*'s convention take the
+    warp-per-line kernels: exact against the oracle's restatement of
+    PakMan*'s FASTA walk, both variants."""
+    reads = var_reads(7, 600, lo=257, hi=1024)
+    fa = fasta(reads)
+    keys, counts, nk = pyoracle.table_of(pyoracle.pakman_kmers(fa, k))
+    for variant in (dk.VARIANT_HASH, dk.VARIANT_SORT):
+        if k == 32 and variant == dk.VARIANT_HASH:
+            continue  # k = 32 always sorts
+        r, width = engine.count_format(fa, dk.FORMAT_FASTA, k, dk.CONV_PAKMAN, variant=variant)
+        assert width == max(len(x) for x in reads)
+        assert r.n_kmers == nk and np.array_equal(r.kmers, keys) and np.array_equal(r.counts, counts)
+
+
+def test_pakman_long_fixed_lines(engine):
+    """dk_count on fixed-width lines of 700 bytes under PakMan*'s
+    convention: reads shorter than the width end at their '\\n' padding."""
+    reads = var_reads(8, 400, lo=100, hi=700)
+    text = b"".join(x + b"\n" * (700 - len(x)) + b"\n" for x in reads)
+    keys, counts, nk = pyoracle.table_of(pyoracle.pakman_kmers(fasta(reads), 21))
+    d = dk.Engine.desc(700, 21, dk.VARIANT_HASH)
+    d.convention = dk.CONV_PAKMAN
+    buf = np.frombuffer(text, np.uint8)
+    t = engine.count_raw(buf.ctypes.data, buf.size, d)
+    try:
+        n = int(t.n)
+        got_k = np.ctypeslib.as_array(t.kmers, shape=(n,)).copy()
+        got_c = np.ctypeslib.as_array(t.counts, shape=(n,)).copy()
+        assert int(t.n_kmers) == nk
+    finally:
+        engine.free_table(t)
+    assert np.array_equal(got_k, keys) and np.array_equal(got_c, counts)
 
 
 import glob  # noqa: E402
