@@ -229,8 +229,8 @@ int Engine::write_small(void* ddst, const void* hsrc, size_t bytes) {
   return DK_OK;
 }
 
-// DAKC's and PakMan*'s conventions, for any line width (thread-per-line
-// kernels up to kLineMaxW bytes, warp-per-line kernels beyond)
+// DAKC's and PakMan*'s conventions, at every line width the engine takes
+// (thread-per-line kernels up to kLineMaxW bytes, warp-per-line kernels beyond)
 bool convention_ok(const dk_input_desc& d) {
   return d.convention == DK_CONV_DAKC || d.convention == DK_CONV_PAKMAN;
 }
