@@ -2284,7 +2284,11 @@ __global__ void __launch_bounds__(kBinThreads, kBinBlocksPerSM) k_bin_count(Node
         if (!done && threadIdx.x == 0) atomicAdd(&ctr[6], 1ull);  // bins that fell back
         __syncthreads();
       }
-      if (!done) bin_sorted(nodes, ni, nd, keys, cnt, skeys, hist, tmp, mark, defer, &n_defer, hot);
+      // the sort path counts its digits without per-warp aggregation: a bin
+      // here holds at most kBinCap keys, so a hot k-mer's adds stay few, and
+      // the aggregated form made every bin slower (large_100m, sort variant:
+      // 92.7 -> 89.8 ms; Zipf k = 31: 20.1 -> 18.7 ms)
+      if (!done) bin_sorted(nodes, ni, nd, keys, cnt, skeys, hist, tmp, mark, defer, &n_defer, false);
     }
     __syncthreads();
   }
